@@ -1,0 +1,264 @@
+"""GB300-native voxel-network builder (BNAPlatform's correlation -> CSR ->
+eigenvector-centrality path), Python host side over the C ABI of libbna.so.
+
+Mapping to the reference (W/ = BNAPlatform-weighted-win64-cuda7.0-20160331/src):
+
+  Builder.corr_csr     CorMat_gpu + post_block + FormFullGraph(_s) + FormCSRGraph
+                       (W/CorMat/CUCorMat/CUCorMat/CorMat.cu:17, CorMat.cpp:683-918)
+  Builder.ec           Lead_Vector_GPU (W/CUEC/weighted-net.cu:55-221)
+  Builder.lead_vector  the same with host buffers and the reference's argument list
+  csr_write / csr_read the .csr format (CorMat.cpp:353-360, weighted-net.cu:275-287)
+
+Device buffers are torch CUDA tensors (torch is plumbing for memory and
+streams only); every computation runs in libbna.so's sm_103a kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import BnaError, lib
+
+__all__ = ["Builder", "CsrResult", "synth_bold", "csr_write", "csr_read", "ec_write",
+           "BnaError", "lib"]
+
+
+def _check(status: int, ctx=None, ok=(L.BNA_OK,)) -> int:
+    if status not in ok:
+        msg = lib().bna_ctx_last_error(ctx).decode() if ctx else ""
+        raise BnaError(status, msg)
+    return status
+
+
+def synth_bold(N: int, T: int, K: int, seed: int, kind: str = "iid", phi: float = 0.7,
+               load_sd: float = 0.3, jitter_sd: float = 0.0, block: int = 500,
+               n_net: int = 60, threads: int = 0) -> np.ndarray:
+    """Deterministic factor-model BOLD, float32 time-major [T][N]."""
+    p = L.SynthParams(N=N, T=T, K=K, kind=L.SYNTH_KINDS[kind], seed=seed, phi=phi,
+                      load_sd=load_sd, jitter_sd=jitter_sd, block=block, n_net=n_net)
+    out = np.empty((T, N), dtype=np.float32)
+    _check(lib().bna_synth_bold(C.byref(p), out.ctypes.data, threads))
+    return out
+
+
+@dataclass
+class CsrResult:
+    n: int
+    nnz: int
+    row_ptr: object   # torch.int32 [n+1] (device) or np.int32 (host)
+    col_idx: object   # [nnz]
+    val: object       # [nnz] float32 or None
+    stats: dict
+
+    def numpy(self) -> "CsrResult":
+        def h(x):
+            if x is None:
+                return None
+            return x.cpu().numpy() if hasattr(x, "cpu") else np.asarray(x)
+        return CsrResult(self.n, self.nnz, h(self.row_ptr), h(self.col_idx), h(self.val),
+                         self.stats)
+
+
+class _DevArray:
+    """Zero-copy __cuda_array_interface__ view of arena memory."""
+
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
+                                         "data": (ptr, False), "version": 3, "strides": None}
+
+
+def _view(ptr, n, typestr, torch, device):
+    if not ptr or n == 0:
+        dt = {"<i4": torch.int32, "<f4": torch.float32, "<f8": torch.float64}[typestr]
+        return torch.empty(0, dtype=dt, device=device)
+    return torch.as_tensor(_DevArray(ptr, n, typestr), device=device)
+
+
+def _opts(mode: str, value: float, precision: str, weighted: bool, delta: Optional[float]):
+    if mode not in L.THR_MODES:
+        raise ValueError(f"mode must be one of {sorted(L.THR_MODES)}")
+    if precision not in L.PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(L.PRECISIONS)}")
+    return L.CorrOpts(mode=L.THR_MODES[mode], precision=L.PRECISIONS[precision],
+                      value=float(value), weighted=1 if weighted else 0,
+                      delta=float(delta) if delta else 0.0)
+
+
+class Builder:
+    """One libbna context on one CUDA device (owns a reusable device arena)."""
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        h = C.c_void_p()
+        _check(lib().bna_ctx_create(device, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bna_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def arena_bytes(self) -> int:
+        return int(lib().bna_ctx_arena_bytes(self._h))
+
+    def trim(self):
+        _check(lib().bna_ctx_trim(self._h), self._h)
+
+    @staticmethod
+    def _stream(stream):
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return C.c_void_p(s.cuda_stream)
+
+    def zscore(self, bold, stream=None):
+        """bold: torch CUDA float32 [T][N] -> z [N][ldz] (ldz = T rounded up to 32)."""
+        import torch
+        T, N = bold.shape
+        ld = int(lib().bna_zscore_ld(T))
+        z = torch.empty((N, ld), dtype=torch.float32, device=bold.device)
+        _check(lib().bna_zscore(self._h, C.c_void_p(bold.data_ptr()), N, T,
+                                C.c_void_p(z.data_ptr()), ld, self._stream(stream)), self._h)
+        return z
+
+    def corr_csr(self, bold, mode: str = "r_gt", value: float = 0.5, precision: str = "fp32",
+                 weighted: bool = True, delta: Optional[float] = None, stream=None,
+                 copy: bool = True) -> CsrResult:
+        """Correlation -> thresholded CSR on the device.
+
+        bold: torch CUDA float32, contiguous, time-major [T][N].  With copy=False
+        the returned tensors alias the context's arena (valid until the next call).
+        """
+        import torch
+        assert bold.is_cuda and bold.dtype == torch.float32 and bold.is_contiguous()
+        T, N = bold.shape
+        o = _opts(mode, value, precision, weighted, delta)
+        out = L.Csr()
+        st = L.CorrStats()
+        _check(lib().bna_corr_csr(self._h, C.c_void_p(bold.data_ptr()), N, T, C.byref(o),
+                                  C.byref(out), C.byref(st), self._stream(stream)), self._h)
+        dev = bold.device
+        rp = _view(out.row_ptr, N + 1, "<i4", torch, dev)
+        ci = _view(out.col_idx, out.nnz, "<i4", torch, dev)
+        va = _view(out.val, out.nnz, "<f4", torch, dev) if out.val else None
+        if copy:
+            rp, ci = rp.clone(), ci.clone()
+            va = va.clone() if va is not None else None
+        return CsrResult(N, int(out.nnz), rp, ci, va, st.as_dict())
+
+    def corr_csr_host(self, bold: np.ndarray, mode: str = "r_gt", value: float = 0.5,
+                      precision: str = "fp32", weighted: bool = True,
+                      delta: Optional[float] = None) -> CsrResult:
+        """Host-buffer form: numpy float32 [T][N] in, numpy CSR out."""
+        bold = np.ascontiguousarray(bold, dtype=np.float32)
+        T, N = bold.shape
+        o = _opts(mode, value, precision, weighted, delta)
+        out = L.Csr()
+        st = L.CorrStats()
+        _check(lib().bna_corr_csr_host(self._h, bold.ctypes.data, N, T, C.byref(o), C.byref(out),
+                                       C.byref(st)), self._h)
+        try:
+            rp = np.ctypeslib.as_array(C.cast(out.row_ptr, C.POINTER(C.c_int32)), (N + 1,)).copy()
+            nnz = int(out.nnz)
+            ci = (np.ctypeslib.as_array(C.cast(out.col_idx, C.POINTER(C.c_int32)), (nnz,)).copy()
+                  if nnz else np.zeros(0, np.int32))
+            va = None
+            if out.val:
+                va = (np.ctypeslib.as_array(C.cast(out.val, C.POINTER(C.c_float)), (nnz,)).copy()
+                      if nnz else np.zeros(0, np.float32))
+        finally:
+            lib().bna_csr_free_host(C.byref(out))
+        return CsrResult(N, nnz, rp, ci, va, st.as_dict())
+
+    def tile_values(self, bold, I: int, J: int, precision: str = "fp32", stream=None):
+        """Approximate r of the 128 x 128 tile (I, J) for a precision form."""
+        import torch
+        T, N = bold.shape
+        out = torch.empty((128, 128), dtype=torch.float32, device=bold.device)
+        _check(lib().bna_corr_tile_values(self._h, C.c_void_p(bold.data_ptr()), N, T,
+                                          L.PRECISIONS[precision], I, J,
+                                          C.c_void_p(out.data_ptr()), self._stream(stream)),
+               self._h)
+        return out
+
+    def ec(self, csr: CsrResult, max_iter: int = 10000, eps: float = 1e-6, stream=None):
+        """Eigenvector centrality of a device CSR -> (ec float64 [n], lambda, iters, converged)."""
+        import torch
+        c = L.Csr(n=csr.n, nnz=csr.nnz, row_ptr=csr.row_ptr.data_ptr(),
+                  col_idx=csr.col_idx.data_ptr() if csr.nnz else None,
+                  val=csr.val.data_ptr() if csr.val is not None else None)
+        ec = torch.empty(csr.n, dtype=torch.float64, device=csr.row_ptr.device)
+        lam = C.c_double()
+        it = C.c_int32()
+        s = _check(lib().bna_ec(self._h, C.byref(c), max_iter, eps, C.c_void_p(ec.data_ptr()),
+                                C.byref(lam), C.byref(it), self._stream(stream)), self._h,
+                   ok=(L.BNA_OK, L.BNA_NOT_CONVERGED))
+        return ec, lam.value, it.value, s == L.BNA_OK
+
+    def lead_vector(self, R: np.ndarray, Cc: np.ndarray, V: Optional[np.ndarray] = None):
+        """Lead_Vector_GPU(R, C, V, N, ec) with host arrays -> (ec, lambda, iters, converged)."""
+        R = np.ascontiguousarray(R, dtype=np.int32)
+        Cc = np.ascontiguousarray(Cc, dtype=np.int32)
+        Vd = None if V is None else np.ascontiguousarray(V, dtype=np.float64)
+        N = len(R) - 1
+        ec = np.empty(N, dtype=np.float64)
+        lam = C.c_double()
+        it = C.c_int32()
+        s = _check(lib().bna_lead_vector(self._h, R.ctypes.data, Cc.ctypes.data if len(Cc) else None,
+                                         Vd.ctypes.data if Vd is not None else None, N,
+                                         ec.ctypes.data, C.byref(lam), C.byref(it)), self._h,
+                   ok=(L.BNA_OK, L.BNA_NOT_CONVERGED))
+        return ec, lam.value, it.value, s == L.BNA_OK
+
+
+def csr_write(path: str, row_ptr: np.ndarray, col_idx: np.ndarray,
+              val: Optional[np.ndarray] = None) -> None:
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_idx, dtype=np.int32)
+    va = None if val is None else np.ascontiguousarray(val, dtype=np.float32)
+    c = L.Csr(n=len(rp) - 1, nnz=len(ci), row_ptr=rp.ctypes.data,
+              col_idx=ci.ctypes.data if len(ci) else None,
+              val=va.ctypes.data if va is not None else None)
+    if va is not None and len(va) == 0:
+        c.val = C.c_void_p(rp.ctypes.data)  # non-null marker: write an empty V section
+    _check(lib().bna_csr_write(os.fsencode(path), C.byref(c)))
+
+
+def csr_read(path: str):
+    """-> (row_ptr, col_idx, val or None) as numpy arrays."""
+    c = L.Csr()
+    _check(lib().bna_csr_read(os.fsencode(path), C.byref(c)))
+    try:
+        n, nnz = c.n, int(c.nnz)
+        rp = np.ctypeslib.as_array(C.cast(c.row_ptr, C.POINTER(C.c_int32)), (n + 1,)).copy()
+        ci = (np.ctypeslib.as_array(C.cast(c.col_idx, C.POINTER(C.c_int32)), (nnz,)).copy()
+              if nnz else np.zeros(0, np.int32))
+        va = None
+        if c.val:
+            va = (np.ctypeslib.as_array(C.cast(c.val, C.POINTER(C.c_float)), (nnz,)).copy()
+                  if nnz else np.zeros(0, np.float32))
+    finally:
+        lib().bna_csr_free_host(C.byref(c))
+    return rp, ci, va
+
+
+def ec_write(path: str, ec: np.ndarray) -> None:
+    e = np.ascontiguousarray(ec, dtype=np.float64)
+    _check(lib().bna_ec_write(os.fsencode(path), e.ctypes.data, len(e)))

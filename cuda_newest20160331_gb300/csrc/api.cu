@@ -1,0 +1,601 @@
+// C ABI of the voxel-network builder: context, device arena and the host
+// orchestration of the correlation -> CSR passes and the power iteration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace bna {
+cudaError_t launch_zscore(const float* bold, int N, int T, int n_pad, float* z, int ldz,
+                          uint16_t* zhi, uint16_t* zlo, int ldb, uint8_t* bad,
+                          cudaStream_t stream);
+cudaError_t launch_corr_simt(const CorrArgs& a, int pass, cudaStream_t stream);
+cudaError_t launch_corr_simt_dump(const CorrArgs& a, int I, int J, float* out,
+                                  cudaStream_t stream);
+cudaError_t launch_recompute(const CorrArgs& a, int grid, cudaStream_t stream);
+cudaError_t launch_exact_pairs(const CorrArgs& a, const uint2* pairs, int n, float* out,
+                               cudaStream_t stream);
+cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* rowlen,
+                            long long* pre, long long* bsum, long long* total, int32_t* row_ptr,
+                            uint32_t* err, cudaStream_t stream);
+size_t ec_state_bytes();
+cudaError_t launch_ec_init(int n, double* u, double* parts, void* st, int grid, int max_iter,
+                           cudaStream_t stream);
+cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                           const double* vald, long long nnz_used, const double* u, double* un,
+                           double* parts, void* st, int grid, int max_iter, double eps,
+                           cudaStream_t stream);
+void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
+                   double* e2, int* iter, int* done);
+}  // namespace bna
+
+using namespace bna;
+
+namespace {
+
+enum Slot {
+  S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
+  S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
+  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_COUNT
+};
+
+// Small device block the host reads once per pass.
+struct DevStatus {
+  unsigned long long cand_count;
+  uint32_t err;
+  uint32_t pad;
+  unsigned long long stats[4];
+  long long total;
+};
+
+struct EcGraph {
+  cudaGraphExec_t exec = nullptr;
+  const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  int n = -1, grid = 0, max_iter = 0;
+  long long nnz_used = -1;
+  double eps = 0;
+};
+
+constexpr int kGraphIters = 32;
+
+}  // namespace
+
+struct bna_ctx {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t own_stream = nullptr;
+  void* ptr[S_COUNT] = {};
+  size_t cap[S_COUNT] = {};
+  void* pinned = nullptr;  // small pinned host buffer for status readback
+  cudaEvent_t ev[8] = {};
+  std::string last_error;
+  long long cand_cap = 1 << 20;
+  EcGraph ecg;
+};
+
+namespace {
+
+int32_t fail(bna_ctx* c, int32_t st, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->last_error = buf;
+  }
+  return st;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, BNA_CUDA_ERROR, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                   \
+  } while (0)
+
+int32_t ensure(bna_ctx* ctx, Slot s, size_t bytes, void** out) {
+  if (bytes == 0) bytes = 16;
+  if (ctx->cap[s] < bytes) {
+    if (ctx->ptr[s]) {
+      cudaError_t e = cudaFree(ctx->ptr[s]);
+      ctx->ptr[s] = nullptr;
+      ctx->cap[s] = 0;
+      if (e != cudaSuccess) return fail(ctx, BNA_CUDA_ERROR, "cudaFree: %s", cudaGetErrorString(e));
+    }
+    const size_t want = bytes + bytes / 8;  // headroom so small growth does not reallocate
+    cudaError_t e = cudaMalloc(&ctx->ptr[s], want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      e = cudaMalloc(&ctx->ptr[s], bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        ctx->ptr[s] = nullptr;
+        return fail(ctx, BNA_OOM, "cudaMalloc(%zu bytes) failed", bytes);
+      }
+      ctx->cap[s] = bytes;
+    } else {
+      ctx->cap[s] = want;
+    }
+  }
+  *out = ctx->ptr[s];
+  return BNA_OK;
+}
+
+#define ENSURE(slot, bytes, ptrvar)                                          \
+  do {                                                                       \
+    void* p_ = nullptr;                                                      \
+    int32_t st_ = ensure(ctx, slot, (size_t)(bytes), &p_);                   \
+    if (st_ != BNA_OK) return st_;                                           \
+    ptrvar = reinterpret_cast<decltype(ptrvar)>(p_);                         \
+  } while (0)
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+double default_delta(int precision, int T) {
+  const double u24 = std::ldexp(1.0, -24), u23 = std::ldexp(1.0, -23);
+  switch (precision) {
+    case BNA_PREC_BF16X3: return std::ldexp(1.0, -14) + 2.0 * (T + 8) * u23;
+    case BNA_PREC_TF32: return std::ldexp(1.0, -9) + 2.0 * (T + 8) * u23;
+    default: return 2.0 * (T + 8) * u24;
+  }
+}
+
+unsigned long long next_pow2(unsigned long long x) {
+  unsigned long long p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int32_t set_device(bna_ctx* ctx) {
+  CK(cudaSetDevice(ctx->device));
+  return BNA_OK;
+}
+
+// Z-score into the arena; fills layout fields of `a`.
+int32_t run_zscore(bna_ctx* ctx, const float* bold, int N, int T, bool need_bf16, CorrArgs& a,
+                   cudaStream_t st) {
+  a.n = N;
+  a.T = T;
+  a.n_pad = round_up(N, kBlk);
+  a.nb = a.n_pad / kBlk;
+  a.ldz = round_up(T, 32);
+  a.ldb = round_up(T, 64);
+  float* z;
+  uint8_t* bad;
+  ENSURE(S_Z, (size_t)a.n_pad * a.ldz * sizeof(float), z);
+  ENSURE(S_BAD, (size_t)a.n_pad, bad);
+  uint16_t *zhi = nullptr, *zlo = nullptr;
+  if (need_bf16) {
+    ENSURE(S_ZHI, (size_t)a.n_pad * a.ldb * 2, zhi);
+    ENSURE(S_ZLO, (size_t)a.n_pad * a.ldb * 2, zlo);
+  }
+  CK(launch_zscore(bold, N, T, a.n_pad, z, a.ldz, zhi, zlo, a.ldb, bad, st));
+  a.z = z;
+  a.zhi = zhi;
+  a.zlo = zlo;
+  a.bad = bad;
+  return BNA_OK;
+}
+
+int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st) {
+  switch (precision) {
+    case BNA_PREC_FP32: CK(launch_corr_simt(a, pass, st)); return BNA_OK;
+    default:
+      return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built in this library", precision);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bna_version(void) { return "bna-gb300 0.1"; }
+
+const char* bna_status_string(int32_t s) {
+  switch (s) {
+    case BNA_OK: return "ok";
+    case BNA_BAD_ARG: return "bad argument";
+    case BNA_OOM: return "out of device memory";
+    case BNA_NNZ_OVERFLOW_INT32: return "edge count exceeds the int32 CSR format";
+    case BNA_NOT_CONVERGED: return "power iteration did not converge";
+    case BNA_TIMEOUT: return "timeout";
+    case BNA_CUDA_ERROR: return "CUDA error";
+    case BNA_NO_DEVICE: return "no CUDA device";
+    case BNA_IO_ERROR: return "I/O error";
+    case BNA_CORRUPT_FILE: return "corrupt file";
+    case BNA_INTERNAL: return "internal consistency check failed";
+    case BNA_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int32_t bna_ctx_create(int32_t device, bna_ctx** out) {
+  if (!out) return BNA_BAD_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return BNA_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return BNA_BAD_ARG;
+  bna_ctx* ctx = new bna_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaMallocHost(&ctx->pinned, 4096) != cudaSuccess) {
+    delete ctx;
+    return BNA_CUDA_ERROR;
+  }
+  for (auto& e : ctx->ev) {
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      delete ctx;
+      return BNA_CUDA_ERROR;
+    }
+  }
+  *out = ctx;
+  return BNA_OK;
+}
+
+int32_t bna_ctx_trim(bna_ctx* ctx) {
+  if (!ctx) return BNA_BAD_ARG;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  for (int s = 0; s < S_COUNT; ++s) {
+    if (ctx->ptr[s]) cudaFree(ctx->ptr[s]);
+    ctx->ptr[s] = nullptr;
+    ctx->cap[s] = 0;
+  }
+  if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
+  ctx->ecg = EcGraph();
+  return BNA_OK;
+}
+
+int64_t bna_ctx_arena_bytes(const bna_ctx* ctx) {
+  if (!ctx) return 0;
+  int64_t t = 0;
+  for (int s = 0; s < S_COUNT; ++s) t += (int64_t)ctx->cap[s];
+  return t;
+}
+
+int32_t bna_ctx_destroy(bna_ctx* ctx) {
+  if (!ctx) return BNA_BAD_ARG;
+  bna_ctx_trim(ctx);
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  delete ctx;
+  return BNA_OK;
+}
+
+const char* bna_ctx_last_error(const bna_ctx* ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int32_t bna_zscore_ld(int32_t T) { return round_up(T, 32); }
+
+int32_t bna_zscore(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T, float* z_dev,
+                   int32_t ldz, void* stream) {
+  if (!ctx || !bold_dev || !z_dev || N <= 0 || T <= 0 || ldz < T || ldz % 32 != 0)
+    return fail(ctx, BNA_BAD_ARG, "bna_zscore: bad arguments");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  const int n_pad = round_up(N, kBlk);
+  uint8_t* bad;
+  ENSURE(S_BAD, (size_t)n_pad, bad);
+  // The kernel writes n_pad rows; the caller's buffer holds N rows, so stage
+  // through the arena when N is not a multiple of the block.
+  if (n_pad == N) {
+    CK(launch_zscore(bold_dev, N, T, n_pad, z_dev, ldz, nullptr, nullptr, 0, bad,
+                     as_stream(stream)));
+  } else {
+    float* z;
+    ENSURE(S_Z, (size_t)n_pad * ldz * sizeof(float), z);
+    CK(launch_zscore(bold_dev, N, T, n_pad, z, ldz, nullptr, nullptr, 0, bad, as_stream(stream)));
+    CK(cudaMemcpyAsync(z_dev, z, (size_t)N * ldz * sizeof(float), cudaMemcpyDeviceToDevice,
+                       as_stream(stream)));
+  }
+  return BNA_OK;
+}
+
+int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
+                     const bna_corr_opts* opts, bna_csr* out_dev, bna_corr_stats* stats,
+                     void* stream) {
+  if (!ctx || !bold_dev || !opts || !out_dev || N < 1 || T < 1)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: bad arguments");
+  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown threshold mode %d", opts->mode);
+  if (opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_TF32)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown precision %d", opts->precision);
+  if (opts->mode == BNA_THR_DENSITY)
+    return fail(ctx, BNA_UNSUPPORTED, "density mode is not built in this library");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  const int prec = opts->precision;
+  CorrArgs a{};
+  CK(cudaEventRecord(ctx->ev[0], st));
+  s = run_zscore(ctx, bold_dev, N, T, prec != BNA_PREC_FP32, a, st);
+  if (s) return s;
+  CK(cudaEventRecord(ctx->ev[1], st));
+  a.th.mode = opts->mode;
+  a.th.tau = (float)opts->value;
+  const double delta = opts->delta > 0 ? opts->delta : default_delta(prec, T);
+  a.th.delta = (float)delta;
+  a.weighted = opts->weighted ? 1 : 0;
+
+  ENSURE(S_SEG, (size_t)a.nb * a.n_pad * sizeof(int32_t), a.seg);
+  long long *rowlen, *pre, *bsum;
+  ENSURE(S_ROWLEN, (size_t)a.n_pad * 8, rowlen);
+  ENSURE(S_PRE, (size_t)a.n_pad * 8, pre);
+  ENSURE(S_BSUM, (size_t)4096 * 8, bsum);
+  int32_t* row_ptr;
+  ENSURE(S_ROWPTR, (size_t)(N + 1) * 4, row_ptr);
+  DevStatus* ds;
+  ENSURE(S_STATUS, sizeof(DevStatus), ds);
+  a.err = &ds->err;
+  a.cand_count = &ds->cand_count;
+  a.stats = ds->stats;
+  a.drop_keys = nullptr;
+  a.n_drop = 0;
+  DevStatus* hs = reinterpret_cast<DevStatus*>(ctx->pinned);
+
+  int passes = 0;
+  for (int attempt = 0;; ++attempt) {
+    a.cand_cap = ctx->cand_cap;
+    const unsigned long long hcap = next_pow2((unsigned long long)a.cand_cap * 2);
+    a.hmask = hcap - 1;
+    ENSURE(S_CAND, (size_t)a.cand_cap * sizeof(uint2), a.cand);
+    ENSURE(S_HKEYS, hcap * 8, a.hkeys);
+    ENSURE(S_HVAL, hcap * 4, a.hval);
+    ENSURE(S_HEDGE, hcap, a.hedge);
+    CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
+    CK(cudaMemsetAsync(a.hkeys, 0xff, hcap * 8, st));
+    s = corr_pass(ctx, a, prec, 0, st);
+    if (s) return s;
+    ++passes;
+    CK(cudaEventRecord(ctx->ev[2], st));
+    CK(launch_recompute(a, ctx->sms * 4, st));
+    CK(cudaEventRecord(ctx->ev[3], st));
+    CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
+                       st));
+    CK(cudaEventRecord(ctx->ev[4], st));
+    CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if ((hs->err & ERR_BAND_OVERFLOW) && attempt < 3) {
+      ctx->cand_cap = (long long)(hs->cand_count * 3 / 2) + 1024;
+      continue;
+    }
+    break;
+  }
+  if (hs->err & ERR_BAND_OVERFLOW)
+    return fail(ctx, BNA_INTERNAL, "candidate list overflow (%llu candidates)", hs->cand_count);
+  if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
+  if (hs->err & ERR_NNZ_INT32 || hs->total > 0x7fffffffLL)
+    return fail(ctx, BNA_NNZ_OVERFLOW_INT32, "nnz %lld exceeds int32", hs->total);
+  const long long nnz = hs->total;
+  const unsigned long long cand_count = hs->cand_count;
+  const unsigned long long band_edges = hs->stats[0], band_1e6 = hs->stats[1];
+  int32_t* col;
+  ENSURE(S_COL, (size_t)std::max(nnz, 1LL) * 4, col);
+  float* val = nullptr;
+  if (a.weighted) ENSURE(S_VAL, (size_t)std::max(nnz, 1LL) * 4, val);
+  a.row_ptr = row_ptr;
+  a.col_idx = col;
+  a.val = val;
+  s = corr_pass(ctx, a, prec, 1, st);
+  if (s) return s;
+  ++passes;
+  CK(cudaEventRecord(ctx->ev[5], st));
+  CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (hs->err & ERR_HASH_MISS) return fail(ctx, BNA_INTERNAL, "fill pass missed a candidate");
+  out_dev->n = N;
+  out_dev->nnz = nnz;
+  out_dev->row_ptr = row_ptr;
+  out_dev->col_idx = col;
+  out_dev->val = val;
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->tau = (double)a.th.tau;
+    stats->delta = delta;
+    stats->nnz = nnz;
+    stats->band_candidates = (int64_t)cand_count;
+    stats->band_edges = (int64_t)band_edges;
+    stats->band_1e6 = (int64_t)band_1e6;
+    stats->passes = passes;
+    // z-score, count, recompute, 4 scan kernels, fill
+    stats->kernel_launches = 1 + passes + 1 + 4;
+    cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);
+    cudaEventElapsedTime(&stats->ms_scan, ctx->ev[3], ctx->ev[4]);
+    cudaEventElapsedTime(&stats->ms_fill, ctx->ev[4], ctx->ev[5]);
+    cudaEventElapsedTime(&stats->ms_total, ctx->ev[0], ctx->ev[5]);
+  }
+  return BNA_OK;
+}
+
+int32_t bna_corr_csr_host(bna_ctx* ctx, const float* bold_host, int32_t N, int32_t T,
+                          const bna_corr_opts* opts, bna_csr* out_host, bna_corr_stats* stats) {
+  if (!ctx || !bold_host || !out_host || N < 1 || T < 1)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_host: bad arguments");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  float* bold;
+  ENSURE(S_BOLD, (size_t)N * T * sizeof(float), bold);
+  CK(cudaMemcpyAsync(bold, bold_host, (size_t)N * T * sizeof(float), cudaMemcpyHostToDevice,
+                     nullptr));
+  bna_csr d{};
+  s = bna_corr_csr(ctx, bold, N, T, opts, &d, stats, nullptr);
+  if (s) return s;
+  out_host->n = N;
+  out_host->nnz = d.nnz;
+  out_host->row_ptr = (int32_t*)std::malloc((size_t)(N + 1) * 4);
+  out_host->col_idx = (int32_t*)std::malloc((size_t)std::max<int64_t>(d.nnz, 1) * 4);
+  out_host->val = d.val ? (float*)std::malloc((size_t)std::max<int64_t>(d.nnz, 1) * 4) : nullptr;
+  if (!out_host->row_ptr || !out_host->col_idx || (d.val && !out_host->val)) {
+    bna_csr_free_host(out_host);
+    return fail(ctx, BNA_OOM, "host allocation failed");
+  }
+  CK(cudaMemcpyAsync(out_host->row_ptr, d.row_ptr, (size_t)(N + 1) * 4, cudaMemcpyDeviceToHost,
+                     nullptr));
+  if (d.nnz > 0) {
+    CK(cudaMemcpyAsync(out_host->col_idx, d.col_idx, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost,
+                       nullptr));
+    if (d.val)
+      CK(cudaMemcpyAsync(out_host->val, d.val, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost,
+                         nullptr));
+  }
+  CK(cudaStreamSynchronize(nullptr));
+  return BNA_OK;
+}
+
+void bna_csr_free_host(bna_csr* c) {
+  if (!c) return;
+  std::free(c->row_ptr);
+  std::free(c->col_idx);
+  std::free(c->val);
+  c->row_ptr = nullptr;
+  c->col_idx = nullptr;
+  c->val = nullptr;
+}
+
+int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
+                             int32_t precision, int32_t I, int32_t J, float* out_dev,
+                             void* stream) {
+  if (!ctx || !bold_dev || !out_dev || N < 1 || T < 1)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_tile_values: bad arguments");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  CorrArgs a{};
+  s = run_zscore(ctx, bold_dev, N, T, precision != BNA_PREC_FP32, a, st);
+  if (s) return s;
+  if (I < 0 || J < 0 || I >= a.nb || J >= a.nb)
+    return fail(ctx, BNA_BAD_ARG, "tile (%d, %d) outside the %d-block grid", I, J, a.nb);
+  switch (precision) {
+    case BNA_PREC_FP32: CK(launch_corr_simt_dump(a, I, J, out_dev, st)); break;
+    default: return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built", precision);
+  }
+  return BNA_OK;
+}
+
+// ---------------------------------------------------------------- centrality
+
+static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci, const float* val,
+                      const double* vald, long long nnz, int max_iter, double eps, double* ec_dev,
+                      double* lambda, int32_t* iters, cudaStream_t st) {
+  const long long nnz_used = 2 * (nnz / 2);  // weighted-net.cu:61
+  double *u, *parts;
+  void* state;
+  ENSURE(S_EC_U, (size_t)2 * n * sizeof(double), u);
+  const int grid = std::max(1, ctx->sms * 4);
+  ENSURE(S_EC_PARTS, (size_t)grid * 3 * sizeof(double), parts);
+  ENSURE(S_EC_STATE, ec_state_bytes(), state);
+  CK(cudaMemsetAsync(state, 0, ec_state_bytes(), st));
+  CK(launch_ec_init(n, u, parts, state, grid, max_iter, st));
+  EcGraph& g = ctx->ecg;
+  const void* key[6] = {rp, ci, val, vald, u, state};
+  bool same = g.exec && g.n == n && g.grid == grid && g.max_iter == max_iter && g.eps == eps &&
+              g.nnz_used == nnz_used;
+  for (int k = 0; k < 6 && same; ++k) same = (g.key[k] == key[k]);
+  if (!same) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = EcGraph();
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < kGraphIters; ++it) {
+      const double* ucur = u + (size_t)(it & 1) * n;
+      double* unext = u + (size_t)((it + 1) & 1) * n;
+      launch_ec_iter(n, rp, ci, val, vald, nnz_used, ucur, unext, parts, state, grid, max_iter,
+                     eps, cap);
+    }
+    cudaGraph_t graph;
+    cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    CK(ce);
+    ce = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ce);
+    for (int k = 0; k < 6; ++k) g.key[k] = key[k];
+    g.n = n;
+    g.grid = grid;
+    g.max_iter = max_iter;
+    g.eps = eps;
+    g.nnz_used = nnz_used;
+  }
+  double lam2 = 0, lam = 0, e1 = 0, e2 = 0;
+  int it = 0, done = 0;
+  for (int launched = 0; launched < max_iter; launched += kGraphIters) {
+    CK(cudaGraphLaunch(g.exec, st));
+    CK(cudaMemcpyAsync(ctx->pinned, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    ec_state_read(ctx->pinned, &lam2, &lam, &e1, &e2, &it, &done);
+    if (done) break;
+  }
+  if (max_iter <= 0) {
+    CK(cudaMemcpyAsync(ctx->pinned, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    ec_state_read(ctx->pinned, &lam2, &lam, &e1, &e2, &it, &done);
+  }
+  // iterate k writes buffer (k+1)&1, so the last iterate sits in buffer it&1
+  CK(cudaMemcpyAsync(ec_dev, u + (size_t)(it & 1) * n, (size_t)n * sizeof(double),
+                     cudaMemcpyDeviceToDevice, st));
+  if (lambda) *lambda = lam;
+  if (iters) *iters = it;
+  const bool converged = (e1 <= eps || e2 <= eps);
+  return converged ? BNA_OK : BNA_NOT_CONVERGED;
+}
+
+int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr, int32_t max_iter, double eps, double* ec_dev,
+               double* lambda, int32_t* iters, void* stream) {
+  if (!ctx || !csr || !ec_dev || csr->n < 1 || !csr->row_ptr || (csr->nnz > 0 && !csr->col_idx))
+    return fail(ctx, BNA_BAD_ARG, "bna_ec: bad arguments");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  return ec_run(ctx, csr->n, csr->row_ptr, csr->col_idx, csr->val, nullptr, csr->nnz, max_iter,
+                eps, ec_dev, lambda, iters, as_stream(stream));
+}
+
+int32_t bna_lead_vector(bna_ctx* ctx, const int32_t* R, const int32_t* C, const double* V,
+                        int64_t N, double* ec_host, double* lambda, int32_t* iters) {
+  if (!ctx || !R || !ec_host || N < 1 || N > 0x7fffffffLL)
+    return fail(ctx, BNA_BAD_ARG, "bna_lead_vector: bad arguments");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  const long long nnz = R[N];
+  if (nnz < 0) return fail(ctx, BNA_BAD_ARG, "bna_lead_vector: negative R[N]");
+  if (nnz > 0 && !C) return fail(ctx, BNA_BAD_ARG, "bna_lead_vector: C is NULL");
+  int32_t *dr, *dc;
+  double* dv = nullptr;
+  double* dec;
+  ENSURE(S_EC_R, (size_t)(N + 1) * 4, dr);
+  ENSURE(S_EC_C, (size_t)std::max(nnz, 1LL) * 4, dc);
+  if (V) ENSURE(S_EC_VD, (size_t)std::max(nnz, 1LL) * 8, dv);
+  ENSURE(S_DUMP, (size_t)N * 8, dec);
+  CK(cudaMemcpyAsync(dr, R, (size_t)(N + 1) * 4, cudaMemcpyHostToDevice, nullptr));
+  if (nnz > 0) {
+    CK(cudaMemcpyAsync(dc, C, (size_t)nnz * 4, cudaMemcpyHostToDevice, nullptr));
+    if (V) CK(cudaMemcpyAsync(dv, V, (size_t)nnz * 8, cudaMemcpyHostToDevice, nullptr));
+  }
+  s = ec_run(ctx, (int)N, dr, dc, nullptr, dv, nnz, 10000, 1e-6, dec, lambda, iters, nullptr);
+  if (s != BNA_OK && s != BNA_NOT_CONVERGED) return s;
+  CK(cudaMemcpyAsync(ec_host, dec, (size_t)N * 8, cudaMemcpyDeviceToHost, nullptr));
+  CK(cudaStreamSynchronize(nullptr));
+  return s;
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+// Shared device-side definitions of the voxel-network builder.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/bna.h"
+
+namespace bna {
+
+// Square block of the voxel index space used for the CSR bookkeeping:
+// seg[b][i] counts (then offsets) the edges of row i whose column lies in
+// block b.  Every correlation tile covers whole 128-blocks.
+constexpr int kBlk = 128;
+
+// Error bits raised by kernels into CorrArgs::err (host reads them once per call).
+enum : uint32_t {
+  ERR_BAND_OVERFLOW = 1u,   // candidate list full
+  ERR_HASH_MISS = 2u,       // fill pass met a candidate the recompute pass never stored
+  ERR_HASH_FULL = 4u,
+  ERR_NNZ_INT32 = 8u,
+  ERR_TIES = 16u,           // density: tie bookkeeping inconsistent
+};
+
+// Outcome of classifying one approximate correlation.
+enum : int { CLS_NO = 0, CLS_EDGE = 1, CLS_BAND = 2 };
+
+struct Threshold {
+  int mode;      // bna_thr_mode (density runs as R_GE on tau = r_k plus the tie list)
+  float tau;
+  float delta;   // band half-width in r units (includes rounding margin)
+};
+
+// Exact decision on the reference's value r (after post_block clamping).
+__device__ __forceinline__ bool edge_exact(float r, const Threshold& th) {
+  switch (th.mode) {
+    case BNA_THR_R_GT: return r > th.tau;
+    case BNA_THR_ABS_GT: return fabsf(r) > th.tau;
+    case BNA_THR_ABS_GE: return fabsf(r) >= th.tau;
+    default: return r >= th.tau;  // R_GE and DENSITY
+  }
+}
+
+// post_block (CorMat.cpp:869-884): values outside [-1, 1], and NaN, become 0.
+__device__ __forceinline__ float post_block(float r) {
+  return (r >= -1.0f && r <= 1.0f) ? r : 0.0f;
+}
+
+// Classify an approximate correlation whose error vs the reference value is
+// at most th.delta.  A value is decided directly only when the whole
+// interval [r - delta, r + delta] lies inside (-1, 1) and on one side of tau.
+__device__ __forceinline__ int classify(float r, const Threshold& th) {
+  const float a = fabsf(r);
+  if (!(a < 1.0f - th.delta)) return CLS_BAND;  // near +-1, or NaN
+  const bool absm = (th.mode == BNA_THR_ABS_GT || th.mode == BNA_THR_ABS_GE);
+  const float x = absm ? a : r;
+  const float d = x - th.tau;
+  if (d > th.delta) return CLS_EDGE;
+  if (d < -th.delta) return CLS_NO;
+  return CLS_BAND;
+}
+
+// Pointers and sizes shared by the correlation passes.
+struct CorrArgs {
+  const float* z;            // voxel-major [n_pad][ldz], FP32 z-scores (exact recompute source)
+  const uint16_t* zhi;       // voxel-major [n_pad][ldb] BF16 hi parts (tensor-core forms)
+  const uint16_t* zlo;       // BF16 lo parts
+  const uint8_t* bad;        // [n_pad] 1 = voxel has a NaN z (every r of it is NaN -> 0)
+  int n, n_pad, T, ldz, ldb, nb;
+  Threshold th;
+  int weighted;
+  int32_t* seg;              // [nb][n_pad]
+  const int32_t* row_ptr;    // [n+1] (fill pass)
+  int32_t* col_idx;          // [nnz]
+  float* val;                // [nnz] or null
+  // near-threshold candidates (count pass appends, recompute resolves)
+  uint2* cand;               // (i, j) with i < j
+  unsigned long long* cand_count;
+  long long cand_cap;
+  // hash of resolved candidates: key (i<<32|j) -> (value, edge flag)
+  unsigned long long* hkeys;
+  float* hval;
+  uint8_t* hedge;
+  unsigned long long hmask;
+  // density ties that must not become edges (sorted keys), see FormFullGraph_s
+  const unsigned long long* drop_keys;
+  int n_drop;
+  uint32_t* err;
+  unsigned long long* stats;  // [0]=band edges [1]=band within 1e-6
+};
+
+__device__ __forceinline__ unsigned long long pair_key(int i, int j) {
+  return ((unsigned long long)(uint32_t)i << 32) | (uint32_t)j;
+}
+
+__device__ __forceinline__ unsigned long long hash64(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdULL;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ULL;
+  k ^= k >> 33;
+  return k;
+}
+
+// Look up a resolved candidate.  Returns false (and flags ERR_HASH_MISS) if absent.
+__device__ __forceinline__ bool hash_lookup(const CorrArgs& a, unsigned long long key, float& v,
+                                            bool& edge) {
+  unsigned long long h = hash64(key) & a.hmask;
+  for (unsigned long long probe = 0; probe <= a.hmask; ++probe) {
+    const unsigned long long k = a.hkeys[h];
+    if (k == key) {
+      v = a.hval[h];
+      edge = a.hedge[h] != 0;
+      return true;
+    }
+    if (k == ~0ull) break;
+    h = (h + 1) & a.hmask;
+  }
+  atomicOr(a.err, ERR_HASH_MISS);
+  v = 0.f;
+  edge = false;
+  return false;
+}
+
+// Append a near-threshold candidate (count pass).
+__device__ __forceinline__ void push_candidate(const CorrArgs& a, int i, int j) {
+  const unsigned long long slot = atomicAdd(a.cand_count, 1ull);
+  if ((long long)slot < a.cand_cap) {
+    a.cand[slot] = make_uint2((unsigned)i, (unsigned)j);
+  } else {
+    atomicOr(a.err, ERR_BAND_OVERFLOW);
+  }
+}
+
+// Upper-triangular tile index -> (I, J), I <= J, row-major over I.
+__device__ __forceinline__ void tile_coords(long long t, int nt, int& I, int& J) {
+  // rows before I hold I*nt - I*(I-1)/2 tiles
+  double disc = (2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * (double)t;
+  int i = (int)(((2.0 * nt + 1.0) - sqrt(disc)) * 0.5);
+  if (i < 0) i = 0;
+  if (i > nt - 1) i = nt - 1;
+  auto start = [nt](long long r) { return r * nt - r * (r - 1) / 2; };
+  while (i > 0 && start(i) > t) --i;
+  while (i + 1 < nt && start(i + 1) <= t) ++i;
+  I = i;
+  J = i + (int)(t - start(i));
+}
+
+}  // namespace bna

@@ -1,0 +1,213 @@
+// Near-threshold recompute and CSR offset scans.
+//
+// Recompute: every candidate pair (|r_approx - tau| <= delta, or |r_approx|
+// near 1) is evaluated with the reference CPU arithmetic of CorMat_cpu
+// (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:955-964): float products of the
+// float z-scores, accumulated in double in time order, rounded to float;
+// then post_block's clamp (CorMat.cpp:883) and the exact threshold rule.
+// Sequential per pair, so the value is bit-identical to the reference's.
+//
+// Scan: seg[b][i] (edges of row i in column block b) becomes the exclusive
+// prefix along b, and row_ptr = exclusive prefix of the row totals
+// (FormCSRGraph's R, CorMat.cpp:889-918).
+#include "common.cuh"
+
+namespace bna {
+
+__device__ __forceinline__ float exact_r(const CorrArgs& a, int i, int j) {
+  if (a.bad[i] | a.bad[j]) return 0.0f;  // NaN -> 0 in post_block
+  const float* zi = a.z + (size_t)i * a.ldz;
+  const float* zj = a.z + (size_t)j * a.ldz;
+  double s = 0.0;
+  for (int t = 0; t < a.T; ++t) s = __dadd_rn(s, (double)__fmul_rn(__ldg(zi + t), __ldg(zj + t)));
+  return post_block(__double2float_rn(s));
+}
+
+__device__ __forceinline__ bool in_sorted(const unsigned long long* keys, int n,
+                                          unsigned long long k) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (keys[mid] < k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < n && keys[lo] == k;
+}
+
+__global__ void recompute_kernel(CorrArgs a) {
+  const unsigned long long cnt = *a.cand_count;
+  const long long n = (long long)cnt < a.cand_cap ? (long long)cnt : a.cand_cap;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const uint2 p = a.cand[c];
+    const int i = (int)p.x, j = (int)p.y;
+    const float r = exact_r(a, i, j);
+    const unsigned long long key = pair_key(i, j);
+    bool e = edge_exact(r, a.th);
+    if (e && a.th.mode == BNA_THR_DENSITY && r == a.th.tau && a.n_drop > 0 &&
+        in_sorted(a.drop_keys, a.n_drop, key))
+      e = false;
+    if (e) {
+      atomicAdd(&a.seg[(size_t)(j / kBlk) * a.n_pad + i], 1);
+      atomicAdd(&a.seg[(size_t)(i / kBlk) * a.n_pad + j], 1);
+      atomicAdd(&a.stats[0], 1ull);
+    }
+    const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
+    if (fabsf((absm ? fabsf(r) : r) - a.th.tau) <= 1e-6f) atomicAdd(&a.stats[1], 1ull);
+    unsigned long long h = hash64(key) & a.hmask;
+    bool stored = false;
+    for (unsigned long long probe = 0; probe <= a.hmask; ++probe) {
+      const unsigned long long prev = atomicCAS(&a.hkeys[h], ~0ull, key);
+      if (prev == ~0ull || prev == key) {
+        a.hval[h] = r;
+        a.hedge[h] = e ? 1 : 0;
+        stored = true;
+        break;
+      }
+      h = (h + 1) & a.hmask;
+    }
+    if (!stored) atomicOr(a.err, ERR_HASH_FULL);
+  }
+}
+
+// Exact values of arbitrary pairs (diagnostics: max |r - r_ref| of a form).
+__global__ void exact_pairs_kernel(CorrArgs a, const uint2* pairs, int n, float* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) out[c] = exact_r(a, (int)pairs[c].x, (int)pairs[c].y);
+}
+
+// seg[b][i] -> exclusive prefix over b; rowlen[i] = row total.
+__global__ void seg_scan_rows_kernel(int32_t* seg, int nb, int n_pad, int n, long long* rowlen) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  long long acc = 0;
+  for (int b = 0; b < nb; ++b) {
+    int32_t* p = seg + (size_t)b * n_pad + i;
+    const int c = *p;
+    *p = (int)acc;
+    acc += c;
+  }
+  if (i < n) rowlen[i] = acc;
+}
+
+// Block-local exclusive scan of 4096 int64 values (1024 threads x 4).
+__global__ __launch_bounds__(1024) void scan_block_kernel(const long long* in, int n, long long* out,
+                                                          long long* bsum) {
+  __shared__ long long wsum[32];
+  const int base = blockIdx.x * 4096 + threadIdx.x * 4;
+  long long v[4];
+  long long s = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0;
+    s += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  long long run = x - s + (warp > 0 ? wsum[warp - 1] : 0);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 1023) bsum[blockIdx.x] = run;
+}
+
+__global__ __launch_bounds__(1024) void scan_sums_kernel(long long* bsum, int nblk,
+                                                         long long* total) {
+  __shared__ long long wsum[32];
+  const int base = threadIdx.x * 4;
+  long long v[4];
+  long long s = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = (base + k < nblk) ? bsum[base + k] : 0;
+    s += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  long long run = x - s + (warp > 0 ? wsum[warp - 1] : 0);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (base + k < nblk) bsum[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 1023) *total = run;
+}
+
+__global__ void scan_finish_kernel(const long long* pre, const long long* bsum, int n,
+                                   const long long* total, int32_t* row_ptr, uint32_t* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const long long v = pre[i] + bsum[i / 4096];
+    row_ptr[i] = (int32_t)v;
+    if (v > 0x7fffffffLL) atomicOr(err, ERR_NNZ_INT32);
+  } else if (i == n) {
+    const long long v = *total;
+    row_ptr[n] = (int32_t)v;
+    if (v > 0x7fffffffLL) atomicOr(err, ERR_NNZ_INT32);
+  }
+}
+
+cudaError_t launch_recompute(const CorrArgs& a, int grid, cudaStream_t stream) {
+  recompute_kernel<<<grid, 128, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_exact_pairs(const CorrArgs& a, const uint2* pairs, int n, float* out,
+                               cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  exact_pairs_kernel<<<(n + 127) / 128, 128, 0, stream>>>(a, pairs, n, out);
+  return cudaGetLastError();
+}
+
+// rowlen/pre: n int64; bsum: ceil(n/4096) int64 (<= 4096 blocks); total: 1 int64.
+cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* rowlen,
+                            long long* pre, long long* bsum, long long* total, int32_t* row_ptr,
+                            uint32_t* err, cudaStream_t stream) {
+  const int nblk = (n + 4095) / 4096;
+  if (nblk > 4096) return cudaErrorInvalidValue;
+  seg_scan_rows_kernel<<<(n_pad + 255) / 256, 256, 0, stream>>>(seg, nb, n_pad, n, rowlen);
+  scan_block_kernel<<<nblk, 1024, 0, stream>>>(rowlen, n, pre, bsum);
+  scan_sums_kernel<<<1, 1024, 0, stream>>>(bsum, nblk, total);
+  scan_finish_kernel<<<(n + 1 + 255) / 256, 256, 0, stream>>>(pre, bsum, n, total, row_ptr, err);
+  return cudaGetLastError();
+}
+
+}  // namespace bna

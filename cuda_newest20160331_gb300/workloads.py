@@ -1,0 +1,53 @@
+"""Synthetic workloads of the voxel-network builder (seeded factor-model BOLD;
+no public dataset exists for this path and the reference's own fMRI data is
+not distributed).  Sizes follow the reference's typical runs (N up to
+~180k grey-matter voxels at 2 mm, T = 120 to 1200 volumes).
+
+  small      N=4,096   T=240  K=20  r >= 0.5, binary CSR, then centrality
+  n45k       N=45,000  T=240  K=40  1 % density: tau = the FP64 quantile
+             (tests/golden/workload_tau.json), weighted CSR
+  n180k      N=180,000 T=1200 K=60  block-network loadings (500-voxel blocks),
+             tau = 0.4, weighted CSR, then centrality
+"""
+from __future__ import annotations
+
+import json
+import os
+from dataclasses import dataclass, field
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+TAU_FILE = os.path.join(ROOT, "tests", "golden", "workload_tau.json")
+
+
+@dataclass
+class Workload:
+    name: str
+    N: int
+    T: int
+    K: int
+    seed: int
+    mode: str
+    value: float
+    weighted: bool
+    kind: str = "iid"
+    synth: dict = field(default_factory=dict)
+
+    def bold(self, threads: int = 0):
+        from . import synth_bold
+        return synth_bold(self.N, self.T, self.K, self.seed, kind=self.kind, threads=threads,
+                          **self.synth)
+
+
+def n45k_tau() -> float:
+    return float(json.load(open(TAU_FILE))["tau_f32"])
+
+
+def get(name: str) -> Workload:
+    if name == "small":
+        return Workload("small", 4096, 240, 20, 1, "r_ge", 0.5, False)
+    if name == "n45k":
+        return Workload("n45k", 45000, 240, 40, 2, "r_ge", n45k_tau(), True)
+    if name == "n180k":
+        return Workload("n180k", 180000, 1200, 60, 3, "r_ge", 0.4, True, kind="blocknet",
+                        synth={"load_sd": 0.117, "jitter_sd": 0.08, "block": 500, "n_net": 60})
+    raise KeyError(name)

@@ -1,0 +1,197 @@
+/*
+ * bna.h — C ABI of the GB300-native voxel-network builder.
+ *
+ * The path: BOLD time series -> z-score -> Pearson correlation as tiled GEMM
+ * -> threshold (r value, |r| value or exact density) -> CSR
+ * (row_ptr / col_idx / val) -> eigenvector centrality by power iteration.
+ *
+ * Reference (BNAPlatform, "W/" = BNAPlatform-weighted-win64-cuda7.0-20160331/src,
+ * "U/" = BNAPlatform-win64-cuda7.0-20160115/src).  The reference has no plugin
+ * or FFI layer; its boundary is a set of in-process C++ functions plus the
+ * .csr / _ec.nm file formats.  Each entry point below names the reference
+ * function(s) whose behaviour it reproduces.
+ *
+ * Conventions
+ *  - Every call returns a bna_status (0 = success).  The reference returned 1
+ *    on success from CorMat_gpu (W/CorMat/CUCorMat/CUCorMat/CorMat.cu:161);
+ *    that convention is not kept.
+ *  - Plain pointers and sizes only.  "_dev" pointers are device memory of the
+ *    context's device; "_host" pointers are host memory.  `stream` is a
+ *    cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - One context per host thread at a time; contexts are independent.
+ */
+#ifndef BNA_H
+#define BNA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bna_status {
+  BNA_OK = 0,
+  BNA_BAD_ARG = 1,
+  BNA_OOM = 2,                /* device allocation failed */
+  BNA_NNZ_OVERFLOW_INT32 = 3, /* edge count exceeds the int32 .csr format */
+  BNA_NOT_CONVERGED = 4,      /* power iteration reached max_iter; outputs are still written */
+  BNA_TIMEOUT = 5,
+  BNA_CUDA_ERROR = 6,
+  BNA_NO_DEVICE = 7,
+  BNA_IO_ERROR = 8,
+  BNA_CORRUPT_FILE = 9,       /* .csr lengths inconsistent (W/CUEC/weighted-net.cu:283) */
+  BNA_INTERNAL = 10,          /* an internal consistency check failed */
+  BNA_UNSUPPORTED = 11
+} bna_status;
+
+/* Threshold rules.  r below is the reference's value after post_block
+ * (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:869-884): a correlation outside
+ * [-1, 1] (or NaN from a zero-variance voxel) becomes 0.  The diagonal is
+ * never an edge. */
+typedef enum bna_thr_mode {
+  BNA_THR_R_GT = 0,   /* r >  tau : FormFullGraph, CorMat.cpp:696 (CUCorMat "r" mode) */
+  BNA_THR_R_GE = 1,   /* r >= tau */
+  BNA_THR_ABS_GT = 2, /* |r| > tau: FormFullGraph, U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:198 */
+  BNA_THR_ABS_GE = 3, /* |r| >= tau */
+  BNA_THR_DENSITY = 4 /* value = sparsity s in percent: exactly k = Clength/2 undirected edges,
+                         Clength = floor(2*M1*s/100) rounded up to even (CorMat.cpp:327-328);
+                         tau = the k-th largest r; ties at tau kept in row-major (i<j) scan
+                         order (FormFullGraph_s, CorMat.cpp:743-822) */
+} bna_thr_mode;
+
+/* Arithmetic of the correlation tiles.  Whatever the form, every pair whose
+ * approximate r lies within `delta` of tau (or of +-1) is recomputed exactly
+ * as the reference CPU path does (float products, double accumulation in
+ * time order, CorMat.cpp:955-964), so the edge set equals the reference's. */
+typedef enum bna_precision {
+  BNA_PREC_FP32 = 0,   /* plain FP32 CUDA-core GEMM */
+  BNA_PREC_BF16X3 = 1, /* split BF16 (hi*hi + hi*lo + lo*hi) on tcgen05 tensor cores, FP32 accumulate */
+  BNA_PREC_TF32 = 2    /* TF32 on tcgen05 tensor cores, FP32 accumulate */
+} bna_precision;
+
+typedef struct bna_csr {
+  int32_t n;        /* vertices (voxels) */
+  int64_t nnz;      /* directed entries = 2 x undirected edges */
+  int32_t* row_ptr; /* n + 1 */
+  int32_t* col_idx; /* nnz, ascending within each row */
+  float* val;       /* nnz, r of each edge; NULL for a binary graph */
+} bna_csr;
+
+typedef struct bna_corr_opts {
+  int32_t mode;      /* bna_thr_mode */
+  int32_t precision; /* bna_precision */
+  double value;      /* tau (compared as float, like the reference's real__t), or density percent */
+  int32_t weighted;  /* 1: fill val; 0: binary graph (val = NULL) */
+  double delta;      /* recompute band half-width; <= 0 selects the precision's bound */
+  int32_t reserved[8];
+} bna_corr_opts;
+
+typedef struct bna_corr_stats {
+  double tau;              /* threshold applied (density mode: the selected k-th largest r) */
+  double delta;            /* recompute band half-width used */
+  int64_t nnz;             /* directed entries */
+  int64_t band_candidates; /* pairs recomputed exactly */
+  int64_t band_edges;      /* recomputed pairs that became edges */
+  int64_t band_1e6;        /* recomputed pairs with |r - tau| <= 1e-6 */
+  int64_t ties_dropped;    /* density mode: pairs equal to tau left out to hit the exact count */
+  float ms_zscore, ms_count, ms_recompute, ms_scan, ms_fill, ms_total; /* device time per stage */
+  int32_t passes;          /* GEMM passes run */
+  int32_t kernel_launches; /* kernels this call launched */
+  int32_t reserved[6];
+} bna_corr_stats;
+
+typedef struct bna_ctx bna_ctx;
+
+const char* bna_status_string(int32_t status);
+const char* bna_version(void);
+
+/* Context on one CUDA device.  Owns a grow-only device arena reused across
+ * calls (no allocation in steady state). */
+int32_t bna_ctx_create(int32_t device, bna_ctx** out);
+int32_t bna_ctx_destroy(bna_ctx* ctx);
+const char* bna_ctx_last_error(const bna_ctx* ctx);
+/* Release the arena's device memory (the context stays usable). */
+int32_t bna_ctx_trim(bna_ctx* ctx);
+/* Bytes currently held by the arena. */
+int64_t bna_ctx_arena_bytes(const bna_ctx* ctx);
+
+/* Z-score, the prologue of CorMat_gpu / CorMat_cpu (W/CorMat/CUCorMat/CUCorMat/CorMat.cu:24-52,
+ * CorMat.cpp:923-951): per voxel mean and centred L2 norm in double, summed in time
+ * order, z = (x - mean) / norm rounded to float.  bold_dev is time-major [T][N];
+ * z_dev is voxel-major [N][ldz] (ldz >= T; columns T..ldz-1 are zeroed).  The
+ * result is bit-identical to the reference's host loop. */
+int32_t bna_zscore(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T, float* z_dev,
+                   int32_t ldz, void* stream);
+
+/* Correlation -> thresholded CSR on the device.  Replaces the chain
+ * CorMat_gpu (CorMat.cu:17) -> post_block (CorMat.cpp:824) -> FormFullGraph /
+ * FormFullGraph_s (CorMat.cpp:683 / :743) -> FormCSRGraph (CorMat.cpp:889),
+ * without materialising the N x N matrix.  bold_dev is time-major [T][N].
+ * On success *out_dev points at device buffers owned by the context, valid
+ * until the next bna_corr_csr / bna_ctx_trim / bna_ctx_destroy on it.
+ * row_ptr and col_idx equal the reference's output on the same input. */
+int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
+                     const bna_corr_opts* opts, bna_csr* out_dev, bna_corr_stats* stats,
+                     void* stream);
+
+/* Host-buffer form of bna_corr_csr: bold_host is time-major [T][N]; the CSR is
+ * returned in host memory allocated by the library (release it with
+ * bna_csr_free_host).  Host<->device copies happen inside the call. */
+int32_t bna_corr_csr_host(bna_ctx* ctx, const float* bold_host, int32_t N, int32_t T,
+                          const bna_corr_opts* opts, bna_csr* out_host, bna_corr_stats* stats);
+void bna_csr_free_host(bna_csr* csr);
+
+/* Approximate correlation values of one BM x BN tile (rows I*128.., columns
+ * J*128.. of the z-scored matrix), written row-major to out_dev (128 x 128
+ * floats), for measuring max |r - r_fp64| of a precision form.  z_dev as
+ * produced by bna_zscore with ldz = bna_zscore_ld(T). */
+int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
+                             int32_t precision, int32_t I, int32_t J, float* out_dev, void* stream);
+int32_t bna_zscore_ld(int32_t T);
+
+/* Eigenvector centrality by power iteration, Lead_Vector_GPU
+ * (W/CUEC/weighted-net.cu:55-221): u0[i] = i; loop { u0 = u; lambda = ||u||;
+ * u = A (u / lambda); e1 = ||u - u0||; e2 = ||u + u0|| } until e1 <= eps or
+ * e2 <= eps or max_iter iterations.  ec = the last u (not unit-norm), lambda =
+ * the norm used in the last iteration.  Values are read as float and
+ * promoted to double (weighted-net.cu:295-297); a NULL val means every entry
+ * is 1 (U/CUEC/CUEC/CUEC_unweighted.cu:47-52).  Only the first 2*floor(nnz/2)
+ * entries are used (weighted-net.cu:61).  Vectors, norms and the stop test are
+ * FP64.  Returns BNA_NOT_CONVERGED (outputs still written) at max_iter. */
+int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr_dev, int32_t max_iter, double eps, double* ec_dev,
+               double* lambda, int32_t* iters, void* stream);
+
+/* Host-buffer form with the reference's signature shape:
+ * double Lead_Vector_GPU(int* R, int* C, double* V, long N, double* ec).
+ * V may be NULL (binary graph).  ec_host has N doubles. */
+int32_t bna_lead_vector(bna_ctx* ctx, const int32_t* R, const int32_t* C, const double* V,
+                        int64_t N, double* ec_host, double* lambda, int32_t* iters);
+
+/* .csr file (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:353-360 writer,
+ * W/CUEC/weighted-net.cu:275-287 reader): int32 Rlength=N+1; int32 R[N+1];
+ * int32 Clength; int32 C[Clength]; then, for a weighted graph, int32 Vlength;
+ * float V[Vlength].  Host buffers; bna_csr_read allocates (bna_csr_free_host). */
+int32_t bna_csr_write(const char* path, const bna_csr* csr_host);
+int32_t bna_csr_read(const char* path, bna_csr* csr_host_out);
+/* _ec.nm file (weighted-net.cu:309-318): int32 N; float ec[N]. */
+int32_t bna_ec_write(const char* path, const double* ec_host, int32_t N);
+
+/* Deterministic synthetic BOLD (factor model), float32 time-major [T][N]. */
+typedef enum bna_synth_kind { BNA_SYNTH_IID = 0, BNA_SYNTH_BLOCKNET = 1 } bna_synth_kind;
+typedef struct bna_synth_params {
+  int32_t N, T, K;
+  int32_t kind;      /* bna_synth_kind */
+  uint64_t seed;
+  double phi;        /* AR(1) coefficient of the factors */
+  double load_sd;    /* loading sd (IID) or network loading scale (BLOCKNET) */
+  double jitter_sd;  /* BLOCKNET: per-voxel loading sd */
+  int32_t block;     /* BLOCKNET: voxels per contiguous block */
+  int32_t n_net;     /* BLOCKNET: networks; block b belongs to network b mod n_net */
+} bna_synth_params;
+int bna_synth_bold(const bna_synth_params* p, float* out_host, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BNA_H */

@@ -1,0 +1,404 @@
+/*
+ * ORACLE — test infrastructure only.  Nothing in the product links or calls
+ * this file; tests/, the smoke check and bench.py's CPU-baseline leg use it
+ * as the checker.
+ *
+ * A plain-C restatement of the reference's CPU arithmetic for the
+ * correlation -> CSR -> eigenvector-centrality path ("W/" =
+ * BNAPlatform-weighted-win64-cuda7.0-20160331/src):
+ *   orc_zscore          CorMat_cpu normalisation   W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:923-951
+ *                       (identical to CorMat_gpu's  W/CorMat/CUCorMat/CUCorMat/CorMat.cu:24-52)
+ *   orc_cormat_packed   CorMat_cpu cross terms     CorMat.cpp:955-965, packed i<j row-major,
+ *                       then post_block's clamp    CorMat.cpp:883 (outside [-1,1] or NaN -> 0)
+ *   orc_threshold_csr   FormFullGraph + FormCSRGraph  CorMat.cpp:683-703, 889-918 (r rules),
+ *                       |r| rule of U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:198
+ *   orc_density         FormFullGraph_s + select   CorMat.cpp:705-822, 327-329
+ *   orc_ec              Lead_Vector_GPU            W/CUEC/weighted-net.cu:55-221 (FP64)
+ *   orc_cormat_mt_f32   CorMat_cpu_MT/Cross_term   U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:283-383
+ *                       (float accumulation; used as the multi-core CPU baseline)
+ * Built with -ffp-contract=off so every operation rounds like the reference's
+ * scalar code.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+enum { R_GT = 0, R_GE = 1, ABS_GT = 2, ABS_GE = 3 };
+
+/* z[i*T + t] (voxel-major) from bold[t*N + i] (time-major). */
+void orc_zscore(const float* bold, int N, int T, float* z) {
+  for (int i = 0; i < N; ++i) {
+    double sum1 = 0, sum2 = 0;
+    for (int l = 0; l < T; ++l) sum1 += bold[(size_t)l * N + i];
+    sum1 /= T;
+    for (int l = 0; l < T; ++l) {
+      const double d = bold[(size_t)l * N + i] - sum1;
+      sum2 += d * d;
+    }
+    sum2 = sqrt(sum2);
+    for (int l = 0; l < T; ++l) z[(size_t)i * T + l] = (float)((bold[(size_t)l * N + i] - sum1) / sum2);
+  }
+}
+
+/* The reference value of one pair: float products, double accumulation in
+ * time order, rounded to float; then post_block's clamp. */
+float orc_pair_r(const float* z, int T, int i, int j) {
+  const float* a = z + (size_t)i * T;
+  const float* b = z + (size_t)j * T;
+  double s = 0;
+  for (int l = 0; l < T; ++l) {
+    const float p = a[l] * b[l];
+    s += p;
+  }
+  const float r = (float)s;
+  return (r >= -1.0f && r <= 1.0f) ? r : 0.0f;
+}
+
+static int64_t packed_index(int64_t N, int64_t i, int64_t j) { /* i < j, CorMat.cpp:905 */
+  return i * N - (1 + i) * i / 2 + j - (i + 1);
+}
+
+struct pk_job { const float* z; int N, T, tid, nth; float* out; };
+
+static void* pk_worker(void* p) {
+  struct pk_job* jb = (struct pk_job*)p;
+  for (int i = jb->tid; i < jb->N; i += jb->nth)
+    for (int j = i + 1; j < jb->N; ++j)
+      jb->out[packed_index(jb->N, i, j)] = orc_pair_r(jb->z, jb->T, i, j);
+  return NULL;
+}
+
+/* packed[M1], M1 = N(N-1)/2, row-major over i < j. */
+void orc_cormat_packed(const float* z, int N, int T, float* packed, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  pthread_t th[256];
+  struct pk_job jobs[256];
+  if (nthreads > 256) nthreads = 256;
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t] = (struct pk_job){z, N, T, t, nthreads, packed};
+    if (t > 0) pthread_create(&th[t], NULL, pk_worker, &jobs[t]);
+  }
+  pk_worker(&jobs[0]);
+  for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+}
+
+static int is_edge(float r, int mode, float tau) {
+  switch (mode) {
+    case R_GT: return r > tau;
+    case ABS_GT: return fabsf(r) > tau;
+    case ABS_GE: return fabsf(r) >= tau;
+    default: return r >= tau;
+  }
+}
+
+/* Key of a pair for the density tie list. */
+static uint64_t pkey(int i, int j) { return ((uint64_t)(uint32_t)i << 32) | (uint32_t)j; }
+
+static int cmp_u64(const void* a, const void* b) {
+  const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+  return x < y ? -1 : x > y;
+}
+
+static int in_sorted(const uint64_t* k, int64_t n, uint64_t key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t m = (lo + hi) / 2;
+    if (k[m] < key) lo = m + 1; else hi = m;
+  }
+  return lo < n && k[lo] == key;
+}
+
+/* CSR of the thresholded graph straight from the packed triangle: row i lists
+ * columns j < i then j > i, ascending, as FormCSRGraph's row-major scan of the
+ * symmetric bool matrix does.  R has N+1 entries; C / V may be NULL (count
+ * only).  drop (sorted keys, may be NULL) removes listed pairs (density ties).
+ * Returns nnz (directed). */
+int64_t orc_threshold_csr(const float* packed, int N, int mode, float tau, const uint64_t* drop,
+                          int64_t ndrop, int32_t* R, int32_t* C, float* V) {
+  int64_t nnz = 0;
+  if (R) R[0] = 0;
+  for (int i = 0; i < N; ++i) {
+    for (int j = 0; j < N; ++j) {
+      if (j == i) continue;
+      const int a = i < j ? i : j, b = i < j ? j : i;
+      const float r = packed[packed_index(N, a, b)];
+      if (!is_edge(r, mode, tau)) continue;
+      if (drop && r == tau && in_sorted(drop, ndrop, pkey(a, b))) continue;
+      if (C) C[nnz] = j;
+      if (V) V[nnz] = r;
+      ++nnz;
+    }
+    if (R) R[i + 1] = (int32_t)nnz;
+  }
+  return nnz;
+}
+
+/* Density rule of FormFullGraph_s.  k = floor(2*M1*s/100) rounded up to even,
+ * halved (CorMat.cpp:327-329); tau = k-th largest packed value; edges r >= tau
+ * in row-major (i<j) scan order, where once the count exceeds k the most
+ * recent tie is removed (:797-808) — i.e. the earliest (k - #greater) ties in
+ * scan order are kept.  Writes the sorted keys of the dropped ties to
+ * drop_out (capacity drop_cap) and returns tau; *k_out = k, *ndrop_out = the
+ * number of dropped ties (-1 if drop_cap was too small). */
+float orc_density(const float* packed, int N, double s_percent, int64_t* k_out,
+                  uint64_t* drop_out, int64_t drop_cap, int64_t* ndrop_out) {
+  const int64_t M1 = (int64_t)N * (N - 1) / 2;
+  int64_t clen = (int64_t)(2 * M1 * s_percent / 100.0);
+  clen += clen % 2;
+  const int64_t k = clen / 2;
+  *k_out = k;
+  if (k <= 0) {
+    *ndrop_out = 0;
+    return INFINITY;
+  }
+  float* cp = (float*)malloc(sizeof(float) * (size_t)M1);
+  memcpy(cp, packed, sizeof(float) * (size_t)M1);
+  /* k-th largest by quickselect on a copy (the value is order-independent) */
+  int64_t lo = 0, hi = M1 - 1;
+  const int64_t want = k - 1;
+  while (lo < hi) {
+    const float pv = cp[lo + (hi - lo) / 2];
+    int64_t a = lo, b = hi;
+    while (a <= b) {
+      while (cp[a] > pv) ++a;
+      while (cp[b] < pv) --b;
+      if (a <= b) {
+        const float t = cp[a]; cp[a] = cp[b]; cp[b] = t;
+        ++a; --b;
+      }
+    }
+    if (want <= b) hi = b;
+    else if (want >= a) lo = a;
+    else break;
+  }
+  const float tau = cp[want];
+  free(cp);
+  int64_t greater = 0;
+  for (int64_t q = 0; q < M1; ++q) greater += packed[q] > tau;
+  int64_t keep = k - greater, nd = 0, idx = 0;
+  for (int i = 0; i < N; ++i)
+    for (int j = i + 1; j < N; ++j, ++idx) {
+      if (packed[idx] != tau) continue;
+      if (keep > 0) { --keep; continue; }
+      if (nd < drop_cap) drop_out[nd] = pkey(i, j);
+      ++nd;
+    }
+  if (nd > drop_cap) { *ndrop_out = -1; return tau; }
+  qsort(drop_out, (size_t)nd, sizeof(uint64_t), cmp_u64);
+  *ndrop_out = nd;
+  return tau;
+}
+
+/* Power iteration of Lead_Vector_GPU.  V may be NULL (every entry 1).
+ * Returns the iteration count; ec = last u, *lambda = norm used last. */
+int orc_ec(const int32_t* R, const int32_t* C, const double* V, int N, int max_iter, double eps,
+           double* ec, double* lambda, double* e1_out, double* e2_out) {
+  const int64_t nnz_used = 2 * (int64_t)(R[N] / 2);
+  double* u = (double*)malloc(sizeof(double) * (size_t)N);
+  double* u0 = (double*)malloc(sizeof(double) * (size_t)N);
+  double* y = (double*)malloc(sizeof(double) * (size_t)N);
+  for (int i = 0; i < N; ++i) u[i] = i;
+  double e1 = 1, e2 = 1, vnorm = 0;
+  int iter = 0;
+  while (e1 > eps && e2 > eps && iter < max_iter) {
+    memcpy(u0, u, sizeof(double) * (size_t)N);
+    double s = 0;
+    for (int i = 0; i < N; ++i) s += u[i] * u[i];
+    vnorm = sqrt(s);
+    const double inv = 1.0 / vnorm;
+    for (int i = 0; i < N; ++i) u[i] = u[i] * inv;
+    for (int i = 0; i < N; ++i) {
+      double acc = 0;
+      int64_t e = R[i + 1] < nnz_used ? R[i + 1] : nnz_used;
+      for (int64_t q = R[i]; q < e; ++q) acc += (V ? V[q] : 1.0) * u[C[q]];
+      y[i] = acc;
+    }
+    memcpy(u, y, sizeof(double) * (size_t)N);
+    double d1 = 0, d2 = 0;
+    for (int i = 0; i < N; ++i) {
+      const double a = u[i] - u0[i], b = u[i] + u0[i];
+      d1 += a * a;
+      d2 += b * b;
+    }
+    e1 = sqrt(d1);
+    e2 = sqrt(d2);
+    ++iter;
+  }
+  memcpy(ec, u, sizeof(double) * (size_t)N);
+  *lambda = vnorm;
+  if (e1_out) *e1_out = e1;
+  if (e2_out) *e2_out = e2;
+  free(u); free(u0); free(y);
+  return iter;
+}
+
+/* CorMat_cpu_MT arithmetic (old CPU tool): rows centred in float,
+ * m2 = sqrt(sum x^2 - (sum x)^2 / L) from double sums, float-accumulated
+ * cross products, r = sum3 / m2_i / m2_j (0 if a moment is 0).  Rows
+ * [row0, row1) against all j > i; values into packed (full M1 layout). */
+struct mt_job { const float* bt; const float* m2; int N, L, row0, row1, tid, nth; float* out; };
+
+static void* mt_worker(void* p) {
+  struct mt_job* jb = (struct mt_job*)p;
+  for (int i = jb->row0; i < jb->row1; ++i)
+    for (int j = i + 1 + jb->tid; j < jb->N; j += jb->nth) {
+      float s3 = 0;
+      for (int l = 0; l < jb->L; ++l) s3 += jb->bt[(size_t)i * jb->L + l] * jb->bt[(size_t)j * jb->L + l];
+      float r = s3 / jb->m2[i] / jb->m2[j];
+      if (jb->m2[i] == 0 || jb->m2[j] == 0) r = 0;
+      jb->out[packed_index(jb->N, i, j)] = r;
+    }
+  return NULL;
+}
+
+void orc_cormat_mt_f32(const float* bold, int N, int L, int row0, int row1, float* packed,
+                       int nthreads) {
+  float* bt = (float*)malloc(sizeof(float) * (size_t)N * L);
+  float* m2 = (float*)malloc(sizeof(float) * (size_t)N);
+  for (int l = 0; l < L; ++l)
+    for (int i = 0; i < N; ++i) bt[(size_t)i * L + l] = bold[(size_t)l * N + i];
+  for (int i = 0; i < N; ++i) {
+    double s1 = 0, s2 = 0;
+    float* row = bt + (size_t)i * L;
+    for (int l = 0; l < L; ++l) {
+      s1 += row[l];
+      s2 += row[l] * row[l];
+    }
+    m2[i] = (float)sqrt(s2 - s1 * s1 / L);
+    s1 /= L;
+    for (int l = 0; l < L; ++l) row[l] -= (float)s1;
+  }
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  struct mt_job jobs[256];
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t] = (struct mt_job){bt, m2, N, L, row0, row1, t, nthreads, packed};
+    if (t > 0) pthread_create(&th[t], NULL, mt_worker, &jobs[t]);
+  }
+  mt_worker(&jobs[0]);
+  for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+  free(bt);
+  free(m2);
+}
+
+/* Rows [row0, row1) of the thresholded CSR, straight from z (no packed
+ * triangle): the full-size parity check of a row slice.  R_local has
+ * row1-row0+1 entries (R_local[0] = 0); C / V may be NULL to count.
+ * Rows are split across threads; each row's columns are ascending. */
+struct rows_job {
+  const float* z; int N, T, mode; float tau; int row0, row1, tid, nth;
+  int64_t* cnt; int32_t* R; int32_t* C; float* V;
+};
+
+static void* rows_worker(void* p) {
+  struct rows_job* jb = (struct rows_job*)p;
+  for (int i = jb->row0 + jb->tid; i < jb->row1; i += jb->nth) {
+    int64_t c = 0;
+    int64_t base = jb->R ? jb->R[i - jb->row0] : 0;
+    for (int j = 0; j < jb->N; ++j) {
+      if (j == i) continue;
+      const float r = orc_pair_r(jb->z, jb->T, i < j ? i : j, i < j ? j : i);
+      if (!is_edge(r, jb->mode, jb->tau)) continue;
+      if (jb->C) jb->C[base + c] = j;
+      if (jb->V) jb->V[base + c] = r;
+      ++c;
+    }
+    if (jb->cnt) jb->cnt[i - jb->row0] = c;
+  }
+  return NULL;
+}
+
+int64_t orc_rows_csr(const float* z, int N, int T, int mode, float tau, int row0, int row1,
+                     int32_t* R_local, int32_t* C, float* V, int nthreads) {
+  const int nr = row1 - row0;
+  int64_t* cnt = (int64_t*)calloc((size_t)nr + 1, sizeof(int64_t));
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  struct rows_job jobs[256];
+  for (int pass = 0; pass < (C ? 2 : 1); ++pass) {
+    for (int t = 0; t < nthreads; ++t) {
+      jobs[t] = (struct rows_job){z, N, T, mode, tau, row0, row1, t, nthreads,
+                                  pass == 0 ? cnt : NULL, pass == 0 ? NULL : R_local,
+                                  pass == 0 ? NULL : C, pass == 0 ? NULL : V};
+      if (t > 0) pthread_create(&th[t], NULL, rows_worker, &jobs[t]);
+    }
+    rows_worker(&jobs[0]);
+    for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+    if (pass == 0) {
+      int64_t s = 0;
+      for (int q = 0; q < nr; ++q) {
+        if (R_local) R_local[q] = (int32_t)s;
+        s += cnt[q];
+      }
+      if (R_local) R_local[nr] = (int32_t)s;
+    }
+  }
+  int64_t total = 0;
+  for (int q = 0; q < nr; ++q) total += cnt[q];
+  free(cnt);
+  return total;
+}
+
+/* CPU baseline: the reference's multi-threaded correlation tool
+ * (CorMat_cpu_MT / Cross_term, U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:283-383:
+ * float-centred rows, float-accumulated cross terms, r = sum3 / m2_i / m2_j,
+ * j strided by thread id) over rows [row0, row1) against every j > i, with
+ * its threshold rule |r| > tau (CorMat_CPU.cpp:198) counted in place instead
+ * of stored (so a bounded row sample needs no N x N buffer).  Returns the
+ * number of undirected edges. */
+struct mtc_job { const float* bt; const float* m2; int N, L, row0, row1, tid, nth; float tau; int64_t cnt; };
+
+static void* mtc_worker(void* p) {
+  struct mtc_job* jb = (struct mtc_job*)p;
+  int64_t c = 0;
+  for (int i = jb->row0; i < jb->row1; ++i)
+    for (int j = i + 1 + jb->tid; j < jb->N; j += jb->nth) {
+      float s3 = 0;
+      for (int l = 0; l < jb->L; ++l) s3 += jb->bt[(size_t)i * jb->L + l] * jb->bt[(size_t)j * jb->L + l];
+      float r = s3 / jb->m2[i] / jb->m2[j];
+      if (jb->m2[i] == 0 || jb->m2[j] == 0) r = 0;
+      c += fabsf(r) > jb->tau;
+    }
+  jb->cnt = c;
+  return NULL;
+}
+
+int64_t orc_rows_mt_f32_count(const float* bold, int N, int L, int row0, int row1, float tau,
+                              int nthreads) {
+  float* bt = (float*)malloc(sizeof(float) * (size_t)N * L);
+  float* m2 = (float*)malloc(sizeof(float) * (size_t)N);
+  for (int l = 0; l < L; ++l)
+    for (int i = 0; i < N; ++i) bt[(size_t)i * L + l] = bold[(size_t)l * N + i];
+  for (int i = 0; i < N; ++i) {
+    double s1 = 0, s2 = 0;
+    float* row = bt + (size_t)i * L;
+    for (int l = 0; l < L; ++l) {
+      s1 += row[l];
+      s2 += row[l] * row[l];
+    }
+    m2[i] = (float)sqrt(s2 - s1 * s1 / L);
+    s1 /= L;
+    for (int l = 0; l < L; ++l) row[l] -= (float)s1;
+  }
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  struct mtc_job jobs[256];
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t] = (struct mtc_job){bt, m2, N, L, row0, row1, t, nthreads, tau, 0};
+    if (t > 0) pthread_create(&th[t], NULL, mtc_worker, &jobs[t]);
+  }
+  mtc_worker(&jobs[0]);
+  int64_t total = jobs[0].cnt;
+  for (int t = 1; t < nthreads; ++t) {
+    pthread_join(th[t], NULL);
+    total += jobs[t].cnt;
+  }
+  free(bt);
+  free(m2);
+  return total;
+}

@@ -1,0 +1,174 @@
+"""Parity of the CUDA path (libbna.so through its C ABI) with the oracle and
+with the reference's golden outputs.  Bar: z-scores, row_ptr and col_idx
+bit-exact; val within the recompute band delta of the reference value (and
+bit-exact for every pair the band recomputed); centrality within 1e-5
+relative."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import cuda_newest20160331_gb300 as bna
+import oracle
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+PRECISIONS = ["fp32"]
+
+
+def dev(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def assert_csr_equal(res, R, C, V, delta, exact_vals=None):
+    g = res.numpy()
+    assert np.array_equal(g.row_ptr, R), "row_ptr differs"
+    assert np.array_equal(g.col_idx, C), "col_idx differs"
+    if V is not None:
+        assert g.val is not None
+        err = np.max(np.abs(g.val - V)) if len(V) else 0.0
+        assert err <= delta, f"val error {err} > delta {delta}"
+
+
+def test_zscore_bit_exact(builder):
+    for N, T in [(1, 5), (127, 33), (300, 240), (1000, 7), (129, 1200)]:
+        b = bna.synth_bold(N, T, 10, N + T)
+        if N > 5:
+            b[:, 3] = 1.25  # zero-variance voxel -> NaN row
+        z = builder.zscore(dev(b)).cpu().numpy()
+        ref = oracle.zscore(b)
+        assert z.shape[1] >= T and not z[:, T:].any()
+        assert np.array_equal(z[:, :T], ref, equal_nan=True), (N, T)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("N,T,mode,tau", [
+    (2, 10, "r_gt", -1.0), (127, 33, "r_gt", 0.3), (128, 240, "r_ge", 0.2),
+    (129, 64, "abs_gt", 0.3), (300, 17, "abs_ge", 0.45), (1000, 240, "r_gt", 0.25),
+    (700, 50, "r_ge", 0.0),
+])
+def test_corr_csr_matches_oracle(builder, precision, N, T, mode, tau):
+    b = bna.synth_bold(N, T, 12, 7 * N + T)
+    R, C, V = oracle.csr_corr(b, mode, tau)
+    res = builder.corr_csr(dev(b), mode=mode, value=tau, precision=precision)
+    assert_csr_equal(res, R, C, V, res.stats["delta"])
+    assert res.nnz == len(C)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_binary_graph_and_zero_variance(builder, precision):
+    b = bna.synth_bold(260, 40, 8, 99)
+    b[:, 5] = 3.0
+    b[:, 200] = -1.0
+    R, C, V = oracle.csr_corr(b, "r_gt", 0.2, weighted=False)
+    res = builder.corr_csr(dev(b), mode="r_gt", value=0.2, precision=precision, weighted=False)
+    assert res.val is None
+    assert_csr_equal(res, R, C, None, 0)
+    # a negative threshold makes the clamped (NaN -> 0) pairs of a constant voxel edges
+    R, C, V = oracle.csr_corr(b, "r_gt", -0.05)
+    res = builder.corr_csr(dev(b), mode="r_gt", value=-0.05, precision=precision)
+    assert_csr_equal(res, R, C, V, res.stats["delta"])
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name,N,T,K,seed,mode,value", [
+    ("small_c1", 4096, 240, 20, 1, "r_ge", 0.5),
+    ("n300_t33_gt", 300, 33, 20, 11, "r_gt", 0.3),
+    ("n129_t240_ge", 129, 240, 20, 12, "r_ge", 0.25),
+    ("n1000_t64_gt", 1000, 64, 10, 13, "r_gt", 0.45),
+])
+def test_corr_csr_matches_reference_golden(builder, precision, name, N, T, K, seed, mode, value):
+    gold = np.load(os.path.join(GOLD, "ref_cases.npz"))
+    b = bna.synth_bold(N, T, K, seed)
+    assert hashlib.sha256(b.tobytes()).digest() == gold[name + "_sha"].tobytes()
+    res = builder.corr_csr(dev(b), mode=mode, value=value, precision=precision)
+    assert_csr_equal(res, gold[name + "_R"], gold[name + "_C"], gold[name + "_V"],
+                     res.stats["delta"])
+
+
+def test_host_buffer_path_equals_device_path(builder):
+    b = bna.synth_bold(1000, 64, 10, 13)
+    h = builder.corr_csr_host(b, mode="r_gt", value=0.45)
+    d = builder.corr_csr(dev(b), mode="r_gt", value=0.45).numpy()
+    assert np.array_equal(h.row_ptr, d.row_ptr) and np.array_equal(h.col_idx, d.col_idx)
+    assert np.array_equal(h.val, d.val)
+
+
+def test_repeat_calls_are_deterministic(builder):
+    b = dev(bna.synth_bold(2000, 120, 20, 5))
+    r1 = builder.corr_csr(b, mode="r_gt", value=0.3).numpy()
+    r2 = builder.corr_csr(b, mode="r_gt", value=0.3).numpy()
+    assert np.array_equal(r1.col_idx, r2.col_idx) and np.array_equal(r1.val, r2.val)
+
+
+def test_full_size_workload_slice(builder):
+    """N=45,000 x T=240 (the benchmark workload): rows of three slices equal the
+    oracle; symmetry, ascending columns and no diagonal over the whole CSR."""
+    import json
+    w = json.load(open(os.path.join(GOLD, "workload_tau.json")))
+    b = bna.synth_bold(w["N"], w["T"], w["K"], w["seed"])
+    tau = w["tau_f32"]
+    res = builder.corr_csr(dev(b), mode="r_ge", value=tau, precision="fp32")
+    g = res.numpy()
+    n = w["N"]
+    # about 1 % density (tau is the FP64 quantile)
+    assert abs(res.nnz - 2 * w["k"]) < 0.001 * 2 * w["k"]
+    rp, ci = g.row_ptr.astype(np.int64), g.col_idx
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    assert not np.any(ci == rows)
+    d = np.diff(ci)
+    starts = rp[1:-1][np.diff(rp)[1:] > 0]
+    ok = np.ones(len(ci), bool)
+    ok[starts] = False
+    assert np.all(d[ok[1:]] > 0) if len(d) else True
+    key = rows.astype(np.int64) * n + ci
+    tkey = ci.astype(np.int64) * n + rows
+    assert np.array_equal(np.sort(key), np.sort(tkey))
+    z = oracle.zscore(b)
+    for r0, r1 in [(0, 96), (22500, 22560), (n - 70, n)]:
+        R, C, V = oracle.rows_csr(z, "r_ge", tau, r0, r1)
+        assert np.array_equal(g.row_ptr[r0:r1 + 1] - g.row_ptr[r0], R)
+        assert np.array_equal(g.col_idx[g.row_ptr[r0]:g.row_ptr[r1]], C)
+        assert np.max(np.abs(g.val[g.row_ptr[r0]:g.row_ptr[r1]] - V)) <= res.stats["delta"]
+
+
+def test_ec_matches_oracle(builder):
+    gold = np.load(os.path.join(GOLD, "ref_cases.npz"))
+    for name in ["small_c1", "n1000_t64_gt", "n1500_t240_dens1"]:
+        R, C, V = gold[name + "_R"], gold[name + "_C"], gold[name + "_V"]
+        ec_o, lam_o, it_o, conv_o = oracle.ec(R, C, V.astype(np.float64))
+        import torch
+        csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), dev(V), {})
+        ec, lam, it, conv = builder.ec(csr)
+        ec = ec.cpu().numpy()
+        assert conv == conv_o
+        assert abs(it - it_o) <= 1, (it, it_o)
+        scale = np.max(np.abs(ec_o))
+        assert np.max(np.abs(ec - ec_o)) <= 1e-5 * scale, name
+        assert abs(lam - lam_o) <= 1e-5 * abs(lam_o)
+        # binary graph (V := 1)
+        ec_o, lam_o, it_o, _ = oracle.ec(R, C)
+        csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), None, {})
+        ec, lam, it, _ = builder.ec(csr)
+        assert np.max(np.abs(ec.cpu().numpy() - ec_o)) <= 1e-5 * np.max(np.abs(ec_o))
+
+
+def test_lead_vector_known_answer_4node(builder):
+    R = np.array([0, 2, 3, 6, 8], np.int32)
+    C = np.array([2, 3, 2, 0, 1, 3, 0, 2], np.int32)
+    ec, lam, it, conv = builder.lead_vector(R, C)
+    ec_o, lam_o, it_o, _ = oracle.ec(R, C)
+    assert conv and abs(lam - lam_o) < 1e-9 and np.allclose(ec, ec_o, rtol=1e-9, atol=1e-12)
+    ec2, lam2, _, _ = builder.lead_vector(R, C, np.full(8, 2.0))
+    assert abs(lam2 - 2 * lam) < 1e-9
+
+
+def test_ec_not_converged_reports_status(builder):
+    R = np.array([0, 1, 2], np.int32)
+    C = np.array([1, 0], np.int32)  # bipartite pair: +-1 eigenvalues, e2 -> 0 quickly
+    csr = bna.CsrResult(2, 2, dev(R), dev(C), None, {})
+    ec, lam, it, conv = builder.ec(csr, max_iter=1)
+    ec_o, lam_o, it_o, conv_o = oracle.ec(R, C, max_iter=1)
+    assert it == it_o == 1 and conv == conv_o

@@ -1,0 +1,122 @@
+"""Host-side checks of libbna.so that need no GPU: the C ABI exports, the
+synthetic generator, the .csr / _ec.nm formats and argument errors."""
+import ctypes as C
+import hashlib
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cuda_newest20160331_gb300 as bna
+from cuda_newest20160331_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "bna.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(bna_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_header_symbol():
+    lib = bna.lib()
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    # the ctypes signature table covers the whole header
+    assert set(names) == set(L.SIGNATURES)
+
+
+def test_status_strings():
+    lib = bna.lib()
+    assert lib.bna_status_string(0) == b"ok"
+    assert b"int32" in lib.bna_status_string(3)
+    assert lib.bna_version().startswith(b"bna-gb300")
+
+
+def test_ctx_create_without_gpu_reports_no_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert bna.lib().bna_ctx_create(0, C.byref(h)) == 7  # BNA_NO_DEVICE
+
+
+def test_synth_is_thread_invariant_and_pinned():
+    a = bna.synth_bold(700, 120, 20, 1, threads=1)
+    b = bna.synth_bold(700, 120, 20, 1, threads=5)
+    assert np.array_equal(a, b)
+    assert a.dtype == np.float32 and a.shape == (120, 700)
+    # statistics of the factor model: unit noise + 20 * 0.09 loading variance
+    assert 2.2 < a.var() < 3.4
+    pins = json.load(open(os.path.join(GOLD, "synth_sha256.json")))
+    for key, want in pins.items():
+        N, T, K, seed, kind = key.split(",")
+        x = bna.synth_bold(int(N), int(T), int(K), int(seed), kind=kind,
+                           **({"load_sd": 0.117, "jitter_sd": 0.08} if kind == "blocknet" else {}))
+        assert hashlib.sha256(x.tobytes()).hexdigest() == want, key
+
+
+def test_csr_roundtrip_weighted_and_binary(tmp_path):
+    rp = np.array([0, 2, 3, 6, 8], np.int32)
+    ci = np.array([2, 3, 2, 0, 1, 3, 0, 2], np.int32)
+    v = np.linspace(0.1, 0.8, 8).astype(np.float32)
+    p = str(tmp_path / "g_weighted.csr")
+    bna.csr_write(p, rp, ci, v)
+    raw = open(p, "rb").read()
+    # int Rlength; R; int Clength; C; int Clength; V  (CorMat.cpp:353-360)
+    assert len(raw) == 4 + 5 * 4 + 4 + 8 * 4 + 4 + 8 * 4
+    assert np.frombuffer(raw[:4], np.int32)[0] == 5
+    r2, c2, v2 = bna.csr_read(p)
+    assert np.array_equal(r2, rp) and np.array_equal(c2, ci) and np.array_equal(v2, v)
+    pb = str(tmp_path / "g.csr")
+    bna.csr_write(pb, rp, ci)
+    r3, c3, v3 = bna.csr_read(pb)
+    assert v3 is None and np.array_equal(c3, ci)
+
+
+def test_csr_read_rejects_damaged_files(tmp_path):
+    rp = np.array([0, 1, 2], np.int32)
+    ci = np.array([1, 0], np.int32)
+    v = np.ones(2, np.float32)
+    p = str(tmp_path / "a.csr")
+    bna.csr_write(p, rp, ci, v)
+    raw = bytearray(open(p, "rb").read())
+    bad = tmp_path / "bad.csr"
+    bad.write_bytes(bytes(raw[:-3]))  # truncated V
+    with pytest.raises(bna.BnaError) as e:
+        bna.csr_read(str(bad))
+    assert e.value.status == 9
+    raw2 = bytearray(raw)
+    raw2[4 + 12 + 4 + 8: 4 + 12 + 4 + 8 + 4] = np.int32(3).tobytes()  # Vlength != Clength
+    bad.write_bytes(bytes(raw2))
+    with pytest.raises(bna.BnaError):
+        bna.csr_read(str(bad))
+    raw3 = bytearray(raw)
+    raw3[4 + 12 + 4: 4 + 12 + 8] = np.int32(7).tobytes()  # column out of range
+    bad.write_bytes(bytes(raw3))
+    with pytest.raises(bna.BnaError):
+        bna.csr_read(str(bad))
+    with pytest.raises(bna.BnaError) as e:
+        bna.csr_read(str(tmp_path / "missing.csr"))
+    assert e.value.status == 8
+
+
+def test_ec_file_format(tmp_path):
+    p = str(tmp_path / "x_ec.nm")
+    bna.ec_write(p, np.array([1.5, 2.25, -3.0]))
+    raw = open(p, "rb").read()
+    assert np.frombuffer(raw[:4], np.int32)[0] == 3
+    assert np.array_equal(np.frombuffer(raw[4:], np.float32), np.array([1.5, 2.25, -3.0], np.float32))
+
+
+def test_bad_arguments_fail_loudly():
+    with pytest.raises(ValueError):
+        bna._opts("nope", 0.5, "fp32", True, None)
+    p = L.SynthParams(N=-1, T=10, K=1)
+    assert bna.lib().bna_synth_bold(C.byref(p), None, 1) == 1
