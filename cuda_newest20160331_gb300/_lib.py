@@ -71,6 +71,8 @@ SIGNATURES = {
                                          C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "bna_ec": (C.c_int32, [C.c_void_p, C.POINTER(Csr), C.c_int32, C.c_double, C.c_void_p,
                            C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_void_p]),
+    "bna_ec_noalloc": (C.c_int32, [C.POINTER(Csr), C.c_int32, C.c_double, C.c_void_p,
+                                   C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_void_p]),
     "bna_lead_vector": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                     C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "bna_csr_write": (C.c_int32, [C.c_char_p, C.POINTER(Csr)]),

@@ -217,6 +217,7 @@ const char* bna_status_string(int32_t s) {
     case BNA_CORRUPT_FILE: return "corrupt file";
     case BNA_INTERNAL: return "internal consistency check failed";
     case BNA_UNSUPPORTED: return "unsupported";
+    case BNA_SCRATCH_LIMIT: return "problem exceeds the fixed scratch of the no-allocation entry point";
     default: return "unknown status";
   }
 }

@@ -42,7 +42,8 @@ typedef enum bna_status {
   BNA_IO_ERROR = 8,
   BNA_CORRUPT_FILE = 9,       /* .csr lengths inconsistent (W/CUEC/weighted-net.cu:283) */
   BNA_INTERNAL = 10,          /* an internal consistency check failed */
-  BNA_UNSUPPORTED = 11
+  BNA_UNSUPPORTED = 11,
+  BNA_SCRATCH_LIMIT = 12      /* problem larger than bna_ec_noalloc's fixed scratch */
 } bna_status;
 
 /* Threshold rules.  r below is the reference's value after post_block
@@ -161,6 +162,21 @@ int32_t bna_zscore_ld(int32_t T);
  * FP64.  Returns BNA_NOT_CONVERGED (outputs still written) at max_iter. */
 int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr_dev, int32_t max_iter, double eps, double* ec_dev,
                double* lambda, int32_t* iters, void* stream);
+
+/* Eigenvector centrality without any allocation.  No counterpart in the
+ * reference: for callers that cannot allocate device memory when they need
+ * the result (a host callback or allocator hook, a process whose device
+ * memory is held by its own pool, an embedder that forbids allocation after
+ * load).  Same kernels and results as bna_ec, but the working vectors and
+ * iteration state live in a fixed __device__ array of the library (about
+ * 4 MB, kept by every GPU that loads the library until exit), so the call
+ * allocates nothing; no context is needed.  Limit: n <= 262,144 vertices,
+ * else BNA_SCRATCH_LIMIT.  All calls share that array: calls that overlap on
+ * a GPU race, so serialise them.  The first call on a device looks up the
+ * array's address (once per device); make it before any stream capture.
+ * Synchronous: returns after ec_dev is written. */
+int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, double eps, double* ec_dev,
+                       double* lambda, int32_t* iters, void* stream);
 
 /* Host-buffer form with the reference's signature shape:
  * double Lead_Vector_GPU(int* R, int* C, double* V, long N, double* ec).
