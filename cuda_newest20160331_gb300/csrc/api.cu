@@ -35,6 +35,11 @@ cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const fl
                            cudaStream_t stream);
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done);
+void tc_tile_list(int nb, std::vector<int2>& out);
+cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
+cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
+                           const uint8_t* blockbad, float* dump, int dump_half, int grid,
+                           cudaStream_t st);
 }  // namespace bna
 
 using namespace bna;
@@ -44,7 +49,7 @@ namespace {
 enum Slot {
   S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
-  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_COUNT
+  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -79,6 +84,8 @@ struct bna_ctx {
   std::string last_error;
   long long cand_cap = 1 << 20;
   EcGraph ecg;
+  int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
+  int ntiles = 0;
 };
 
 namespace {
@@ -189,9 +196,32 @@ int32_t run_zscore(bna_ctx* ctx, const float* bold, int N, int T, bool need_bf16
   return BNA_OK;
 }
 
+// Tensor-core preparation: per-block NaN flags and the upper-triangle tile list.
+int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
+  uint8_t* bb;
+  ENSURE(S_BLOCKBAD, (size_t)a.nb, bb);
+  CK(launch_block_bad(a.bad, a.nb, bb, st));
+  if (ctx->tiles_nb != a.nb) {
+    std::vector<int2> t;
+    tc_tile_list(a.nb, t);
+    int2* d;
+    ENSURE(S_TILES, t.size() * sizeof(int2), d);
+    CK(cudaMemcpyAsync(d, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    ctx->tiles_nb = a.nb;
+    ctx->ntiles = (int)t.size();
+  }
+  return BNA_OK;
+}
+
 int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st) {
   switch (precision) {
     case BNA_PREC_FP32: CK(launch_corr_simt(a, pass, st)); return BNA_OK;
+    case BNA_PREC_BF16X3:
+      CK(launch_corr_tc(a, pass, reinterpret_cast<const int2*>(ctx->ptr[S_TILES]), ctx->ntiles,
+                        reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
+                        ctx->sms, st));
+      return BNA_OK;
     default:
       return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built in this library", precision);
   }
@@ -329,6 +359,10 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   CK(cudaEventRecord(ctx->ev[0], st));
   s = run_zscore(ctx, bold_dev, N, T, prec != BNA_PREC_FP32, a, st);
   if (s) return s;
+  if (prec == BNA_PREC_BF16X3) {
+    s = tc_prepare(ctx, a, st);
+    if (s) return s;
+  }
   CK(cudaEventRecord(ctx->ev[1], st));
   a.th.mode = opts->mode;
   a.th.tau = (float)opts->value;
@@ -380,6 +414,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     }
     break;
   }
+  if (hs->err & ERR_TIMEOUT) return fail(ctx, BNA_TIMEOUT, "count pass: a bounded wait expired");
   if (hs->err & ERR_BAND_OVERFLOW)
     return fail(ctx, BNA_INTERNAL, "candidate list overflow (%llu candidates)", hs->cand_count);
   if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
@@ -395,13 +430,16 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   a.row_ptr = row_ptr;
   a.col_idx = col;
   a.val = val;
+  a.nnz = nnz;
   s = corr_pass(ctx, a, prec, 1, st);
   if (s) return s;
   ++passes;
   CK(cudaEventRecord(ctx->ev[5], st));
   CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  if (hs->err & ERR_TIMEOUT) return fail(ctx, BNA_TIMEOUT, "fill pass: a bounded wait expired");
   if (hs->err & ERR_HASH_MISS) return fail(ctx, BNA_INTERNAL, "fill pass missed a candidate");
+  if (hs->err & ERR_RANGE) return fail(ctx, BNA_INTERNAL, "fill pass position out of range");
   out_dev->n = N;
   out_dev->nnz = nnz;
   out_dev->row_ptr = row_ptr;
@@ -416,8 +454,8 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     stats->band_edges = (int64_t)band_edges;
     stats->band_1e6 = (int64_t)band_1e6;
     stats->passes = passes;
-    // z-score, count, recompute, 4 scan kernels, fill
-    stats->kernel_launches = 1 + passes + 1 + 4;
+    // z-score, [block flags], count, recompute, 4 scan kernels, fill
+    stats->kernel_launches = 1 + (prec == BNA_PREC_BF16X3 ? 1 : 0) + passes + 1 + 4;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);
@@ -488,6 +526,18 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
     return fail(ctx, BNA_BAD_ARG, "tile (%d, %d) outside the %d-block grid", I, J, a.nb);
   switch (precision) {
     case BNA_PREC_FP32: CK(launch_corr_simt_dump(a, I, J, out_dev, st)); break;
+    case BNA_PREC_BF16X3: {
+      uint8_t* bb;
+      ENSURE(S_BLOCKBAD, (size_t)a.nb, bb);
+      CK(launch_block_bad(a.bad, a.nb, bb, st));
+      int2* d;
+      ENSURE(S_DUMPTILE, sizeof(int2), d);
+      const int2 t = make_int2(I, J / 2);
+      CK(cudaMemcpyAsync(d, &t, sizeof t, cudaMemcpyHostToDevice, st));
+      CK(launch_corr_tc(a, 2, d, 1, bb, out_dev, J % 2, 1, st));
+      CK(cudaStreamSynchronize(st));
+      break;
+    }
     default: return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built", precision);
   }
   return BNA_OK;

@@ -19,6 +19,8 @@ enum : uint32_t {
   ERR_HASH_FULL = 4u,
   ERR_NNZ_INT32 = 8u,
   ERR_TIES = 16u,           // density: tie bookkeeping inconsistent
+  ERR_TIMEOUT = 32u,        // a bounded wait in a tensor-core kernel expired
+  ERR_RANGE = 64u,          // a fill-pass position fell outside the CSR (write skipped)
 };
 
 // Outcome of classifying one approximate correlation.
@@ -72,6 +74,7 @@ struct CorrArgs {
   const int32_t* row_ptr;    // [n+1] (fill pass)
   int32_t* col_idx;          // [nnz]
   float* val;                // [nnz] or null
+  long long nnz;             // fill pass: entries of col_idx / val (positions are checked)
   // near-threshold candidates (count pass appends, recompute resolves)
   uint2* cand;               // (i, j) with i < j
   unsigned long long* cand_count;
@@ -87,6 +90,17 @@ struct CorrArgs {
   uint32_t* err;
   unsigned long long* stats;  // [0]=band edges [1]=band within 1e-6
 };
+
+// Fill-pass store with a range check (an inconsistent count would otherwise
+// write outside the CSR).
+__device__ __forceinline__ void put_edge(const CorrArgs& a, long long pos, int col, float v) {
+  if (pos < 0 || pos >= a.nnz) {
+    atomicOr(a.err, ERR_RANGE);
+    return;
+  }
+  a.col_idx[pos] = col;
+  if (a.weighted) a.val[pos] = v;
+}
 
 __device__ __forceinline__ unsigned long long pair_key(int i, int j) {
   return ((unsigned long long)(uint32_t)i << 32) | (uint32_t)j;

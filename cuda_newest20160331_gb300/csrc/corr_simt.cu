@@ -213,12 +213,8 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
         if (ii == i && jj == j) v = acc[ii][jj];
     const int pr = rowbase[il] + popc_before(rowmask[il], jl);
     const int pc = colbase[jl] + popc_before(colmask[jl], il);
-    a.col_idx[pr] = j0 + jl;
-    a.col_idx[pc] = i0 + il;
-    if (a.weighted) {
-      a.val[pr] = v;
-      a.val[pc] = v;
-    }
+    put_edge(a, pr, j0 + jl, v);
+    put_edge(a, pc, i0 + il, v);
   }
 }
 

@@ -1,0 +1,485 @@
+// Split-BF16 correlation -> CSR on the tcgen05 tensor cores.
+//
+// Reference: the same tile loop as the plain form (CorMat_gpu's cublasSgemm
+// tiles, W/CorMat/CUCorMat/CUCorMat/CorMat.cu:87-154, then post_block /
+// FormFullGraph / FormCSRGraph, CorMat.cpp:824-918), here as one persistent,
+// warp-specialised kernel per pass:
+//
+//   warp 0      TMA producer: per K block of 64, loads A = Z[I-block] (128 rows)
+//               and B = Z[2 column blocks] (256 rows) as BF16 hi and lo parts,
+//               128-byte swizzled, into a 2-stage shared-memory ring;
+//   warp 1      MMA issuer (one thread): per K16 step three tcgen05.mma
+//               (hi*hi, hi*lo, lo*hi) accumulate a 128 x 256 FP32 tile in TMEM;
+//               two TMEM accumulators (512 columns) so the epilogue of tile t
+//               overlaps the MMAs of tile t+1;
+//   warps 2..9  epilogue: each 128 x 128 half-tile is read from TMEM by four
+//               warps (one per 32-lane quadrant, thread = row), thresholded in
+//               registers, and compacted with the same count / fill scheme as
+//               the plain form: row bitmasks in registers, column bitmasks by a
+//               32 x 32 bit transpose across the warp, ranks by popcount.
+//
+// Every wait is bounded (4 s of wall time); on expiry the kernel raises
+// ERR_TIMEOUT, drains its own copies and MMAs, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "tc_ptx.cuh"
+
+namespace bna {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BN = 256;
+constexpr int TC_BK = 64;  // BF16 elements per K block (one 128-byte row)
+constexpr int TC_STAGES = 2;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;                    // 16 KB
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;                    // 32 KB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB
+constexpr int TC_THREADS = 320;
+constexpr int TC_EPI_THREADS = 256;
+constexpr uint32_t TC_TMEM_COLS = 512;
+constexpr uint64_t kWaitNs = 4000000000ull;
+
+struct TcSmem {
+  uint64_t full[TC_STAGES], empty[TC_STAGES], tfull[2], tempty[2], done, hbar[2];
+  uint32_t tmem_base;
+  volatile uint32_t abort;
+  uint32_t colmask[2][128][4];
+  int colbase[2][128];
+};
+
+constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_STAGES * TC_STAGE_BYTES + sizeof(TcSmem);
+
+struct TcArgs {
+  CorrArgs a;
+  const int2* tiles;        // (I, Jp): rows of block I x columns of blocks 2Jp, 2Jp+1
+  int ntiles;
+  int nk16;                 // K16 steps = ceil(T / 16)
+  const uint8_t* blockbad;  // [nb]: block holds a voxel with NaN z
+  float* dump;              // dump pass: 128 x 128 values of half `dump_half`
+  int dump_half;
+};
+
+// 32 x 32 bit transpose across a warp: lane L holds row L on entry and
+// column L on exit (bit b of the result = bit L of lane b's input).
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+  const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int j = 16 >> s;
+    const uint32_t m = masks[s];
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y & ~m) >> j)) : ((x & m) | ((y & m) << j));
+  }
+  return x;
+}
+
+// Bounded barrier of the 128 threads of one half (mbarrier based, so a lost
+// peer cannot hang the CTA).
+__device__ __forceinline__ bool half_sync(TcSmem& S, int h, uint32_t& phase) {
+  const uint32_t bar = ptx::smem_u32(&S.hbar[h]);
+  ptx::mbar_arrive(bar);
+  const bool ok = ptx::mbar_wait(bar, phase, kWaitNs);
+  phase ^= 1u;
+  return ok;
+}
+
+template <int PASS>
+__device__ __forceinline__ void resolve_special(const CorrArgs& a, int gi, int gj, uint32_t bit,
+                                                uint32_t& eb) {
+  if (PASS == 0) {
+    push_candidate(a, gi, gj);
+  } else {
+    float v;
+    bool e;
+    hash_lookup(a, pair_key(gi, gj), v, e);
+    if (e) eb |= bit;
+  }
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    corr_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
+                   const __grid_constant__ CUtensorMap tm_lo, const TcArgs p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  TcSmem& S = *reinterpret_cast<TcSmem*>(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const CorrArgs& a = p.a;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      ptx::mbar_init(ptx::smem_u32(&S.full[s]), 1);
+      ptx::mbar_init(ptx::smem_u32(&S.empty[s]), 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      ptx::mbar_init(ptx::smem_u32(&S.tfull[s]), 1);
+      ptx::mbar_init(ptx::smem_u32(&S.tempty[s]), TC_EPI_THREADS);
+      ptx::mbar_init(ptx::smem_u32(&S.hbar[s]), 128);
+    }
+    ptx::mbar_init(ptx::smem_u32(&S.done), 1);
+    S.abort = 0;
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(ptx::smem_u32(&S.tmem_base), TC_TMEM_COLS);
+    ptx::tmem_relinquish();
+  }
+  if (warp == 0 && lane == 0) {
+    ptx::prefetch_tensormap(&tm_hi);
+    ptx::prefetch_tensormap(&tm_lo);
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = S.tmem_base;
+  const int nkb = (p.nk16 + 3) / 4;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      uint32_t f = 0;
+      int last_round[TC_STAGES];
+      for (int s = 0; s < TC_STAGES; ++s) last_round[s] = -1;
+      for (int t = blockIdx.x; t < p.ntiles && !S.abort; t += gridDim.x) {
+        const int2 tile = p.tiles[t];
+        for (int kb = 0; kb < nkb; ++kb, ++f) {
+          const int s = f % TC_STAGES;
+          const uint32_t round = f / TC_STAGES;
+          const uint32_t empty = ptx::smem_u32(&S.empty[s]);
+          if (!ptx::mbar_wait(empty, (round & 1u) ^ 1u, kWaitNs)) {
+            atomicOr(a.err, ERR_TIMEOUT);
+            S.abort = 1;
+            break;
+          }
+          const uint32_t full = ptx::smem_u32(&S.full[s]);
+          const uint32_t base = ptx::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
+          ptx::mbar_arrive_expect_tx(full, TC_STAGE_BYTES);
+          const int k0 = kb * TC_BK;
+          const int ra = tile.x * TC_BM, rb = tile.y * TC_BN;
+          ptx::tma_load_2d(base, &tm_hi, full, k0, ra);
+          ptx::tma_load_2d(base + TC_A_BYTES, &tm_lo, full, k0, ra);
+          ptx::tma_load_2d(base + 2 * TC_A_BYTES, &tm_hi, full, k0, rb);
+          ptx::tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES / 2, &tm_hi, full, k0, rb + 128);
+          ptx::tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES, &tm_lo, full, k0, rb);
+          ptx::tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES + TC_B_BYTES / 2, &tm_lo, full,
+                           k0, rb + 128);
+          last_round[s] = (int)round;
+        }
+      }
+      // drain: every issued copy must have landed before the CTA exits
+      for (int s = 0; s < TC_STAGES; ++s)
+        if (last_round[s] >= 0)
+          ptx::mbar_wait(ptx::smem_u32(&S.full[s]), (uint32_t)last_round[s] & 1u, kWaitNs);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = ptx::make_idesc(1, 1, TC_BM, TC_BN);
+      uint32_t f = 0;
+      int m = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < p.ntiles && ok && !S.abort; t += gridDim.x, ++m) {
+        const int acc = m & 1;
+        const uint32_t ar = (uint32_t)(m >> 1);
+        if (!ptx::mbar_wait(ptx::smem_u32(&S.tempty[acc]), (ar & 1u) ^ 1u, kWaitNs)) {
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(acc * TC_BN);
+        for (int kb = 0; kb < nkb; ++kb, ++f) {
+          const int s = f % TC_STAGES;
+          const uint32_t round = f / TC_STAGES;
+          if (!ptx::mbar_wait(ptx::smem_u32(&S.full[s]), round & 1u, kWaitNs)) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t base = ptx::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
+          const int steps = min(4, p.nk16 - kb * 4);
+          for (int kk = 0; kk < steps; ++kk) {
+            const uint64_t ahi = ptx::sw128_desc(base + kk * 32);
+            const uint64_t alo = ptx::sw128_desc(base + TC_A_BYTES + kk * 32);
+            const uint64_t bhi = ptx::sw128_desc(base + 2 * TC_A_BYTES + kk * 32);
+            const uint64_t blo = ptx::sw128_desc(base + 2 * TC_A_BYTES + TC_B_BYTES + kk * 32);
+            ptx::mma_bf16(d, ahi, bhi, idesc, (kb | kk) != 0);
+            ptx::mma_bf16(d, ahi, blo, idesc, 1);
+            ptx::mma_bf16(d, alo, bhi, idesc, 1);
+          }
+          ptx::mma_commit(ptx::smem_u32(&S.empty[s]));
+        }
+        if (!ok) break;
+        ptx::mma_commit(ptx::smem_u32(&S.tfull[acc]));
+      }
+      if (!ok) {
+        atomicOr(a.err, ERR_TIMEOUT);
+        S.abort = 1;
+      }
+      // no MMA may still be running when TMEM is freed
+      ptx::mma_commit(ptx::smem_u32(&S.done));
+      ptx::mbar_wait(ptx::smem_u32(&S.done), 0, kWaitNs);
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3;        // TMEM lane quadrant
+    const int h = (warp - 2) >> 2; // which 128-column half of the tile
+    const int il = q * 32 + lane;  // row within the tile
+    const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
+    const float tau = a.th.tau, delta = a.th.delta, lim = 1.0f - a.th.delta;
+    const bool zero_edge = edge_exact(0.0f, a.th);
+    uint32_t hphase = 0;
+    int m = 0;
+    for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++m) {
+      if (S.abort) break;
+      const int2 tile = p.tiles[t];
+      const int I = tile.x, J = 2 * tile.y + h;
+      const int acc = m & 1;
+      const uint32_t ar = (uint32_t)(m >> 1);
+      if (!half_sync(S, h, hphase)) {  // previous tile's shared-memory readers are done
+        atomicOr(a.err, ERR_TIMEOUT);
+        S.abort = 1;
+        break;
+      }
+      if (!ptx::mbar_wait(ptx::smem_u32(&S.tfull[acc]), ar & 1u, kWaitNs)) {
+        atomicOr(a.err, ERR_TIMEOUT);
+        S.abort = 1;
+        break;
+      }
+      ptx::tc_fence_after();
+      const bool active = (PASS == 2) ? (J < a.nb) : ((J >= I) && (J < a.nb));
+      if (active) {
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TC_BN + h * 128);
+        const int gi = I * 128 + il;
+        const bool diag = (I == J);
+        const bool slow = p.blockbad[I] | p.blockbad[J];
+        const bool rowbad = slow && a.bad[gi];
+        uint32_t rowbits[4], spbits[4];
+        int rowcount = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          uint32_t v[32];
+          ptx::tmem_ld32(taddr + c * 32, v);
+          if (PASS == 2) {
+            if (h == p.dump_half)
+              for (int k = 0; k < 32; ++k) p.dump[il * 128 + c * 32 + k] = __uint_as_float(v[k]);
+            rowbits[c] = spbits[c] = 0;
+            continue;
+          }
+          const int jb = J * 128 + c * 32;
+          uint32_t valid = (jb + 32 <= a.n) ? 0xffffffffu
+                                            : (jb >= a.n ? 0u : ((1u << (a.n - jb)) - 1u));
+          if (diag) {
+            const int lo = il - c * 32 + 1;  // first column index k with jl > il
+            valid &= (lo <= 0) ? 0xffffffffu : (lo >= 32 ? 0u : (0xffffffffu << lo));
+          }
+          uint32_t eb = 0, sb = 0;
+#pragma unroll
+          for (int k = 0; k < 32; ++k) {
+            const float r = __uint_as_float(v[k]);
+            const float x = absm ? fabsf(r) : r;
+            const float dd = x - tau;
+            eb |= (dd > delta) ? (1u << k) : 0u;
+            sb |= ((fabsf(dd) <= delta) | (fabsf(r) >= lim)) ? (1u << k) : 0u;
+          }
+          if (slow) {
+            uint32_t badm = 0;
+            for (int k = 0; k < 32; ++k)
+              if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm |= 1u << k;
+            eb = (eb & ~badm) | (zero_edge ? badm : 0u);
+            sb &= ~badm;
+          }
+          eb &= ~sb;
+          eb &= valid;
+          sb &= valid;
+          uint32_t s2 = sb;
+          while (s2) {
+            const int k = __ffs(s2) - 1;
+            s2 &= s2 - 1;
+            resolve_special<PASS>(a, gi, jb + k, 1u << k, eb);
+          }
+          rowbits[c] = eb;
+          spbits[c] = sb;
+          rowcount += __popc(eb);
+          S.colmask[h][c * 32 + lane][q] = transpose32(eb, lane);
+        }
+        if (PASS == 2) {
+          // nothing else
+        } else if (!half_sync(S, h, hphase)) {
+          atomicOr(a.err, ERR_TIMEOUT);
+          S.abort = 1;
+        } else if (PASS == 0) {
+          const uint32_t* cm = S.colmask[h][il];
+          const int cc = __popc(cm[0]) + __popc(cm[1]) + __popc(cm[2]) + __popc(cm[3]);
+          if (diag) {
+            a.seg[(size_t)I * a.n_pad + gi] = rowcount + cc;
+          } else {
+            a.seg[(size_t)J * a.n_pad + gi] = rowcount;
+            a.seg[(size_t)I * a.n_pad + J * 128 + il] = cc;
+          }
+        } else {
+          const uint32_t* cm = S.colmask[h][il];
+          const int cdiag = diag ? (__popc(cm[0]) + __popc(cm[1]) + __popc(cm[2]) + __popc(cm[3])) : 0;
+          int rowpos = (gi < a.n) ? a.row_ptr[gi] + a.seg[(size_t)J * a.n_pad + gi] + cdiag : 0;
+          const int gcol = J * 128 + il;
+          S.colbase[h][il] = (gcol < a.n) ? a.row_ptr[gcol] + a.seg[(size_t)I * a.n_pad + gcol] : 0;
+          if (!half_sync(S, h, hphase)) {
+            atomicOr(a.err, ERR_TIMEOUT);
+            S.abort = 1;
+          } else {
+            const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (!__any_sync(0xffffffffu, rowbits[c] != 0u)) continue;
+              uint32_t v[32];
+              ptx::tmem_ld32(taddr + c * 32, v);
+              uint32_t eb = rowbits[c];
+              while (eb) {
+                const int k = __ffs(eb) - 1;
+                eb &= eb - 1;
+                const int jl = c * 32 + k;
+                const int gj = J * 128 + jl;
+                float r = 0.f;
+#pragma unroll
+                for (int kk = 0; kk < 32; ++kk)
+                  if (kk == k) r = __uint_as_float(v[kk]);
+                if ((spbits[c] >> k) & 1u) {
+                  bool e;
+                  hash_lookup(a, pair_key(gi, gj), r, e);
+                } else if (slow && (rowbad || a.bad[gj])) {
+                  r = 0.f;
+                }
+                const uint32_t* cj = S.colmask[h][jl];
+                int rk = 0;
+                for (int w = 0; w < q; ++w) rk += __popc(cj[w]);
+                rk += __popc(cj[q] & below);
+                const int pc = S.colbase[h][jl] + rk;
+                put_edge(a, rowpos, gj, r);
+                put_edge(a, pc, gi, r);
+                ++rowpos;
+              }
+            }
+          }
+        }
+      } else if (PASS != 2) {
+        // keep the per-half barrier phases in step with the active halves
+        if (!half_sync(S, h, hphase)) {
+          atomicOr(a.err, ERR_TIMEOUT);
+          S.abort = 1;
+        } else if (PASS == 1 && !half_sync(S, h, hphase)) {
+          atomicOr(a.err, ERR_TIMEOUT);
+          S.abort = 1;
+        }
+      }
+      ptx::tc_fence_before();
+      ptx::mbar_arrive(ptx::smem_u32(&S.tempty[acc]));
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, TC_TMEM_COLS);
+  }
+}
+
+__global__ void block_bad_kernel(const uint8_t* bad, int nb, uint8_t* blockbad) {
+  const int b = blockIdx.x;
+  const int any = __syncthreads_or(bad[b * 128 + threadIdx.x] != 0);
+  if (threadIdx.x == 0 && b < nb) blockbad[b] = any ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- host side
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2-D BF16 map over [rows][ld] with a 64 x 128 box, 128-byte swizzle.
+bool make_map(CUtensorMap* m, const void* base, int ld, int rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {TC_BK, TC_BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Tile list (I, Jp) of the upper triangle in 128 x 256 tiles, row-major.
+void tc_tile_list(int nb, std::vector<int2>& out) {
+  out.clear();
+  const int njp = (nb + 1) / 2;
+  for (int I = 0; I < nb; ++I)
+    for (int jp = I / 2; jp < njp; ++jp) out.push_back(make_int2(I, jp));
+}
+
+size_t tc_smem_bytes() { return TC_SMEM_BYTES; }
+
+cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st) {
+  block_bad_kernel<<<nb, 128, 0, st>>>(bad, nb, blockbad);
+  return cudaGetLastError();
+}
+
+// pass 0 count, 1 fill, 2 dump (tiles must then hold the one tile to dump)
+cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
+                           const uint8_t* blockbad, float* dump, int dump_half, int grid,
+                           cudaStream_t st) {
+  if (!a.zhi || !a.zlo || a.ldb % TC_BK != 0) return cudaErrorInvalidValue;
+  CUtensorMap mh, ml;
+  if (!make_map(&mh, a.zhi, a.ldb, a.n_pad) || !make_map(&ml, a.zlo, a.ldb, a.n_pad))
+    return cudaErrorInvalidValue;
+  TcArgs p;
+  p.a = a;
+  p.tiles = tiles;
+  p.ntiles = ntiles;
+  p.nk16 = (a.T + 15) / 16;
+  p.blockbad = blockbad;
+  p.dump = dump;
+  p.dump_half = dump_half;
+  const int g = grid < ntiles ? grid : ntiles;
+  if (g <= 0) return cudaSuccess;
+  cudaError_t e;
+  switch (pass) {
+    case 0:
+      e = cudaFuncSetAttribute(corr_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TC_SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      corr_tc_kernel<0><<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
+      break;
+    case 1:
+      e = cudaFuncSetAttribute(corr_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TC_SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      corr_tc_kernel<1><<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
+      break;
+    default:
+      e = cudaFuncSetAttribute(corr_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TC_SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      corr_tc_kernel<2><<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace bna

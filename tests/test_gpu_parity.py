@@ -14,7 +14,7 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-PRECISIONS = ["fp32"]
+PRECISIONS = ["fp32", "bf16x3"]
 
 
 def dev(x):
@@ -30,6 +30,30 @@ def assert_csr_equal(res, R, C, V, delta, exact_vals=None):
         assert g.val is not None
         err = np.max(np.abs(g.val - V)) if len(V) else 0.0
         assert err <= delta, f"val error {err} > delta {delta}"
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_tile_values_within_error_bound(builder, precision):
+    """max |r_form - r| over whole tiles, r = exact dot of the float z-scores;
+    must sit well inside the recompute band delta."""
+    N, T = 600, 240
+    b = bna.synth_bold(N, T, 20, 77)
+    z = oracle.zscore(b).astype(np.float64)
+    res = builder.corr_csr(dev(b), mode="r_gt", value=0.5, precision=precision)
+    delta = res.stats["delta"]
+    worst = 0.0
+    for I, J in [(0, 0), (0, 1), (1, 2), (2, 4), (3, 3), (4, 1)]:
+        t = builder.tile_values(dev(b), I, J, precision=precision).cpu().numpy().astype(np.float64)
+        zi = np.zeros((128, T))
+        zj = np.zeros((128, T))
+        ri = z[I * 128:(I + 1) * 128]
+        rj = z[J * 128:(J + 1) * 128]
+        zi[:len(ri)] = ri
+        zj[:len(rj)] = rj
+        ref = zi @ zj.T
+        worst = max(worst, float(np.max(np.abs(t - ref))))
+    print(f"{precision}: max |r - r_fp64| = {worst:.3e} (delta {delta:.3e})")
+    assert worst <= 0.5 * delta
 
 
 def test_zscore_bit_exact(builder):
@@ -103,14 +127,15 @@ def test_repeat_calls_are_deterministic(builder):
     assert np.array_equal(r1.col_idx, r2.col_idx) and np.array_equal(r1.val, r2.val)
 
 
-def test_full_size_workload_slice(builder):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_full_size_workload_slice(builder, precision):
     """N=45,000 x T=240 (the benchmark workload): rows of three slices equal the
     oracle; symmetry, ascending columns and no diagonal over the whole CSR."""
     import json
     w = json.load(open(os.path.join(GOLD, "workload_tau.json")))
     b = bna.synth_bold(w["N"], w["T"], w["K"], w["seed"])
     tau = w["tau_f32"]
-    res = builder.corr_csr(dev(b), mode="r_ge", value=tau, precision="fp32")
+    res = builder.corr_csr(dev(b), mode="r_ge", value=tau, precision=precision)
     g = res.numpy()
     n = w["N"]
     # about 1 % density (tau is the FP64 quantile)
