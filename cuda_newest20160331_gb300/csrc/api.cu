@@ -40,6 +40,8 @@ cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cuda
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st);
+cudaError_t launch_csr_fill(const CorrArgs& a, int sms, cudaStream_t stream);
+cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream);
 }  // namespace bna
 
 using namespace bna;
@@ -49,7 +51,7 @@ namespace {
 enum Slot {
   S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
-  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_COUNT
+  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -59,6 +61,7 @@ struct DevStatus {
   uint32_t pad;
   unsigned long long stats[4];
   long long total;
+  unsigned long long epool;  // edge-list entries handed out by the count pass
 };
 
 struct EcGraph {
@@ -83,6 +86,7 @@ struct bna_ctx {
   cudaEvent_t ev[8] = {};
   std::string last_error;
   long long cand_cap = 1 << 20;
+  long long elist_cap = 1LL << 23;  // edge-list pool entries (grows on demand)
   EcGraph ecg;
   int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
   int ntiles = 0;
@@ -386,21 +390,30 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   a.n_drop = 0;
   DevStatus* hs = reinterpret_cast<DevStatus*>(ctx->pinned);
 
+  const long long nst = (long long)a.nb * (a.nb + 1) / 2;
+  ENSURE(S_ETAB, (size_t)nst * 4 * sizeof(longlong2), a.etab);
+  a.epool = &ds->epool;
   int passes = 0;
   for (int attempt = 0;; ++attempt) {
     a.cand_cap = ctx->cand_cap;
+    // the pool hands out one chunk per warp at a time: room for two per warp
+    const long long min_pool = (long long)ctx->sms * 8 * 2 * kElistChunk;
+    if (ctx->elist_cap < min_pool) ctx->elist_cap = min_pool;
+    a.ecap = ctx->elist_cap;
     const unsigned long long hcap = next_pow2((unsigned long long)a.cand_cap * 2);
     a.hmask = hcap - 1;
     ENSURE(S_CAND, (size_t)a.cand_cap * sizeof(uint2), a.cand);
     ENSURE(S_HKEYS, hcap * 8, a.hkeys);
     ENSURE(S_HVAL, hcap * 4, a.hval);
     ENSURE(S_HEDGE, hcap, a.hedge);
+    ENSURE(S_ELIST, (size_t)a.ecap * sizeof(uint2), a.elist);
     CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
     CK(cudaMemsetAsync(a.hkeys, 0xff, hcap * 8, st));
     s = corr_pass(ctx, a, prec, 0, st);
     if (s) return s;
     ++passes;
     CK(cudaEventRecord(ctx->ev[2], st));
+    CK(launch_collect_candidates(a, ctx->sms, st));
     CK(launch_recompute(a, ctx->sms * 4, st));
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
@@ -408,15 +421,22 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     CK(cudaEventRecord(ctx->ev[4], st));
     CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    bool again = false;
     if ((hs->err & ERR_BAND_OVERFLOW) && attempt < 3) {
       ctx->cand_cap = (long long)(hs->cand_count * 3 / 2) + 1024;
-      continue;
+      again = true;
     }
-    break;
+    if ((hs->err & ERR_ELIST) && attempt < 3) {
+      ctx->elist_cap = (long long)(hs->epool + hs->epool / 4) + kElistChunk;
+      again = true;
+    }
+    if (!again) break;
   }
   if (hs->err & ERR_TIMEOUT) return fail(ctx, BNA_TIMEOUT, "count pass: a bounded wait expired");
   if (hs->err & ERR_BAND_OVERFLOW)
     return fail(ctx, BNA_INTERNAL, "candidate list overflow (%llu candidates)", hs->cand_count);
+  if (hs->err & ERR_ELIST)
+    return fail(ctx, BNA_INTERNAL, "edge-list pool overflow (%llu entries)", hs->epool);
   if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
   if (hs->err & ERR_NNZ_INT32 || hs->total > 0x7fffffffLL)
     return fail(ctx, BNA_NNZ_OVERFLOW_INT32, "nnz %lld exceeds int32", hs->total);
@@ -431,13 +451,10 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   a.col_idx = col;
   a.val = val;
   a.nnz = nnz;
-  s = corr_pass(ctx, a, prec, 1, st);
-  if (s) return s;
-  ++passes;
+  CK(launch_csr_fill(a, ctx->sms, st));
   CK(cudaEventRecord(ctx->ev[5], st));
   CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (hs->err & ERR_TIMEOUT) return fail(ctx, BNA_TIMEOUT, "fill pass: a bounded wait expired");
   if (hs->err & ERR_HASH_MISS) return fail(ctx, BNA_INTERNAL, "fill pass missed a candidate");
   if (hs->err & ERR_RANGE) return fail(ctx, BNA_INTERNAL, "fill pass position out of range");
   out_dev->n = N;
@@ -454,8 +471,8 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     stats->band_edges = (int64_t)band_edges;
     stats->band_1e6 = (int64_t)band_1e6;
     stats->passes = passes;
-    // z-score, [block flags], count, recompute, 4 scan kernels, fill
-    stats->kernel_launches = 1 + (prec == BNA_PREC_BF16X3 ? 1 : 0) + passes + 1 + 4;
+    // z-score, [block flags], per attempt: count, collect, recompute, 4 scan kernels; fill
+    stats->kernel_launches = 1 + (prec == BNA_PREC_BF16X3 ? 1 : 0) + passes * 7 + 1;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);

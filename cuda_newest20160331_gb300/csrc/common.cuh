@@ -21,7 +21,12 @@ enum : uint32_t {
   ERR_TIES = 16u,           // density: tie bookkeeping inconsistent
   ERR_TIMEOUT = 32u,        // a bounded wait in a tensor-core kernel expired
   ERR_RANGE = 64u,          // a fill-pass position fell outside the CSR (write skipped)
+  ERR_ELIST = 128u,         // edge-list pool too small (entries not written; pass is rerun)
 };
+
+// Edge-list pool: the count pass allocates it in chunks of kElistChunk
+// entries per warp (one atomic per chunk) and never writes past ecap.
+constexpr long long kElistChunk = 16384;
 
 // Outcome of classifying one approximate correlation.
 enum : int { CLS_NO = 0, CLS_EDGE = 1, CLS_BAND = 2 };
@@ -84,6 +89,13 @@ struct CorrArgs {
   float* hval;
   uint8_t* hedge;
   unsigned long long hmask;
+  // per-tile edge lists written by the count pass, placed by the fill pass:
+  // entry = (il | jl << 7 | candidate << 14, value bits); etab[4*st + q] =
+  // (first entry, count) of part q of 128 x 128 sub-tile st (upper-triangle index)
+  uint2* elist;
+  unsigned long long* epool;
+  long long ecap;
+  longlong2* etab;
   // density ties that must not become edges (sorted keys), see FormFullGraph_s
   const unsigned long long* drop_keys;
   int n_drop;
@@ -143,6 +155,15 @@ __device__ __forceinline__ void push_candidate(const CorrArgs& a, int i, int j) 
   } else {
     atomicOr(a.err, ERR_BAND_OVERFLOW);
   }
+}
+
+// Upper-triangular 128-block pair (I, J), I <= J -> its row-major index.
+__host__ __device__ __forceinline__ long long subtile_index(int I, int J, int nb) {
+  return (long long)I * nb - (long long)I * (I - 1) / 2 + (J - I);
+}
+
+__device__ __forceinline__ uint32_t elist_key(int il, int jl, uint32_t cand) {
+  return (uint32_t)il | ((uint32_t)jl << 7) | (cand << 14);
 }
 
 // Upper-triangular tile index -> (I, J), I <= J, row-major over I.

@@ -72,18 +72,90 @@ __global__ void recompute_kernel(CorrArgs a) {
   }
 }
 
+// Gather the candidates flagged in the sub-tiles' edge lists into the
+// candidate list (warp per sub-tile, one atomic per warp and round).
+__global__ void collect_candidates_kernel(CorrArgs a, long long nst) {
+  const int wpb = blockDim.x >> 5;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t below = (1u << lane) - 1u;
+  for (long long st = (long long)blockIdx.x * wpb + w; st < nst; st += (long long)gridDim.x * wpb) {
+    long long s0 = 0, c0 = 0;
+    if (lane < 4) {
+      const longlong2 e = a.etab[st * 4 + lane];
+      s0 = e.x;
+      c0 = e.y;
+    }
+    long long start[4], cnt[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      start[q] = __shfl_sync(0xffffffffu, s0, q);
+      cnt[q] = __shfl_sync(0xffffffffu, c0, q);
+    }
+    bool inside = true;  // ranges written while the pool overflowed are not read
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      inside &= cnt[q] >= 0 && start[q] >= 0 && start[q] + cnt[q] <= a.ecap;
+    if (!inside) {
+      if (lane == 0) atomicOr(a.err, ERR_ELIST);
+      continue;
+    }
+    const long long E = cnt[0] + cnt[1] + cnt[2] + cnt[3];
+    if (E == 0) continue;
+    int I, J;
+    tile_coords(st, a.nb, I, J);
+    const long long p1 = cnt[0], p2 = p1 + cnt[1], p3 = p2 + cnt[2];
+    for (long long e0 = 0; e0 < E; e0 += 32) {
+      const long long e = e0 + lane;
+      bool flag = false;
+      uint32_t key = 0;
+      if (e < E) {
+        const int q = e < p1 ? 0 : e < p2 ? 1 : e < p3 ? 2 : 3;
+        const long long off = e - (q == 0 ? 0 : q == 1 ? p1 : q == 2 ? p2 : p3);
+        const long long s = q == 0 ? start[0] : q == 1 ? start[1] : q == 2 ? start[2] : start[3];
+        key = a.elist[s + off].x;
+        flag = ((key >> 14) & 1u) != 0u;
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+      if (!bal) continue;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(a.cand_count, (unsigned long long)__popc(bal));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (flag) {
+        const unsigned long long slot = base + __popc(bal & below);
+        if ((long long)slot < a.cand_cap)
+          a.cand[slot] = make_uint2((unsigned)(I * 128 + (key & 127)),
+                                    (unsigned)(J * 128 + ((key >> 7) & 127)));
+        else
+          atomicOr(a.err, ERR_BAND_OVERFLOW);
+      }
+    }
+  }
+}
+
 // Exact values of arbitrary pairs (diagnostics: max |r - r_ref| of a form).
 __global__ void exact_pairs_kernel(CorrArgs a, const uint2* pairs, int n, float* out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) out[c] = exact_r(a, (int)pairs[c].x, (int)pairs[c].y);
 }
 
-// seg[b][i] -> exclusive prefix over b; rowlen[i] = row total.
+// seg[b][i] -> exclusive prefix over b; rowlen[i] = row total.  Loads are
+// issued 16 at a time so each thread keeps 16 requests in flight.
 __global__ void seg_scan_rows_kernel(int32_t* seg, int nb, int n_pad, int n, long long* rowlen) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_pad) return;
   long long acc = 0;
-  for (int b = 0; b < nb; ++b) {
+  int b = 0;
+  for (; b + 16 <= nb; b += 16) {
+    int c[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) c[u] = seg[(size_t)(b + u) * n_pad + i];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      seg[(size_t)(b + u) * n_pad + i] = (int)acc;
+      acc += c[u];
+    }
+  }
+  for (; b < nb; ++b) {
     int32_t* p = seg + (size_t)b * n_pad + i;
     const int c = *p;
     *p = (int)acc;
@@ -190,6 +262,15 @@ cudaError_t launch_recompute(const CorrArgs& a, int grid, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream) {
+  const long long nst = (long long)a.nb * (a.nb + 1) / 2;
+  const long long want = (nst + 7) / 8;
+  const int grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
+  if (grid <= 0) return cudaSuccess;
+  collect_candidates_kernel<<<grid, 256, 0, stream>>>(a, nst);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_exact_pairs(const CorrArgs& a, const uint2* pairs, int n, float* out,
                                cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
@@ -203,7 +284,7 @@ cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* r
                             uint32_t* err, cudaStream_t stream) {
   const int nblk = (n + 4095) / 4096;
   if (nblk > 4096) return cudaErrorInvalidValue;
-  seg_scan_rows_kernel<<<(n_pad + 255) / 256, 256, 0, stream>>>(seg, nb, n_pad, n, rowlen);
+  seg_scan_rows_kernel<<<(n_pad + 127) / 128, 128, 0, stream>>>(seg, nb, n_pad, n, rowlen);
   scan_block_kernel<<<nblk, 1024, 0, stream>>>(rowlen, n, pre, bsum);
   scan_sums_kernel<<<1, 1024, 0, stream>>>(bsum, nblk, total);
   scan_finish_kernel<<<(n + 1 + 255) / 256, 256, 0, stream>>>(pre, bsum, n, total, row_ptr, err);

@@ -6,12 +6,12 @@
 // I <= J, of Z Z^T in FP32 and thresholds it in registers; the N x N matrix
 // never exists.
 //
-// The tile epilogue is shared by two launches over the same tiles:
-//   count pass: per tile, count edges per row (seg[J][i]) and per column
-//               (seg[I][j]); near-threshold pairs go to the candidate list;
-//   fill pass : recompute the identical tile, place every edge at
-//               row_ptr[row] + seg[block][row] + its rank in the tile's
-//               row (or column) bitmask, writing both (i, j) and (j, i).
+// The tile epilogue (count pass) counts edges per row (seg[J][i]) and per
+// column (seg[I][j]), sends near-threshold pairs to the candidate list, and
+// appends the tile's edges with their values to its edge list (one pool
+// allocation per tile, slots by a block prefix scan).  The fill pass
+// (csr_fill.cu) places every listed edge at row_ptr[row] + seg[block][row] +
+// its rank in the tile's row (or column) bitmask, writing (i, j) and (j, i).
 // A pair is evaluated once (diagonal tiles keep il < jl), so the CSR is
 // symmetric by construction.
 #include "common.cuh"
@@ -22,17 +22,7 @@ constexpr int SB = 128;  // tile edge
 constexpr int SK = 16;   // K (time) chunk per stage
 constexpr int SPAD = 4;
 
-__device__ __forceinline__ int popc_before(const uint32_t* m, int pos) {
-  int c = 0;
-  const int w = pos >> 5;
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (k < w) c += __popc(m[k]);
-  const uint32_t part = m[w] & ((1u << (pos & 31)) - 1u);
-  return c + __popc(part);
-}
-
-// PASS 0 = count, 1 = fill, 2 = dump approximate values of one tile.
+// PASS 0 = count (+ edge list), 2 = dump approximate values of one tile.
 template <int PASS>
 __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, int dumpI,
                                                            int dumpJ, float* dump) {
@@ -40,8 +30,8 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
   __shared__ __align__(16) float Bs[2][SK][SB + SPAD];
   __shared__ uint32_t rowmask[SB][4];
   __shared__ uint32_t colmask[SB][4];
-  __shared__ int rowbase[SB];
-  __shared__ int colbase[SB];
+  __shared__ int wsum[8];
+  __shared__ long long tbase;
 
   int I, J;
   if (PASS == 2) {
@@ -134,8 +124,8 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
     badr |= (uint32_t)a.bad[i0 + il] << i;
     badc |= (uint32_t)a.bad[j0 + jl] << i;
   }
-  const float zero_is_edge = edge_exact(0.0f, a.th) ? 1.f : 0.f;
-  unsigned long long emask = 0ull;
+  const bool zero_is_edge = edge_exact(0.0f, a.th);
+  unsigned long long emask = 0ull, cmask = 0ull;  // edges, near-threshold candidates
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int il = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
@@ -144,77 +134,80 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
       const int jl = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
       const int gi = i0 + il, gj = j0 + jl;
       if (gj >= a.n || (diag && jl <= il)) continue;
-      float r = acc[i][j];
       int c;
       if (((badr >> i) | (badc >> j)) & 1u) {
-        r = 0.f;
-        c = zero_is_edge != 0.f ? CLS_EDGE : CLS_NO;
+        acc[i][j] = 0.f;
+        c = zero_is_edge ? CLS_EDGE : CLS_NO;
       } else {
-        c = classify(r, a.th);
+        c = classify(acc[i][j], a.th);
       }
       if (c == CLS_BAND) {
-        if (PASS == 0) {
-          push_candidate(a, gi, gj);
-          continue;
-        }
-        bool e;
-        hash_lookup(a, pair_key(gi, gj), r, e);
-        c = e ? CLS_EDGE : CLS_NO;
-      }
-      if (c == CLS_EDGE) {
+        cmask |= 1ull << (i * 8 + j);  // flagged; collected after the pass
+      } else if (c == CLS_EDGE) {
         emask |= 1ull << (i * 8 + j);
-        acc[i][j] = r;
         atomicOr(&rowmask[il][jl >> 5], 1u << (jl & 31));
         atomicOr(&colmask[jl][il >> 5], 1u << (il & 31));
       }
     }
   }
+  // edge list of the tile: block prefix scan of the per-thread entry counts,
+  // one pool allocation per tile
+  const unsigned long long ent = emask | cmask;
+  const int ne = __popcll(ent);
+  const int lane = tid & 31, warp = tid >> 5;
+  int incl = ne;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
   __syncthreads();
-
-  if (PASS == 0) {
-    if (tid < SB) {
-      const int rc = __popc(rowmask[tid][0]) + __popc(rowmask[tid][1]) +
-                     __popc(rowmask[tid][2]) + __popc(rowmask[tid][3]);
-      const int cc = __popc(colmask[tid][0]) + __popc(colmask[tid][1]) +
-                     __popc(colmask[tid][2]) + __popc(colmask[tid][3]);
-      if (diag) {
-        a.seg[(size_t)I * a.n_pad + i0 + tid] = rc + cc;
-      } else {
-        a.seg[(size_t)J * a.n_pad + i0 + tid] = rc;
-        a.seg[(size_t)I * a.n_pad + j0 + tid] = cc;
+  if (tid == 0) {
+    int run = 0;
+    for (int w = 0; w < 8; ++w) {
+      const int c = wsum[w];
+      wsum[w] = run;
+      run += c;
+    }
+    const unsigned long long base = run ? atomicAdd(a.epool, (unsigned long long)run) : 0ull;
+    tbase = (long long)base;
+    const bool fits = !run || (long long)(base + run) <= a.ecap;
+    if (!fits) atomicOr(a.err, ERR_ELIST);
+    const long long st = subtile_index(I, J, a.nb);
+    a.etab[st * 4 + 0] = fits ? make_longlong2((long long)base, run) : make_longlong2(0, 0);
+    a.etab[st * 4 + 1] = make_longlong2(0, 0);
+    a.etab[st * 4 + 2] = make_longlong2(0, 0);
+    a.etab[st * 4 + 3] = make_longlong2(0, 0);
+  }
+  __syncthreads();
+  if (ent && tbase + wsum[warp] + incl <= a.ecap) {
+    uint2* dst = a.elist + tbase + wsum[warp] + (incl - ne);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int il = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int jl = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
+        const int b = i * 8 + j;
+        if ((ent >> b) & 1ull) {
+          const uint32_t cf = (uint32_t)((cmask >> b) & 1ull);
+          *dst++ = make_uint2(elist_key(il, jl, cf), cf ? 0u : __float_as_uint(acc[i][j]));
+        }
       }
     }
-    return;
   }
-
-  // fill pass
   if (tid < SB) {
-    const int gi = i0 + tid, gj = j0 + tid;
-    int cdiag = 0;
-    if (diag)
-      cdiag = __popc(colmask[tid][0]) + __popc(colmask[tid][1]) + __popc(colmask[tid][2]) +
-              __popc(colmask[tid][3]);
-    rowbase[tid] = (gi < a.n) ? a.row_ptr[gi] + a.seg[(size_t)J * a.n_pad + gi] + cdiag : 0;
-    colbase[tid] = (gj < a.n) ? a.row_ptr[gj] + a.seg[(size_t)I * a.n_pad + gj] : 0;
-  }
-  __syncthreads();
-  while (emask) {
-    const int bit = __ffsll((long long)emask) - 1;
-    emask &= emask - 1;
-    const int i = bit >> 3, j = bit & 7;
-    const int il = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
-    const int jl = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
-    float v = 0.f;
-    // runtime index into the register tile: resolved through a small switch
-#pragma unroll
-    for (int ii = 0; ii < 8; ++ii)
-#pragma unroll
-      for (int jj = 0; jj < 8; ++jj)
-        if (ii == i && jj == j) v = acc[ii][jj];
-    const int pr = rowbase[il] + popc_before(rowmask[il], jl);
-    const int pc = colbase[jl] + popc_before(colmask[jl], il);
-    put_edge(a, pr, j0 + jl, v);
-    put_edge(a, pc, i0 + il, v);
+    const int rc = __popc(rowmask[tid][0]) + __popc(rowmask[tid][1]) +
+                   __popc(rowmask[tid][2]) + __popc(rowmask[tid][3]);
+    const int cc = __popc(colmask[tid][0]) + __popc(colmask[tid][1]) +
+                   __popc(colmask[tid][2]) + __popc(colmask[tid][3]);
+    if (diag) {
+      a.seg[(size_t)I * a.n_pad + i0 + tid] = rc + cc;
+    } else {
+      a.seg[(size_t)J * a.n_pad + i0 + tid] = rc;
+      a.seg[(size_t)I * a.n_pad + j0 + tid] = cc;
+    }
   }
 }
 
@@ -222,10 +215,8 @@ cudaError_t launch_corr_simt(const CorrArgs& a, int pass, cudaStream_t stream) {
   const int nt = a.nb;
   const long long tiles = (long long)nt * (nt + 1) / 2;
   if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-  if (pass == 0)
-    corr_simt_kernel<0><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
-  else
-    corr_simt_kernel<1><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
+  if (pass != 0) return cudaErrorInvalidValue;
+  corr_simt_kernel<0><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
   return cudaGetLastError();
 }
 

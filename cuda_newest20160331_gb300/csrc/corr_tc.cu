@@ -13,10 +13,15 @@
 //               two TMEM accumulators (512 columns) so the epilogue of tile t
 //               overlaps the MMAs of tile t+1;
 //   warps 2..9  epilogue: each 128 x 128 half-tile is read from TMEM by four
-//               warps (one per 32-lane quadrant, thread = row), thresholded in
-//               registers, and compacted with the same count / fill scheme as
-//               the plain form: row bitmasks in registers, column bitmasks by a
-//               32 x 32 bit transpose across the warp, ranks by popcount.
+//               warps (one per 32-lane quadrant, thread = row), 32 columns at
+//               a time (the next load in flight), and thresholded in registers:
+//               one compare per value marks the "interesting" entries (edge or
+//               near-threshold candidate); a warp prefix scan gives their slots
+//               in the sub-tile's compact edge list (warp-private bump
+//               allocator), candidates only flagged; row counts from register
+//               bitmasks, column counts from a 32 x 32 bit transpose across the
+//               warp.  The fill pass (csr_fill.cu) places the listed edges; the
+//               GEMM runs once.
 //
 // Every wait is bounded (4 s of wall time); on expiry the kernel raises
 // ERR_TIMEOUT, drains its own copies and MMAs, frees TMEM and returns.
@@ -47,7 +52,6 @@ struct TcSmem {
   uint32_t tmem_base;
   volatile uint32_t abort;
   uint32_t colmask[2][128][4];
-  int colbase[2][128];
 };
 
 constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_STAGES * TC_STAGE_BYTES + sizeof(TcSmem);
@@ -61,6 +65,20 @@ struct TcArgs {
   float* dump;              // dump pass: 128 x 128 values of half `dump_half`
   int dump_half;
 };
+
+// v[k] for a run-time k through a 5-level select tree (no local-memory copy).
+__device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[32], int k) {
+  uint32_t t[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) t[i] = (k & 16) ? v[i + 16] : v[i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) t[i] = (k & 8) ? t[i + 8] : t[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) t[i] = (k & 4) ? t[i + 4] : t[i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) t[i] = (k & 2) ? t[i + 2] : t[i];
+  return (k & 1) ? t[1] : t[0];
+}
 
 // 32 x 32 bit transpose across a warp: lane L holds row L on entry and
 // column L on exit (bit b of the result = bit L of lane b's input).
@@ -86,20 +104,7 @@ __device__ __forceinline__ bool half_sync(TcSmem& S, int h, uint32_t& phase) {
   return ok;
 }
 
-template <int PASS>
-__device__ __forceinline__ void resolve_special(const CorrArgs& a, int gi, int gj, uint32_t bit,
-                                                uint32_t& eb) {
-  if (PASS == 0) {
-    push_candidate(a, gi, gj);
-  } else {
-    float v;
-    bool e;
-    hash_lookup(a, pair_key(gi, gj), v, e);
-    if (e) eb |= bit;
-  }
-}
-
-template <int PASS>
+template <int PASS, bool ABS>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
                    const __grid_constant__ CUtensorMap tm_lo, const TcArgs p) {
@@ -225,20 +230,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp & 3;        // TMEM lane quadrant
-    const int h = (warp - 2) >> 2; // which 128-column half of the tile
-    const int il = q * 32 + lane;  // row within the tile
-    const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
+    const int q = warp & 3;         // TMEM lane quadrant
+    const int h = (warp - 2) >> 2;  // which 128-column half of the tile
+    const int il = q * 32 + lane;   // row within the tile
     const float tau = a.th.tau, delta = a.th.delta, lim = 1.0f - a.th.delta;
+    const float lo_thr = tau - delta;
+    // Near +1 is always covered by x >= tau - delta when tau < 1 - delta; near
+    // -1 can be an edge only through post_block's 0 for tau <= 0 in the signed
+    // rules (|r| rules cover -1 like +1).
+    const bool simple = (tau < lim) && (ABS || lo_thr > 0.0f);
     const bool zero_edge = edge_exact(0.0f, a.th);
     uint32_t hphase = 0;
+    long long wcur = 0, wend = 0;  // this warp's current edge-list chunk [wcur, wend)
+    bool wok = true;
     int m = 0;
+    // tile coordinates and NaN-block flags run one tile ahead
+    int2 nxt = make_int2(0, 0);
+    uint8_t nbi = 0, nbj = 0;
+    if ((int)blockIdx.x < p.ntiles) {
+      nxt = p.tiles[blockIdx.x];
+      nbi = p.blockbad[nxt.x];
+      const int jj = 2 * nxt.y + h;
+      nbj = jj < a.nb ? p.blockbad[jj] : 0;
+    }
     for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++m) {
       if (S.abort) break;
-      const int2 tile = p.tiles[t];
+      const int2 tile = nxt;
+      const bool bad_i = nbi != 0, bad_j = nbj != 0;
+      if (t + (int)gridDim.x < p.ntiles) {
+        nxt = p.tiles[t + gridDim.x];
+        nbi = p.blockbad[nxt.x];
+        const int jj = 2 * nxt.y + h;
+        nbj = jj < a.nb ? p.blockbad[jj] : 0;
+      }
       const int I = tile.x, J = 2 * tile.y + h;
       const int acc = m & 1;
       const uint32_t ar = (uint32_t)(m >> 1);
+      const bool active = (PASS == 2) ? (J < a.nb) : ((J >= I) && (J < a.nb));
+      const int gi = I * 128 + il;
+      long long start = 0;
+      if (PASS == 0 && active) {
+        // room for this warp's worst case (32 rows x 128 columns) in one chunk
+        if (wend - wcur < 32 * 128) {
+          long long base = 0;
+          if (lane == 0) base = (long long)atomicAdd(a.epool, (unsigned long long)kElistChunk);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          wcur = base;
+          wend = base + kElistChunk;
+          wok = wend <= a.ecap;
+          if (!wok && lane == 0) atomicOr(a.err, ERR_ELIST);
+        }
+        start = wcur;
+      }
       if (!half_sync(S, h, hphase)) {  // previous tile's shared-memory readers are done
         atomicOr(a.err, ERR_TIMEOUT);
         S.abort = 1;
@@ -250,23 +293,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         break;
       }
       ptx::tc_fence_after();
-      const bool active = (PASS == 2) ? (J < a.nb) : ((J >= I) && (J < a.nb));
+      const uint32_t taddr =
+          tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TC_BN + h * 128);
+      const bool diag = (I == J);
+      const bool slow = active && (bad_i || bad_j);
+      const bool rowbad = slow && a.bad[gi];
+      int rowcount = 0;
       if (active) {
-        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TC_BN + h * 128);
-        const int gi = I * 128 + il;
-        const bool diag = (I == J);
-        const bool slow = p.blockbad[I] | p.blockbad[J];
-        const bool rowbad = slow && a.bad[gi];
-        uint32_t rowbits[4], spbits[4];
-        int rowcount = 0;
+        uint32_t vb[2][32];
+        ptx::tmem_ld32_async(taddr, vb[0]);
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          uint32_t v[32];
-          ptx::tmem_ld32(taddr + c * 32, v);
+          uint32_t(&v)[32] = vb[c & 1];
+          ptx::tmem_wait32(v);
+          if (c + 1 < 4) ptx::tmem_ld32_async(taddr + (c + 1) * 32, vb[(c + 1) & 1]);
           if (PASS == 2) {
             if (h == p.dump_half)
               for (int k = 0; k < 32; ++k) p.dump[il * 128 + c * 32 + k] = __uint_as_float(v[k]);
-            rowbits[c] = spbits[c] = 0;
             continue;
           }
           const int jb = J * 128 + c * 32;
@@ -276,106 +319,87 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int lo = il - c * 32 + 1;  // first column index k with jl > il
             valid &= (lo <= 0) ? 0xffffffffu : (lo >= 32 ? 0u : (0xffffffffu << lo));
           }
-          uint32_t eb = 0, sb = 0;
+          // "interesting" = an edge or a candidate: x >= tau - delta, or
+          // |r| >= 1 - delta; 8 partial masks so no long dependency chain forms
+          uint32_t pm[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+          if (simple) {
 #pragma unroll
-          for (int k = 0; k < 32; ++k) {
-            const float r = __uint_as_float(v[k]);
-            const float x = absm ? fabsf(r) : r;
-            const float dd = x - tau;
-            eb |= (dd > delta) ? (1u << k) : 0u;
-            sb |= ((fabsf(dd) <= delta) | (fabsf(r) >= lim)) ? (1u << k) : 0u;
-          }
-          if (slow) {
-            uint32_t badm = 0;
-            for (int k = 0; k < 32; ++k)
-              if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm |= 1u << k;
-            eb = (eb & ~badm) | (zero_edge ? badm : 0u);
-            sb &= ~badm;
-          }
-          eb &= ~sb;
-          eb &= valid;
-          sb &= valid;
-          uint32_t s2 = sb;
-          while (s2) {
-            const int k = __ffs(s2) - 1;
-            s2 &= s2 - 1;
-            resolve_special<PASS>(a, gi, jb + k, 1u << k, eb);
-          }
-          rowbits[c] = eb;
-          spbits[c] = sb;
-          rowcount += __popc(eb);
-          S.colmask[h][c * 32 + lane][q] = transpose32(eb, lane);
-        }
-        if (PASS == 2) {
-          // nothing else
-        } else if (!half_sync(S, h, hphase)) {
-          atomicOr(a.err, ERR_TIMEOUT);
-          S.abort = 1;
-        } else if (PASS == 0) {
-          const uint32_t* cm = S.colmask[h][il];
-          const int cc = __popc(cm[0]) + __popc(cm[1]) + __popc(cm[2]) + __popc(cm[3]);
-          if (diag) {
-            a.seg[(size_t)I * a.n_pad + gi] = rowcount + cc;
+            for (int k = 0; k < 32; ++k) {
+              const float r = __uint_as_float(v[k]);
+              pm[k & 7] |= ((ABS ? fabsf(r) : r) >= lo_thr) ? (1u << k) : 0u;
+            }
           } else {
-            a.seg[(size_t)J * a.n_pad + gi] = rowcount;
-            a.seg[(size_t)I * a.n_pad + J * 128 + il] = cc;
-          }
-        } else {
-          const uint32_t* cm = S.colmask[h][il];
-          const int cdiag = diag ? (__popc(cm[0]) + __popc(cm[1]) + __popc(cm[2]) + __popc(cm[3])) : 0;
-          int rowpos = (gi < a.n) ? a.row_ptr[gi] + a.seg[(size_t)J * a.n_pad + gi] + cdiag : 0;
-          const int gcol = J * 128 + il;
-          S.colbase[h][il] = (gcol < a.n) ? a.row_ptr[gcol] + a.seg[(size_t)I * a.n_pad + gcol] : 0;
-          if (!half_sync(S, h, hphase)) {
-            atomicOr(a.err, ERR_TIMEOUT);
-            S.abort = 1;
-          } else {
-            const uint32_t below = (1u << lane) - 1u;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              if (!__any_sync(0xffffffffu, rowbits[c] != 0u)) continue;
-              uint32_t v[32];
-              ptx::tmem_ld32(taddr + c * 32, v);
-              uint32_t eb = rowbits[c];
-              while (eb) {
-                const int k = __ffs(eb) - 1;
-                eb &= eb - 1;
-                const int jl = c * 32 + k;
-                const int gj = J * 128 + jl;
-                float r = 0.f;
-#pragma unroll
-                for (int kk = 0; kk < 32; ++kk)
-                  if (kk == k) r = __uint_as_float(v[kk]);
-                if ((spbits[c] >> k) & 1u) {
-                  bool e;
-                  hash_lookup(a, pair_key(gi, gj), r, e);
-                } else if (slow && (rowbad || a.bad[gj])) {
-                  r = 0.f;
-                }
-                const uint32_t* cj = S.colmask[h][jl];
-                int rk = 0;
-                for (int w = 0; w < q; ++w) rk += __popc(cj[w]);
-                rk += __popc(cj[q] & below);
-                const int pc = S.colbase[h][jl] + rk;
-                put_edge(a, rowpos, gj, r);
-                put_edge(a, pc, gi, r);
-                ++rowpos;
-              }
+            for (int k = 0; k < 32; ++k) {
+              const float r = __uint_as_float(v[k]);
+              pm[k & 7] |= (((ABS ? fabsf(r) : r) >= lo_thr) | (fabsf(r) >= lim)) ? (1u << k) : 0u;
             }
           }
-        }
-      } else if (PASS != 2) {
-        // keep the per-half barrier phases in step with the active halves
-        if (!half_sync(S, h, hphase)) {
-          atomicOr(a.err, ERR_TIMEOUT);
-          S.abort = 1;
-        } else if (PASS == 1 && !half_sync(S, h, hphase)) {
-          atomicOr(a.err, ERR_TIMEOUT);
-          S.abort = 1;
+          uint32_t it = ((pm[0] | pm[1]) | (pm[2] | pm[3])) | ((pm[4] | pm[5]) | (pm[6] | pm[7]));
+          uint32_t badm = 0;
+          if (slow) {
+            for (int k = 0; k < 32; ++k)
+              if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm |= 1u << k;
+            it = (it & ~badm) | (zero_edge ? badm : 0u);
+          }
+          it &= valid;
+          // slots in the warp's edge-list chunk: warp prefix scan of the counts
+          const int ne = __popc(it);
+          int incl = ne;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(0xffffffffu, incl, 31);
+          uint2* dst = a.elist + wcur + (incl - ne);
+          // classify this lane's few interesting entries; candidates are only
+          // flagged here (collected for the exact recompute after the pass)
+          uint32_t eb = 0;
+          uint32_t w2 = it;
+          while (w2) {
+            const int k = __ffs(w2) - 1;
+            w2 &= w2 - 1;
+            uint32_t val = pick32(v, k);
+            const float r = __uint_as_float(val);
+            const float x = ABS ? fabsf(r) : r;
+            uint32_t cf = 0;
+            if ((badm >> k) & 1u) {
+              val = 0u;  // NaN voxel: r = 0 (post_block), decided exactly above
+            } else if (!((x - tau > delta) && (fabsf(r) < lim))) {
+              cf = 1u;  // candidate: collected for the exact recompute after the pass
+              val = 0u;
+            }
+            eb |= (cf ^ 1u) << k;
+            if (wok) *dst++ = make_uint2(elist_key(il, c * 32 + k, cf), val);
+          }
+          rowcount += __popc(eb);
+          S.colmask[h][c * 32 + lane][q] = transpose32(eb, lane);
+          wcur += total;
         }
       }
+      // the accumulator has been read: hand it back to the MMA warp
       ptx::tc_fence_before();
       ptx::mbar_arrive(ptx::smem_u32(&S.tempty[acc]));
+      if (PASS == 2) continue;
+      if (active && lane == 0)
+        a.etab[subtile_index(I, J, a.nb) * 4 + q] =
+            wok ? make_longlong2(start, wcur - start) : make_longlong2(0, 0);
+      if (!half_sync(S, h, hphase)) {
+        atomicOr(a.err, ERR_TIMEOUT);
+        S.abort = 1;
+        break;
+      }
+      if (active) {
+        const uint32_t* cm = S.colmask[h][il];
+        const int cc = __popc(cm[0]) + __popc(cm[1]) + __popc(cm[2]) + __popc(cm[3]);
+        if (diag) {
+          a.seg[(size_t)I * a.n_pad + gi] = rowcount + cc;
+        } else {
+          a.seg[(size_t)J * a.n_pad + gi] = rowcount;
+          a.seg[(size_t)I * a.n_pad + J * 128 + il] = cc;
+        }
+      }
     }
   }
   ptx::tc_fence_before();
@@ -440,7 +464,7 @@ cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cuda
   return cudaGetLastError();
 }
 
-// pass 0 count, 1 fill, 2 dump (tiles must then hold the one tile to dump)
+// pass 0 count (+ edge lists), 2 dump (tiles must then hold the one tile to dump)
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st) {
@@ -458,27 +482,13 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int n
   p.dump_half = dump_half;
   const int g = grid < ntiles ? grid : ntiles;
   if (g <= 0) return cudaSuccess;
-  cudaError_t e;
-  switch (pass) {
-    case 0:
-      e = cudaFuncSetAttribute(corr_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)TC_SMEM_BYTES);
-      if (e != cudaSuccess) return e;
-      corr_tc_kernel<0><<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
-      break;
-    case 1:
-      e = cudaFuncSetAttribute(corr_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)TC_SMEM_BYTES);
-      if (e != cudaSuccess) return e;
-      corr_tc_kernel<1><<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
-      break;
-    default:
-      e = cudaFuncSetAttribute(corr_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)TC_SMEM_BYTES);
-      if (e != cudaSuccess) return e;
-      corr_tc_kernel<2><<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
-      break;
-  }
+  const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
+  auto kern = pass == 0 ? (absm ? corr_tc_kernel<0, true> : corr_tc_kernel<0, false>)
+                        : corr_tc_kernel<2, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TC_SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  kern<<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(mh, ml, p);
   return cudaGetLastError();
 }
 
