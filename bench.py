@@ -37,7 +37,8 @@ def parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--precision", default=None)
+    p.add_argument("--precision", default="bf16x3")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
     p.add_argument("--workload", default="n45k")
     p.add_argument("--impl", default="gb300")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -72,15 +73,19 @@ def cpu_model() -> str:
 
 def cpu_sample(w, bold, seconds: float, threads: int) -> dict:
     """Reference CPU arithmetic (CorMat_cpu_MT + |r| > tau) on a row sample,
-    grown until it takes about `seconds`; edges/s over the sampled pairs."""
+    sized from a calibration run to take about `seconds`; edges/s over the
+    sampled pairs (the fixed per-call transpose is part of the timed work)."""
     import oracle
     N, T = w.N, w.T
-    rows = 8
+    t0 = time.perf_counter()
+    oracle.rows_mt_f32_count(bold, 0, 1, w.value, threads)
+    fixed = time.perf_counter() - t0
+    rows = 64
     t0 = time.perf_counter()
     oracle.rows_mt_f32_count(bold, 0, rows, w.value, threads)
-    dt = max(time.perf_counter() - t0, 1e-3)
+    dt = max(time.perf_counter() - t0 - fixed, 1e-3)
     pairs_per_s = sum(N - 1 - i for i in range(rows)) / dt
-    target_pairs = pairs_per_s * seconds
+    target_pairs = pairs_per_s * max(seconds - fixed, 0.5)
     acc, r1 = 0, 0
     while acc < target_pairs and r1 < N:
         acc += N - 1 - r1
@@ -210,7 +215,7 @@ def main():
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     w = workloads.get(args.workload)
-    precision = args.precision or "fp32"
+    precision = args.precision
     bold_h = w.bold()
     T, N = bold_h.shape
     bold = torch.from_numpy(bold_h).to(dev)
@@ -253,6 +258,29 @@ def main():
     pairs = N * (N - 1) // 2
     flop = pairs * 2.0 * T
     value = world * nnz / (ms / 1000.0)
+
+    # the plain FP32 CUDA-core form on the same input, same edge set (3 timed steps)
+    plain = None
+    if precision != "fp32" and not args.no_plain:
+        for _ in range(2):
+            rp = b.corr_csr(bold, mode=w.mode, value=w.value, precision="fp32",
+                            weighted=w.weighted, copy=False)
+        pms = []
+        for _ in range(3):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rp = b.corr_csr(bold, mode=w.mode, value=w.value, precision="fp32",
+                            weighted=w.weighted, copy=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            pms.append(e0.elapsed_time(e1))
+        pm = statistics.median(pms)
+        plain = {"value": rp.nnz / (pm / 1000.0), "unit": "edges/s", "ms_per_step": pm,
+                 "nnz": rp.nnz, "same_edge_count": rp.nnz == nnz,
+                 "tflops_algorithmic": flop / (pm / 1000.0) / 1e12,
+                 "speedup_of_chosen_form": pm / ms}
 
     # end to end through the host-buffer API: pinned BOLD in, CSR to host
     pinned = torch.from_numpy(bold_h).pin_memory()
@@ -301,6 +329,7 @@ def main():
         "band_candidates": stats[-1]["band_candidates"], "band_1e6": stats[-1]["band_1e6"],
         "delta": stats[-1]["delta"],
         "roofline": roof,
+        "plain_fp32": plain,
         "e2e": {"value": world * he.nnz / (e2e / 1000.0), "unit": "edges/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms": e2e},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),

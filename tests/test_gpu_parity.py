@@ -61,6 +61,15 @@ def test_zscore_bit_exact(builder):
         b = bna.synth_bold(N, T, 10, N + T)
         if N > 5:
             b[:, 3] = 1.25  # zero-variance voxel -> NaN row
+        if N > 10:
+            # wide dynamic range in one series (the exact integer mean sum does
+            # not apply; the sequential double sum must), an offset series and
+            # a series with zeros and subnormals
+            rng = np.random.default_rng(T)
+            b[:, 7] = (rng.standard_normal(T) * 10.0 ** rng.uniform(-8, 6, T)).astype(np.float32)
+            b[:, 8] = b[:, 8] + np.float32(1000.0)
+            b[::3, 9] = 0.0
+            b[1::5, 9] = np.float32(1e-40)
         z = builder.zscore(dev(b)).cpu().numpy()
         ref = oracle.zscore(b)
         assert z.shape[1] >= T and not z[:, T:].any()
