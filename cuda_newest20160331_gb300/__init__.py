@@ -187,6 +187,25 @@ class Builder:
             lib().bna_csr_free_host(C.byref(out))
         return CsrResult(N, nnz, rp, ci, va, st.as_dict())
 
+    def corr_csr_host_into(self, bold: np.ndarray, row_ptr: np.ndarray, col_idx: np.ndarray,
+                           val: Optional[np.ndarray], mode: str = "r_gt", value: float = 0.5,
+                           precision: str = "fp32", delta: Optional[float] = None):
+        """Host form into caller-owned buffers (pinned numpy views make it fast).
+
+        Returns (nnz, stats); raises BnaError(13) when col_idx / val are too small."""
+        assert bold.dtype == np.float32 and bold.flags.c_contiguous
+        T, N = bold.shape
+        assert row_ptr.dtype == np.int32 and len(row_ptr) >= N + 1
+        o = _opts(mode, value, precision, val is not None, delta)
+        nnz = C.c_int64()
+        st = L.CorrStats()
+        _check(lib().bna_corr_csr_host_into(
+            self._h, bold.ctypes.data, N, T, C.byref(o), row_ptr.ctypes.data,
+            col_idx.ctypes.data if len(col_idx) else None,
+            val.ctypes.data if val is not None and len(val) else None, len(col_idx),
+            C.byref(nnz), C.byref(st)), self._h)
+        return int(nnz.value), st.as_dict()
+
     def tile_values(self, bold, I: int, J: int, precision: str = "fp32", stream=None):
         """Approximate r of the 128 x 128 tile (I, J) for a precision form."""
         import torch

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(PKG, "libbna.so")
 # enums (bna.h)
 BNA_OK = 0
 BNA_NOT_CONVERGED = 4
+BNA_CAPACITY = 13
 THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4}
 PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2}
 SYNTH_KINDS = {"iid": 0, "blocknet": 1}
@@ -67,6 +68,10 @@ SIGNATURES = {
                                       C.POINTER(CorrOpts), C.POINTER(Csr),
                                       C.POINTER(CorrStats)]),
     "bna_csr_free_host": (None, [C.POINTER(Csr)]),
+    "bna_corr_csr_host_into": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                           C.POINTER(CorrOpts), C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
+                                           C.POINTER(CorrStats)]),
     "bna_corr_tile_values": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                          C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "bna_ec": (C.c_int32, [C.c_void_p, C.POINTER(Csr), C.c_int32, C.c_double, C.c_void_p,

@@ -252,6 +252,7 @@ const char* bna_status_string(int32_t s) {
     case BNA_INTERNAL: return "internal consistency check failed";
     case BNA_UNSUPPORTED: return "unsupported";
     case BNA_SCRATCH_LIMIT: return "problem exceeds the fixed scratch of the no-allocation entry point";
+    case BNA_CAPACITY: return "output buffers too small";
     default: return "unknown status";
   }
 }
@@ -414,7 +415,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     ++passes;
     CK(cudaEventRecord(ctx->ev[2], st));
     CK(launch_collect_candidates(a, ctx->sms, st));
-    CK(launch_recompute(a, ctx->sms * 4, st));
+    CK(launch_recompute(a, ctx->sms * 8, st));
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
                        st));
@@ -513,6 +514,40 @@ int32_t bna_corr_csr_host(bna_ctx* ctx, const float* bold_host, int32_t N, int32
     if (d.val)
       CK(cudaMemcpyAsync(out_host->val, d.val, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost,
                          nullptr));
+  }
+  CK(cudaStreamSynchronize(nullptr));
+  return BNA_OK;
+}
+
+int32_t bna_corr_csr_host_into(bna_ctx* ctx, const float* bold_host, int32_t N, int32_t T,
+                               const bna_corr_opts* opts, int32_t* row_ptr_host,
+                               int32_t* col_idx_host, float* val_host, int64_t cap,
+                               int64_t* nnz_out, bna_corr_stats* stats) {
+  if (!ctx || !bold_host || !opts || !row_ptr_host || N < 1 || T < 1 || cap < 0)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_host_into: bad arguments");
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  float* bold;
+  ENSURE(S_BOLD, (size_t)N * T * sizeof(float), bold);
+  CK(cudaMemcpyAsync(bold, bold_host, (size_t)N * T * sizeof(float), cudaMemcpyHostToDevice,
+                     nullptr));
+  bna_csr d{};
+  s = bna_corr_csr(ctx, bold, N, T, opts, &d, stats, nullptr);
+  if (s) return s;
+  if (nnz_out) *nnz_out = d.nnz;
+  CK(cudaMemcpyAsync(row_ptr_host, d.row_ptr, (size_t)(N + 1) * 4, cudaMemcpyDeviceToHost,
+                     nullptr));
+  if (d.nnz > cap) {
+    CK(cudaStreamSynchronize(nullptr));
+    return fail(ctx, BNA_CAPACITY, "%lld entries do not fit the %lld given", (long long)d.nnz,
+                (long long)cap);
+  }
+  if (d.nnz > 0) {
+    if (!col_idx_host) return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_host_into: col_idx is NULL");
+    CK(cudaMemcpyAsync(col_idx_host, d.col_idx, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost,
+                       nullptr));
+    if (d.val && val_host)
+      CK(cudaMemcpyAsync(val_host, d.val, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost, nullptr));
   }
   CK(cudaStreamSynchronize(nullptr));
   return BNA_OK;

@@ -166,11 +166,13 @@ __device__ __forceinline__ uint32_t elist_key(int il, int jl, uint32_t cand) {
   return (uint32_t)il | ((uint32_t)jl << 7) | (cand << 14);
 }
 
-// Upper-triangular tile index -> (I, J), I <= J, row-major over I.
+// Upper-triangular tile index -> (I, J), I <= J, row-major over I.  A float
+// square root gives the row to within one; integer steps settle it.
 __device__ __forceinline__ void tile_coords(long long t, int nt, int& I, int& J) {
   // rows before I hold I*nt - I*(I-1)/2 tiles
-  double disc = (2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * (double)t;
-  int i = (int)(((2.0 * nt + 1.0) - sqrt(disc)) * 0.5);
+  const float b = 2.0f * (float)nt + 1.0f;
+  const float disc = fmaxf(b * b - 8.0f * (float)t, 0.0f);
+  int i = (int)((b - sqrtf(disc)) * 0.5f);
   if (i < 0) i = 0;
   if (i > nt - 1) i = nt - 1;
   auto start = [nt](long long r) { return r * nt - r * (r - 1) / 2; };

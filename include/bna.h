@@ -43,7 +43,8 @@ typedef enum bna_status {
   BNA_CORRUPT_FILE = 9,       /* .csr lengths inconsistent (W/CUEC/weighted-net.cu:283) */
   BNA_INTERNAL = 10,          /* an internal consistency check failed */
   BNA_UNSUPPORTED = 11,
-  BNA_SCRATCH_LIMIT = 12      /* problem larger than bna_ec_noalloc's fixed scratch */
+  BNA_SCRATCH_LIMIT = 12,     /* problem larger than bna_ec_noalloc's fixed scratch */
+  BNA_CAPACITY = 13           /* caller's output buffers too small (required size reported) */
 } bna_status;
 
 /* Threshold rules.  r below is the reference's value after post_block
@@ -142,6 +143,17 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
 int32_t bna_corr_csr_host(bna_ctx* ctx, const float* bold_host, int32_t N, int32_t T,
                           const bna_corr_opts* opts, bna_csr* out_host, bna_corr_stats* stats);
 void bna_csr_free_host(bna_csr* csr);
+
+/* Host-buffer form with caller-owned outputs, like FormCSRGraph's R, C, V
+ * (CorMat.cpp:889, caller-allocated after FormFullGraph returned Clength).
+ * row_ptr_host has N+1 entries; col_idx_host and val_host (NULL for a binary
+ * graph) have room for `cap` entries.  Pinned buffers make the copies fast.
+ * *nnz_out receives the edge count; if it exceeds cap, only row_ptr is
+ * written and BNA_CAPACITY is returned so the caller can grow and retry. */
+int32_t bna_corr_csr_host_into(bna_ctx* ctx, const float* bold_host, int32_t N, int32_t T,
+                               const bna_corr_opts* opts, int32_t* row_ptr_host,
+                               int32_t* col_idx_host, float* val_host, int64_t cap,
+                               int64_t* nnz_out, bna_corr_stats* stats);
 
 /* Approximate correlation values of one BM x BN tile (rows I*128.., columns
  * J*128.. of the z-scored matrix), written row-major to out_dev (128 x 128

@@ -129,6 +129,21 @@ def test_host_buffer_path_equals_device_path(builder):
     assert np.array_equal(h.val, d.val)
 
 
+def test_host_into_caller_buffers_and_capacity(builder):
+    b = bna.synth_bold(1000, 64, 10, 13)
+    d = builder.corr_csr(dev(b), mode="r_gt", value=0.45).numpy()
+    rp = np.empty(1001, np.int32)
+    small = np.empty(10, np.int32)
+    with pytest.raises(bna.BnaError) as e:
+        builder.corr_csr_host_into(b, rp, small, np.empty(10, np.float32), mode="r_gt", value=0.45)
+    assert e.value.status == 13
+    ci = np.empty(d.nnz, np.int32)
+    va = np.empty(d.nnz, np.float32)
+    nnz, st = builder.corr_csr_host_into(b, rp, ci, va, mode="r_gt", value=0.45)
+    assert nnz == d.nnz and np.array_equal(rp, d.row_ptr)
+    assert np.array_equal(ci, d.col_idx) and np.array_equal(va, d.val)
+
+
 def test_repeat_calls_are_deterministic(builder):
     b = dev(bna.synth_bold(2000, 120, 20, 5))
     r1 = builder.corr_csr(b, mode="r_gt", value=0.3).numpy()
