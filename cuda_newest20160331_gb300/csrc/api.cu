@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -42,6 +43,7 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int n
                            cudaStream_t st);
 cudaError_t launch_csr_fill(const CorrArgs& a, int sms, cudaStream_t stream);
 cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream);
+cudaError_t launch_cand_values(const CorrArgs& a, float* vals, int grid, cudaStream_t stream);
 }  // namespace bna
 
 using namespace bna;
@@ -51,7 +53,7 @@ namespace {
 enum Slot {
   S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
-  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_COUNT
+  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -218,6 +220,7 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
   return BNA_OK;
 }
 
+// pass 0: count (+ edge lists); pass 3: density histogram
 int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st) {
   switch (precision) {
     case BNA_PREC_FP32: CK(launch_corr_simt(a, pass, st)); return BNA_OK;
@@ -354,8 +357,9 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown threshold mode %d", opts->mode);
   if (opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_TF32)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown precision %d", opts->precision);
-  if (opts->mode == BNA_THR_DENSITY)
-    return fail(ctx, BNA_UNSUPPORTED, "density mode is not built in this library");
+  const bool density = opts->mode == BNA_THR_DENSITY;
+  if (density && !(opts->value >= 0.0 && opts->value <= 100.0))
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: density %g%% outside [0, 100]", opts->value);
   int32_t s = set_device(ctx);
   if (s) return s;
   cudaStream_t st = as_stream(stream);
@@ -369,10 +373,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     if (s) return s;
   }
   CK(cudaEventRecord(ctx->ev[1], st));
-  a.th.mode = opts->mode;
-  a.th.tau = (float)opts->value;
   const double delta = opts->delta > 0 ? opts->delta : default_delta(prec, T);
-  a.th.delta = (float)delta;
   a.weighted = opts->weighted ? 1 : 0;
 
   ENSURE(S_SEG, (size_t)a.nb * a.n_pad * sizeof(int32_t), a.seg);
@@ -389,12 +390,66 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   a.stats = ds->stats;
   a.drop_keys = nullptr;
   a.n_drop = 0;
+  a.cand_val = nullptr;
   DevStatus* hs = reinterpret_cast<DevStatus*>(ctx->pinned);
-
   const long long nst = (long long)a.nb * (a.nb + 1) / 2;
   ENSURE(S_ETAB, (size_t)nst * 4 * sizeof(longlong2), a.etab);
   a.epool = &ds->epool;
+
+  // ---- threshold of the count pass
+  long long k_dens = 0;  // density: exact undirected edge count (CorMat.cpp:327-329)
+  if (!density) {
+    a.th.mode = opts->mode;
+    a.th.tau = (float)opts->value;
+    a.th.delta = (float)delta;
+  } else {
+    const long long M1 = (long long)N * (N - 1) / 2;
+    const float sf = (float)opts->value;
+    long long clen = (long long)((double)((float)(2 * M1) * sf) / 100.0);
+    clen += clen % 2;
+    k_dens = clen / 2;
+    if (k_dens == 0) {
+      a.th.mode = BNA_THR_R_GT;  // no edge at all
+      a.th.tau = 2.0f;
+      a.th.delta = (float)delta;
+    } else {
+      // histogram pass: locate the bin(s) that can hold the k-th largest r
+      unsigned int* hist;
+      ENSURE(S_HIST, (kHistBins + 1) * sizeof(unsigned int), hist);
+      CK(cudaMemsetAsync(hist, 0, (kHistBins + 1) * sizeof(unsigned int), st));
+      a.hist = hist;
+      a.th.mode = BNA_THR_R_GE;
+      a.th.tau = 0.0f;
+      a.th.delta = (float)delta;
+      s = corr_pass(ctx, a, prec, 3, st);
+      if (s) return s;
+      std::vector<unsigned int> hh(kHistBins + 1);
+      CK(cudaMemcpyAsync(hh.data(), hist, hh.size() * sizeof(unsigned int),
+                         cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      const long long specials = hh[kHistBins];
+      long long cum = 0;
+      int b1 = 0, b2 = 0;
+      bool f1 = false, f2 = false;
+      for (int b = kHistBins - 1; b >= 0; --b) {
+        cum += hh[b];
+        if (!f2 && cum >= k_dens - specials) { b2 = b; f2 = true; }
+        if (!f1 && cum >= k_dens) { b1 = b; f1 = true; }
+      }
+      if (!f2) b2 = kHistBins - 1;
+      const double w = 2.0 / kHistBins;
+      const double A = (b1 * w - 1.0) - delta;        // tau* >= A
+      const double B = ((b2 + 1) * w - 1.0) + delta;  // tau* <= B
+      // count pass band = every pair whose exact r can lie in [A, B]
+      a.th.mode = BNA_THR_R_GE;
+      a.th.tau = (float)(0.5 * (A + B));
+      a.th.delta = (float)((0.5 * (B - A) + delta) * (1.0 + 1e-6) + 1e-7);
+    }
+  }
+  const Threshold count_th = a.th;
+
   int passes = 0;
+  float* cvals = nullptr;
   for (int attempt = 0;; ++attempt) {
     a.cand_cap = ctx->cand_cap;
     // the pool hands out one chunk per warp at a time: room for two per warp
@@ -408,22 +463,28 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     ENSURE(S_HVAL, hcap * 4, a.hval);
     ENSURE(S_HEDGE, hcap, a.hedge);
     ENSURE(S_ELIST, (size_t)a.ecap * sizeof(uint2), a.elist);
+    if (density && k_dens > 0) ENSURE(S_CANDVAL, (size_t)a.cand_cap * sizeof(float), cvals);
     CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
     CK(cudaMemsetAsync(a.hkeys, 0xff, hcap * 8, st));
+    a.th = count_th;
     s = corr_pass(ctx, a, prec, 0, st);
     if (s) return s;
     ++passes;
     CK(cudaEventRecord(ctx->ev[2], st));
     CK(launch_collect_candidates(a, ctx->sms, st));
-    CK(launch_recompute(a, ctx->sms * 8, st));
-    CK(cudaEventRecord(ctx->ev[3], st));
-    CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
-                       st));
+    if (density && k_dens > 0) {
+      CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
+    } else {
+      CK(launch_recompute(a, ctx->sms * 8, st));
+      CK(cudaEventRecord(ctx->ev[3], st));
+      CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
+                         st));
+    }
     CK(cudaEventRecord(ctx->ev[4], st));
     CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     bool again = false;
-    if ((hs->err & ERR_BAND_OVERFLOW) && attempt < 3) {
+    if ((hs->err & (ERR_BAND_OVERFLOW | ERR_HASH_FULL)) && attempt < 3) {
       ctx->cand_cap = (long long)(hs->cand_count * 3 / 2) + 1024;
       again = true;
     }
@@ -439,6 +500,60 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   if (hs->err & ERR_ELIST)
     return fail(ctx, BNA_INTERNAL, "edge-list pool overflow (%llu entries)", hs->epool);
   if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
+  long long ties_dropped = 0;
+  if (density && k_dens > 0) {
+    // FormFullGraph_s (CorMat.cpp:770-808): tau* = the k-th largest r; every
+    // larger pair is an edge; of the pairs equal to tau*, the first ones in
+    // row-major (i < j) order are kept up to k edges.  Every pair that can be
+    // tau* or a tie is a candidate with its exact value here.
+    const long long n = (long long)hs->cand_count;
+    const long long definite = (long long)hs->stats[2];
+    const long long need = k_dens - definite;
+    if (need < 1 || need > n)
+      return fail(ctx, BNA_INTERNAL, "density window missed the k-th value (k %lld, definite %lld, "
+                  "candidates %lld)", k_dens, definite, n);
+    std::vector<float> v(n);
+    std::vector<uint2> keys(n);
+    CK(cudaMemcpyAsync(v.data(), cvals, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(keys.data(), a.cand, n * sizeof(uint2), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<float> w(v);
+    std::nth_element(w.begin(), w.begin() + (need - 1), w.end(), std::greater<float>());
+    const float tau_star = w[need - 1];
+    long long greater = definite;
+    std::vector<unsigned long long> ties;
+    for (long long c = 0; c < n; ++c) {
+      if (v[c] > tau_star) ++greater;
+      else if (v[c] == tau_star)
+        ties.push_back(((unsigned long long)keys[c].x << 32) | keys[c].y);
+    }
+    const long long keep = k_dens - greater;
+    std::sort(ties.begin(), ties.end());
+    std::vector<unsigned long long> drop(ties.begin() + std::min<long long>(keep, ties.size()),
+                                         ties.end());
+    std::sort(drop.begin(), drop.end());
+    ties_dropped = (long long)drop.size();
+    unsigned long long* dk = nullptr;
+    ENSURE(S_DROP, std::max<size_t>(drop.size(), 1) * 8, dk);
+    if (!drop.empty())
+      CK(cudaMemcpyAsync(dk, drop.data(), drop.size() * 8, cudaMemcpyHostToDevice, st));
+    a.drop_keys = dk;
+    a.n_drop = (int)drop.size();
+    a.th.mode = BNA_THR_DENSITY;
+    a.th.tau = tau_star;
+    a.cand_val = cvals;
+    CK(launch_recompute(a, ctx->sms * 8, st));
+    CK(cudaEventRecord(ctx->ev[3], st));
+    CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
+                       st));
+    CK(cudaEventRecord(ctx->ev[4], st));
+    CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
+    if (hs->total != 2 * k_dens)
+      return fail(ctx, BNA_INTERNAL, "density: %lld entries instead of %lld", hs->total,
+                  2 * k_dens);
+  }
   if (hs->err & ERR_NNZ_INT32 || hs->total > 0x7fffffffLL)
     return fail(ctx, BNA_NNZ_OVERFLOW_INT32, "nnz %lld exceeds int32", hs->total);
   const long long nnz = hs->total;
@@ -465,15 +580,18 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   out_dev->val = val;
   if (stats) {
     std::memset(stats, 0, sizeof *stats);
-    stats->tau = (double)a.th.tau;
+    stats->tau = density && k_dens == 0 ? INFINITY : (double)a.th.tau;
     stats->delta = delta;
     stats->nnz = nnz;
     stats->band_candidates = (int64_t)cand_count;
     stats->band_edges = (int64_t)band_edges;
     stats->band_1e6 = (int64_t)band_1e6;
-    stats->passes = passes;
-    // z-score, [block flags], per attempt: count, collect, recompute, 4 scan kernels; fill
-    stats->kernel_launches = 1 + (prec == BNA_PREC_BF16X3 ? 1 : 0) + passes * 7 + 1;
+    stats->ties_dropped = ties_dropped;
+    stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
+    // z-score, [block flags], [histogram], per attempt: count, collect, recompute or values,
+    // 4 scan kernels; [decide + 4 scan kernels]; fill
+    stats->kernel_launches = 1 + (prec == BNA_PREC_BF16X3 ? 1 : 0) +
+                             (density && k_dens > 0 ? 1 + passes * 3 + 5 : passes * 7) + 1;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);

@@ -28,6 +28,15 @@ enum : uint32_t {
 // entries per warp (one atomic per chunk) and never writes past ecap.
 constexpr long long kElistChunk = 16384;
 
+// Density mode: histogram of the approximate r over [-1, 1) in kHistBins
+// bins (bin = floor((r + 1) * kHistBins / 2)); entry kHistBins counts the
+// pairs near +-1 whose clamped value is not known yet.
+constexpr int kHistBins = 2048;
+__device__ __forceinline__ int hist_bin(float r) {
+  int b = (int)floorf((r + 1.0f) * (0.5f * kHistBins));
+  return b < 0 ? 0 : (b >= kHistBins ? kHistBins - 1 : b);
+}
+
 // Outcome of classifying one approximate correlation.
 enum : int { CLS_NO = 0, CLS_EDGE = 1, CLS_BAND = 2 };
 
@@ -100,7 +109,9 @@ struct CorrArgs {
   const unsigned long long* drop_keys;
   int n_drop;
   uint32_t* err;
-  unsigned long long* stats;  // [0]=band edges [1]=band within 1e-6
+  unsigned long long* stats;  // [0]=band edges [1]=band within 1e-6 [2]=definite listed edges
+  unsigned int* hist;         // density histogram pass: kHistBins + 1 counters
+  const float* cand_val;      // density: exact values of the candidates (decide pass)
 };
 
 // Fill-pass store with a range check (an inconsistent count would otherwise

@@ -99,6 +99,24 @@ __device__ __forceinline__ bool in_sorted(const unsigned long long* keys, int n,
   return lo < n && keys[lo] == k;
 }
 
+// Exact values of the candidates only (density mode: the threshold is
+// selected from them before any decision is made).
+__global__ void cand_values_kernel(CorrArgs a, float* vals) {
+  const unsigned long long cnt = *a.cand_count;
+  const long long n = (long long)cnt < a.cand_cap ? (long long)cnt : a.cand_cap;
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long c = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); c < n;
+       c += nwarps) {
+    const uint2 p = a.cand[c];
+    const float r = exact_r_warp(a, (int)p.x, (int)p.y, lane);
+    if (lane == 0) vals[c] = r;
+  }
+}
+
+// Decide every candidate on its exact value (computed here, or given in
+// a.cand_val), add the edges to the counts and store value + decision in the
+// hash the fill pass reads.
 __global__ void recompute_kernel(CorrArgs a) {
   const unsigned long long cnt = *a.cand_count;
   const long long n = (long long)cnt < a.cand_cap ? (long long)cnt : a.cand_cap;
@@ -108,7 +126,7 @@ __global__ void recompute_kernel(CorrArgs a) {
        c += nwarps) {
     const uint2 p = a.cand[c];
     const int i = (int)p.x, j = (int)p.y;
-    const float r = exact_r_warp(a, i, j, lane);
+    const float r = a.cand_val ? a.cand_val[c] : exact_r_warp(a, i, j, lane);
     if (lane != 0) continue;
     const unsigned long long key = pair_key(i, j);
     bool e = edge_exact(r, a.th);
@@ -182,6 +200,10 @@ __global__ void collect_candidates_kernel(CorrArgs a, long long nst) {
         flag = ((key >> 14) & 1u) != 0u;
       }
       const uint32_t bal = __ballot_sync(0xffffffffu, flag);
+      // definite (unflagged) entries of this round, for the density selection
+      const int nvalid = (int)((E - e0) < 32 ? (E - e0) : 32);
+      if (lane == 0 && nvalid - __popc(bal) > 0)
+        atomicAdd(&a.stats[2], (unsigned long long)(nvalid - __popc(bal)));
       if (!bal) continue;
       unsigned long long base = 0;
       if (lane == 0) base = atomicAdd(a.cand_count, (unsigned long long)__popc(bal));
@@ -325,6 +347,11 @@ __global__ void scan_finish_kernel(const long long* pre, const long long* bsum, 
 
 cudaError_t launch_recompute(const CorrArgs& a, int grid, cudaStream_t stream) {
   recompute_kernel<<<grid, 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cand_values(const CorrArgs& a, float* vals, int grid, cudaStream_t stream) {
+  cand_values_kernel<<<grid, 256, 0, stream>>>(a, vals);
   return cudaGetLastError();
 }
 

@@ -22,7 +22,8 @@ constexpr int SB = 128;  // tile edge
 constexpr int SK = 16;   // K (time) chunk per stage
 constexpr int SPAD = 4;
 
-// PASS 0 = count (+ edge list), 2 = dump approximate values of one tile.
+// PASS 0 = count (+ edge list), 2 = dump approximate values of one tile,
+// 3 = density histogram.
 template <int PASS>
 __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, int dumpI,
                                                            int dumpJ, float* dump) {
@@ -104,6 +105,33 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
       }
     return;
   }
+  if (PASS == 3) {
+    // density histogram of the approximate values in shared memory (the
+    // operand tiles are free now), merged into the global one
+    unsigned int* h = reinterpret_cast<unsigned int*>(&As[0][0][0]);
+    for (int b = tid; b <= kHistBins; b += 256) h[b] = 0u;
+    __syncthreads();
+    const bool diag = (I == J);
+    const float lim = 1.0f - a.th.delta;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int il = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+      const bool rb = a.bad[I * SB + il] != 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int jl = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
+        const int gj = J * SB + jl;
+        if (gj >= a.n || (diag && jl <= il)) continue;
+        const bool badk = rb || a.bad[gj];
+        const float r = badk ? 0.0f : acc[i][j];
+        atomicAdd(&h[(!badk && !(fabsf(r) < lim)) ? kHistBins : hist_bin(r)], 1u);
+      }
+    }
+    __syncthreads();
+    for (int b = tid; b <= kHistBins; b += 256)
+      if (h[b]) atomicAdd(&a.hist[b], h[b]);
+    return;
+  }
 
   // ---- fused threshold epilogue ----
   if (tid < SB) {
@@ -124,7 +152,6 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
     badr |= (uint32_t)a.bad[i0 + il] << i;
     badc |= (uint32_t)a.bad[j0 + jl] << i;
   }
-  const bool zero_is_edge = edge_exact(0.0f, a.th);
   unsigned long long emask = 0ull, cmask = 0ull;  // edges, near-threshold candidates
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -136,8 +163,9 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
       if (gj >= a.n || (diag && jl <= il)) continue;
       int c;
       if (((badr >> i) | (badc >> j)) & 1u) {
-        acc[i][j] = 0.f;
-        c = zero_is_edge ? CLS_EDGE : CLS_NO;
+        acc[i][j] = 0.f;  // NaN voxel: the exact value is 0 (post_block)
+        const float x = 0.0f - a.th.tau;
+        c = x > a.th.delta ? CLS_EDGE : (x < -a.th.delta ? CLS_NO : CLS_BAND);
       } else {
         c = classify(acc[i][j], a.th);
       }
@@ -215,8 +243,12 @@ cudaError_t launch_corr_simt(const CorrArgs& a, int pass, cudaStream_t stream) {
   const int nt = a.nb;
   const long long tiles = (long long)nt * (nt + 1) / 2;
   if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-  if (pass != 0) return cudaErrorInvalidValue;
-  corr_simt_kernel<0><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
+  if (pass == 0)
+    corr_simt_kernel<0><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
+  else if (pass == 3)
+    corr_simt_kernel<3><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

@@ -52,6 +52,7 @@ struct TcSmem {
   uint32_t tmem_base;
   volatile uint32_t abort;
   uint32_t colmask[2][128][4];
+  unsigned int hist[kHistBins + 1];  // density histogram pass
 };
 
 constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_STAGES * TC_STAGE_BYTES + sizeof(TcSmem);
@@ -129,6 +130,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     S.abort = 0;
     ptx::fence_mbar_init();
   }
+  if (PASS == 3)
+    for (int b = threadIdx.x; b <= kHistBins; b += blockDim.x) S.hist[b] = 0u;
   if (warp == 1) {
     ptx::tmem_alloc(ptx::smem_u32(&S.tmem_base), TC_TMEM_COLS);
     ptx::tmem_relinquish();
@@ -239,7 +242,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // -1 can be an edge only through post_block's 0 for tau <= 0 in the signed
     // rules (|r| rules cover -1 like +1).
     const bool simple = (tau < lim) && (ABS || lo_thr > 0.0f);
-    const bool zero_edge = edge_exact(0.0f, a.th);
+    // a pair with a NaN voxel has the exact value 0 (post_block)
+    const bool zero_int = (0.0f >= lo_thr) || (0.0f >= lim);
     uint32_t hphase = 0;
     long long wcur = 0, wend = 0;  // this warp's current edge-list chunk [wcur, wend)
     bool wok = true;
@@ -267,9 +271,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int acc = m & 1;
       const uint32_t ar = (uint32_t)(m >> 1);
       const bool active = (PASS == 2) ? (J < a.nb) : ((J >= I) && (J < a.nb));
+      const bool listing = (PASS == 0);
       const int gi = I * 128 + il;
       long long start = 0;
-      if (PASS == 0 && active) {
+      if (listing && active) {
         // room for this warp's worst case (32 rows x 128 columns) in one chunk
         if (wend - wcur < 32 * 128) {
           long long base = 0;
@@ -319,6 +324,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int lo = il - c * 32 + 1;  // first column index k with jl > il
             valid &= (lo <= 0) ? 0xffffffffu : (lo >= 32 ? 0u : (0xffffffffu << lo));
           }
+          if (PASS == 3) {
+            // density histogram of the approximate values (exact 0 for NaN voxels)
+            uint32_t badm3 = 0;
+            if (slow)
+              for (int k = 0; k < 32; ++k)
+                if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm3 |= 1u << k;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+              if ((valid >> k) & 1u) {
+                const bool badk = (badm3 >> k) & 1u;
+                const float r = badk ? 0.0f : __uint_as_float(v[k]);
+                atomicAdd(&S.hist[(!badk && !(fabsf(r) < lim)) ? kHistBins : hist_bin(r)], 1u);
+              }
+            }
+            continue;
+          }
           // "interesting" = an edge or a candidate: x >= tau - delta, or
           // |r| >= 1 - delta; 8 partial masks so no long dependency chain forms
           uint32_t pm[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
@@ -340,7 +361,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           if (slow) {
             for (int k = 0; k < 32; ++k)
               if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm |= 1u << k;
-            it = (it & ~badm) | (zero_edge ? badm : 0u);
+            it = (it & ~badm) | (zero_int ? badm : 0u);
           }
           it &= valid;
           // slots in the warp's edge-list chunk: warp prefix scan of the counts
@@ -360,13 +381,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           while (w2) {
             const int k = __ffs(w2) - 1;
             w2 &= w2 - 1;
-            uint32_t val = pick32(v, k);
+            const bool badk = (badm >> k) & 1u;
+            uint32_t val = badk ? 0u : pick32(v, k);  // NaN voxel: exact r = 0
             const float r = __uint_as_float(val);
             const float x = ABS ? fabsf(r) : r;
             uint32_t cf = 0;
-            if ((badm >> k) & 1u) {
-              val = 0u;  // NaN voxel: r = 0 (post_block), decided exactly above
-            } else if (!((x - tau > delta) && (fabsf(r) < lim))) {
+            if (!((x - tau > delta) && (fabsf(r) < lim))) {
               cf = 1u;  // candidate: collected for the exact recompute after the pass
               val = 0u;
             }
@@ -381,7 +401,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // the accumulator has been read: hand it back to the MMA warp
       ptx::tc_fence_before();
       ptx::mbar_arrive(ptx::smem_u32(&S.tempty[acc]));
-      if (PASS == 2) continue;
+      if (PASS == 2 || PASS == 3) continue;
       if (active && lane == 0)
         a.etab[subtile_index(I, J, a.nb) * 4 + q] =
             wok ? make_longlong2(start, wcur - start) : make_longlong2(0, 0);
@@ -408,6 +428,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, TC_TMEM_COLS);
   }
+  if (PASS == 3)
+    for (int b = threadIdx.x; b <= kHistBins; b += blockDim.x)
+      if (S.hist[b]) atomicAdd(&a.hist[b], S.hist[b]);
 }
 
 __global__ void block_bad_kernel(const uint8_t* bad, int nb, uint8_t* blockbad) {
@@ -464,7 +487,8 @@ cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cuda
   return cudaGetLastError();
 }
 
-// pass 0 count (+ edge lists), 2 dump (tiles must then hold the one tile to dump)
+// pass 0 count (+ edge lists), 2 dump (tiles must then hold the one tile to dump),
+// 3 density histogram
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st) {
@@ -483,8 +507,9 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int n
   const int g = grid < ntiles ? grid : ntiles;
   if (g <= 0) return cudaSuccess;
   const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
-  auto kern = pass == 0 ? (absm ? corr_tc_kernel<0, true> : corr_tc_kernel<0, false>)
-                        : corr_tc_kernel<2, false>;
+  auto kern = pass == 0   ? (absm ? corr_tc_kernel<0, true> : corr_tc_kernel<0, false>)
+              : pass == 3 ? corr_tc_kernel<3, false>
+                          : corr_tc_kernel<2, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)TC_SMEM_BYTES);
   if (e != cudaSuccess) return e;

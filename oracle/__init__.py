@@ -41,6 +41,8 @@ def lib():
         o.orc_density.argtypes = [P, C.c_int, C.c_double, C.POINTER(C.c_int64), P, C.c_int64,
                                   C.POINTER(C.c_int64)]
         o.orc_density.restype = C.c_float
+        o.orc_density_k.argtypes = [C.c_int, C.c_double]
+        o.orc_density_k.restype = C.c_int64
         o.orc_ec.argtypes = [P, P, P, C.c_int, C.c_int, C.c_double, P, C.POINTER(C.c_double),
                              C.POINTER(C.c_double), C.POINTER(C.c_double)]
         o.orc_ec.restype = C.c_int
@@ -136,6 +138,11 @@ def density(packed: np.ndarray, N: int, s_percent: float):
         cap *= 16
 
 
+def density_k(N: int, s_percent: float) -> int:
+    """Undirected edge count of the density rule (CorMat.cpp:327-329 arithmetic)."""
+    return int(lib().orc_density_k(N, s_percent))
+
+
 def ec(R, Cc, V=None, max_iter: int = 10000, eps: float = 1e-6):
     R = np.ascontiguousarray(R, np.int32)
     Cc = np.ascontiguousarray(Cc, np.int32)
@@ -220,10 +227,10 @@ def ref_density_csr(bold: np.ndarray, s_percent: float):
     M1 = N * (N - 1) // 2
     packed = np.empty(M1, np.float32)
     r.ref_w_cormat_cpu(_p(packed), _p(bold), N, T)
-    clen = int(2 * M1 * s_percent / 100.0)
-    clen += clen % 2
+    k = density_k(N, s_percent)
+    clen = 2 * k
     adj = np.zeros(N * N, np.bool_)
-    tau = r.ref_w_form_full_graph_s(_p(adj), _p(packed), N, clen // 2)
+    tau = r.ref_w_form_full_graph_s(_p(adj), _p(packed), N, k)
     R = np.empty(N + 1, np.int32)
     Cc = np.empty(clen, np.int32)
     V = np.empty(clen, np.float32)

@@ -135,19 +135,29 @@ int64_t orc_threshold_csr(const float* packed, int N, int mode, float tau, const
   return nnz;
 }
 
-/* Density rule of FormFullGraph_s.  k = floor(2*M1*s/100) rounded up to even,
- * halved (CorMat.cpp:327-329); tau = k-th largest packed value; edges r >= tau
+/* Density rule of FormFullGraph_s.  k = orc_density_k (CorMat.cpp:327-329);
+ * tau = k-th largest packed value; edges r >= tau
  * in row-major (i<j) scan order, where once the count exceeds k the most
  * recent tie is removed (:797-808) — i.e. the earliest (k - #greater) ties in
  * scan order are kept.  Writes the sorted keys of the dropped ties to
  * drop_out (capacity drop_cap) and returns tau; *k_out = k, *ndrop_out = the
  * number of dropped ties (-1 if drop_cap was too small). */
+/* Edge count of the density rule as CorMat.cpp:327-328 computes it:
+ * Clength = (long long) 2*M1*s/100.0 with s a float (parsed by atof into
+ * real__t): the product 2*M1*s is formed in float, then divided in double. */
+int64_t orc_density_k(int N, double s_percent) {
+  const int64_t M1 = (int64_t)N * (N - 1) / 2;
+  const float s = (float)s_percent;
+  const float prod = (float)(2 * M1) * s;
+  int64_t clen = (int64_t)((double)prod / 100.0);
+  clen += clen % 2;
+  return clen / 2;
+}
+
 float orc_density(const float* packed, int N, double s_percent, int64_t* k_out,
                   uint64_t* drop_out, int64_t drop_cap, int64_t* ndrop_out) {
   const int64_t M1 = (int64_t)N * (N - 1) / 2;
-  int64_t clen = (int64_t)(2 * M1 * s_percent / 100.0);
-  clen += clen % 2;
-  const int64_t k = clen / 2;
+  const int64_t k = orc_density_k(N, s_percent);
   *k_out = k;
   if (k <= 0) {
     *ndrop_out = 0;

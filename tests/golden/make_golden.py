@@ -87,10 +87,7 @@ def workload_tau(N=45000, T=240, K=40, seed=2, s_percent=1.0):
     b = bna.synth_bold(N, T, K, seed).astype(np.float64)
     x = b.T - b.T.mean(axis=1, keepdims=True)
     z = x / np.sqrt((x * x).sum(axis=1, keepdims=True))
-    M1 = N * (N - 1) // 2
-    clen = int(2 * M1 * s_percent / 100.0)
-    clen += clen % 2
-    k = clen // 2
+    k = oracle.density_k(N, s_percent)
     nbins = 1 << 20
     hist = np.zeros(nbins + 1, np.int64)
     blk = 1024
@@ -141,12 +138,23 @@ def main():
     out["dupties_seed"] = np.int64(s)
     out["dupties_sha"] = np.frombuffer(hashlib.sha256(b.tobytes()).digest(), np.uint8)
     # a density whose k-th largest r is a tied value split by the cut, so that
-    # FormFullGraph_s has to drop ties (CorMat.cpp:797-808)
+    # FormFullGraph_s has to drop ties (CorMat.cpp:797-808); the percent goes
+    # through the reference's own edge-count arithmetic, so search for one
+    # whose k lands on the first of a tied pair
     P = oracle.cormat_packed(oracle.zscore(b))
     vals, counts = np.unique(P[P > 0.3], return_counts=True)
-    v = vals[counts >= 2][len(vals[counts >= 2]) // 2]
-    k = int((P > v).sum()) + 1
-    pct = k * 100.0 / len(P)
+    tied = vals[counts >= 2]
+    pct = None
+    for v in tied[len(tied) // 2:]:
+        k = int((P > v).sum()) + 1
+        for scale in (1.0, 1.0 + 1e-7, 1.0 - 1e-7, 1.0 + 3e-7):
+            cand = k * 100.0 / len(P) * scale
+            if oracle.density_k(400, cand) == k:
+                pct = cand
+                break
+        if pct is not None:
+            break
+    assert pct is not None
     out["dupties_percent"] = np.float64(pct)
     check_and_pack("dupties", b, "density", pct, out)
     assert out["dupties_ndrop"] >= 1

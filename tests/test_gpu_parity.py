@@ -121,6 +121,52 @@ def test_corr_csr_matches_reference_golden(builder, precision, name, N, T, K, se
                      res.stats["delta"])
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name,N,T,K,seed,pct", [
+    ("n1500_t240_dens1", 1500, 240, 20, 14, 1.0),
+    ("n700_t50_dens5", 700, 50, 5, 15, 5.0),
+])
+def test_density_matches_reference_golden(builder, precision, name, N, T, K, seed, pct):
+    """FormFullGraph_s: exactly k edges, tau* = the k-th largest r (CorMat.cpp:743-822)."""
+    gold = np.load(os.path.join(GOLD, "ref_cases.npz"))
+    b = bna.synth_bold(N, T, K, seed)
+    res = builder.corr_csr(dev(b), mode="density", value=pct, precision=precision)
+    assert np.float32(res.stats["tau"]) == gold[name + "_tau"]
+    assert res.nnz == 2 * oracle.density_k(N, pct)
+    assert_csr_equal(res, gold[name + "_R"], gold[name + "_C"], gold[name + "_V"],
+                     res.stats["delta"])
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_density_drops_ties_like_reference(builder, precision):
+    gold = np.load(os.path.join(GOLD, "ref_cases.npz"))
+    N, T = 400, 48
+    b = bna.synth_bold(N, T, 8, int(gold["dupties_seed"]))
+    for k in range(6):
+        b[:, N - 1 - k] = b[:, 3 * k + 1]
+    res = builder.corr_csr(dev(b), mode="density", value=float(gold["dupties_percent"]),
+                           precision=precision)
+    assert res.stats["ties_dropped"] == int(gold["dupties_ndrop"]) >= 1
+    assert np.float32(res.stats["tau"]) == gold["dupties_tau"]
+    assert_csr_equal(res, gold["dupties_R"], gold["dupties_C"], gold["dupties_V"],
+                     res.stats["delta"])
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_density_edge_cases(builder, precision):
+    b = bna.synth_bold(300, 40, 8, 5)
+    b[:, 11] = 2.0  # zero-variance voxel (its pairs are exact zeros)
+    z = oracle.zscore(b)
+    P = oracle.cormat_packed(z)
+    for pct in (0.0, 0.01, 35.0, 60.0, 100.0):
+        tau, k, drop = oracle.density(P, 300, pct)
+        res = builder.corr_csr(dev(b), mode="density", value=pct, precision=precision)
+        assert res.nnz == 2 * k, pct
+        if k:
+            R, C, V = oracle.threshold_csr(P, 300, "r_ge", tau, drop=drop)
+            assert_csr_equal(res, R, C, V, res.stats["delta"])
+
+
 def test_host_buffer_path_equals_device_path(builder):
     b = bna.synth_bold(1000, 64, 10, 13)
     h = builder.corr_csr_host(b, mode="r_gt", value=0.45)
