@@ -259,6 +259,25 @@ def main():
     flop = pairs * 2.0 * T
     value = world * nnz / (ms / 1000.0)
 
+    # eigenvector centrality on the device-resident CSR of the last step
+    # (Lead_Vector_GPU semantics: 10,000 iterations max, stop at 1e-6)
+    csr_dev = b.corr_csr(bold, mode=w.mode, value=w.value, precision=precision,
+                         weighted=w.weighted, copy=True)
+    ec_ms = []
+    for rep in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ec_vec, lam, iters, conv = b.ec(csr_dev)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ec_ms.append(e0.elapsed_time(e1))
+    ec_info = {"ms": statistics.median(ec_ms), "iterations": iters, "lambda": lam,
+               "converged": conv,
+               "hbm_gbs_per_iteration": (8.0 * csr_dev.nnz + 4.0 * (N + 1) + 16.0 * N) * iters
+               / (statistics.median(ec_ms) / 1000.0) / 1e9 if iters else None}
+    del csr_dev
+
     # the plain FP32 CUDA-core form on the same input, same edge set (3 timed steps)
     plain = None
     if precision != "fp32" and not args.no_plain:
@@ -335,6 +354,7 @@ def main():
         "delta": stats[-1]["delta"],
         "roofline": roof,
         "plain_fp32": plain,
+        "ec": ec_info,
         "e2e": {"value": world * he_nnz / (e2e / 1000.0), "unit": "edges/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms": e2e},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
