@@ -278,11 +278,11 @@ def main():
                / (statistics.median(ec_ms) / 1000.0) / 1e9 if iters else None}
     del csr_dev
 
-    # the plain FP32 CUDA-core form on the same input, same edge set (3 timed steps)
-    plain = None
-    if precision != "fp32" and not args.no_plain:
+    # the other forms on the same input, same edge set (3 timed steps each):
+    # plain FP32 on CUDA cores, and the single-product TF32 tensor-core form
+    def time_form(prec):
         for _ in range(2):
-            rp = b.corr_csr(bold, mode=w.mode, value=w.value, precision="fp32",
+            rp = b.corr_csr(bold, mode=w.mode, value=w.value, precision=prec,
                             weighted=w.weighted, copy=False)
         pms = []
         for _ in range(3):
@@ -290,16 +290,25 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            rp = b.corr_csr(bold, mode=w.mode, value=w.value, precision="fp32",
+            rp = b.corr_csr(bold, mode=w.mode, value=w.value, precision=prec,
                             weighted=w.weighted, copy=False)
             e1.record(stream)
             torch.cuda.synchronize()
             pms.append(e0.elapsed_time(e1))
         pm = statistics.median(pms)
-        plain = {"value": rp.nnz / (pm / 1000.0), "unit": "edges/s", "ms_per_step": pm,
-                 "nnz": rp.nnz, "same_edge_count": rp.nnz == nnz,
-                 "tflops_algorithmic": flop / (pm / 1000.0) / 1e12,
-                 "speedup_of_chosen_form": pm / ms}
+        return {"value": rp.nnz / (pm / 1000.0), "unit": "edges/s", "ms_per_step": pm,
+                "nnz": rp.nnz, "same_edge_count": rp.nnz == nnz,
+                "ms_count": rp.stats["ms_count"], "ms_recompute": rp.stats["ms_recompute"],
+                "band_candidates": rp.stats["band_candidates"], "delta": rp.stats["delta"],
+                "tflops_algorithmic": flop / (pm / 1000.0) / 1e12,
+                "speedup_of_chosen_form": pm / ms}
+
+    plain = None
+    if precision != "fp32" and not args.no_plain:
+        plain = time_form("fp32")
+    other_tc = None
+    if precision in ("bf16x3", "tf32") and not args.no_plain:
+        other_tc = time_form("tf32" if precision == "bf16x3" else "bf16x3")
 
     # end to end through the host-buffer API (bna_corr_csr_host_into): pinned
     # BOLD in, CSR out into pinned caller buffers, copies inside the timed region
@@ -354,6 +363,7 @@ def main():
         "delta": stats[-1]["delta"],
         "roofline": roof,
         "plain_fp32": plain,
+        ("tf32" if precision == "bf16x3" else "bf16x3"): other_tc,
         "ec": ec_info,
         "e2e": {"value": world * he_nnz / (e2e / 1000.0), "unit": "edges/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms": e2e},

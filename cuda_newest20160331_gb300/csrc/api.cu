@@ -38,7 +38,7 @@ void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, dou
                    double* e2, int* iter, int* done);
 void tc_tile_list(int nb, std::vector<int2>& out);
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
-cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
+cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st);
 cudaError_t launch_csr_fill(const CorrArgs& a, int sms, cudaStream_t stream);
@@ -225,7 +225,9 @@ int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cuda
   switch (precision) {
     case BNA_PREC_FP32: CK(launch_corr_simt(a, pass, st)); return BNA_OK;
     case BNA_PREC_BF16X3:
-      CK(launch_corr_tc(a, pass, reinterpret_cast<const int2*>(ctx->ptr[S_TILES]), ctx->ntiles,
+    case BNA_PREC_TF32:
+      CK(launch_corr_tc(a, pass, precision == BNA_PREC_BF16X3 ? 0 : 1,
+                        reinterpret_cast<const int2*>(ctx->ptr[S_TILES]), ctx->ntiles,
                         reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
                         ctx->sms, st));
       return BNA_OK;
@@ -366,9 +368,9 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   const int prec = opts->precision;
   CorrArgs a{};
   CK(cudaEventRecord(ctx->ev[0], st));
-  s = run_zscore(ctx, bold_dev, N, T, prec != BNA_PREC_FP32, a, st);
+  s = run_zscore(ctx, bold_dev, N, T, prec == BNA_PREC_BF16X3, a, st);
   if (s) return s;
-  if (prec == BNA_PREC_BF16X3) {
+  if (prec != BNA_PREC_FP32) {
     s = tc_prepare(ctx, a, st);
     if (s) return s;
   }
@@ -590,7 +592,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
     // z-score, [block flags], [histogram], per attempt: count, collect, recompute or values,
     // 4 scan kernels; [decide + 4 scan kernels]; fill
-    stats->kernel_launches = 1 + (prec == BNA_PREC_BF16X3 ? 1 : 0) +
+    stats->kernel_launches = 1 + (prec != BNA_PREC_FP32 ? 1 : 0) +
                              (density && k_dens > 0 ? 1 + passes * 3 + 5 : passes * 7) + 1;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
@@ -690,13 +692,14 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
   if (s) return s;
   cudaStream_t st = as_stream(stream);
   CorrArgs a{};
-  s = run_zscore(ctx, bold_dev, N, T, precision != BNA_PREC_FP32, a, st);
+  s = run_zscore(ctx, bold_dev, N, T, precision == BNA_PREC_BF16X3, a, st);
   if (s) return s;
   if (I < 0 || J < 0 || I >= a.nb || J >= a.nb)
     return fail(ctx, BNA_BAD_ARG, "tile (%d, %d) outside the %d-block grid", I, J, a.nb);
   switch (precision) {
     case BNA_PREC_FP32: CK(launch_corr_simt_dump(a, I, J, out_dev, st)); break;
-    case BNA_PREC_BF16X3: {
+    case BNA_PREC_BF16X3:
+    case BNA_PREC_TF32: {
       uint8_t* bb;
       ENSURE(S_BLOCKBAD, (size_t)a.nb, bb);
       CK(launch_block_bad(a.bad, a.nb, bb, st));
@@ -704,7 +707,8 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
       ENSURE(S_DUMPTILE, sizeof(int2), d);
       const int2 t = make_int2(I, J / 2);
       CK(cudaMemcpyAsync(d, &t, sizeof t, cudaMemcpyHostToDevice, st));
-      CK(launch_corr_tc(a, 2, d, 1, bb, out_dev, J % 2, 1, st));
+      CK(launch_corr_tc(a, 2, precision == BNA_PREC_BF16X3 ? 0 : 1, d, 1, bb, out_dev, J % 2, 1,
+                        st));
       CK(cudaStreamSynchronize(st));
       break;
     }

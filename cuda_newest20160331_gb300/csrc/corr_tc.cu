@@ -37,31 +37,45 @@ namespace bna {
 
 constexpr int TC_BM = 128;
 constexpr int TC_BN = 256;
-constexpr int TC_BK = 64;  // BF16 elements per K block (one 128-byte row)
-constexpr int TC_STAGES = 2;
-constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;                    // 16 KB
-constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;                    // 32 KB
-constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB
+// Operand forms.  Every K block is one 128-byte swizzled row per matrix row
+// (64 BF16 or 32 FP32 values) and one MMA K step covers 32 bytes of it.
+//   FORM_BF16X3: A hi, A lo, B hi, B lo per stage (96 KB), 2 stages, three
+//                kind::f16 MMAs (hi*hi, hi*lo, lo*hi) per K16 step;
+//   FORM_TF32:   A, B per stage (48 KB) from the FP32 z-scores, 4 stages, one
+//                kind::tf32 MMA per K8 step.
+constexpr int FORM_BF16X3 = 0, FORM_TF32 = 1;
+constexpr int TC_RING_BYTES = 192 * 1024;
+constexpr int TC_A_BYTES = TC_BM * 128;  // 16 KB: 128 rows x 128 bytes
+constexpr int TC_B_BYTES = TC_BN * 128;  // 32 KB
+template <int FORM>
+struct Form {
+  static constexpr int kParts = FORM == FORM_BF16X3 ? 2 : 1;           // hi/lo or one
+  static constexpr int kStageBytes = kParts * (TC_A_BYTES + TC_B_BYTES);
+  static constexpr int kStages = TC_RING_BYTES / kStageBytes;
+  static constexpr int kElemsPerBlock = FORM == FORM_BF16X3 ? 64 : 32;   // per 128-byte row
+  static constexpr int kElemsPerStep = kElemsPerBlock / 4;              // per MMA K step
+};
+constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_THREADS = 320;
 constexpr int TC_EPI_THREADS = 256;
 constexpr uint32_t TC_TMEM_COLS = 512;
 constexpr uint64_t kWaitNs = 4000000000ull;
 
 struct TcSmem {
-  uint64_t full[TC_STAGES], empty[TC_STAGES], tfull[2], tempty[2], done, hbar[2];
+  uint64_t full[TC_MAX_STAGES], empty[TC_MAX_STAGES], tfull[2], tempty[2], done, hbar[2];
   uint32_t tmem_base;
   volatile uint32_t abort;
   uint32_t colmask[2][128][4];
   unsigned int hist[kHistBins + 1];  // density histogram pass
 };
 
-constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_STAGES * TC_STAGE_BYTES + sizeof(TcSmem);
+constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_RING_BYTES + sizeof(TcSmem);
 
 struct TcArgs {
   CorrArgs a;
   const int2* tiles;        // (I, Jp): rows of block I x columns of blocks 2Jp, 2Jp+1
   int ntiles;
-  int nk16;                 // K16 steps = ceil(T / 16)
+  int nksteps;              // MMA K steps = ceil(T / elements per step)
   const uint8_t* blockbad;  // [nb]: block holds a voxel with NaN z
   float* dump;              // dump pass: 128 x 128 values of half `dump_half`
   int dump_half;
@@ -105,14 +119,18 @@ __device__ __forceinline__ bool half_sync(TcSmem& S, int h, uint32_t& phase) {
   return ok;
 }
 
-template <int PASS, bool ABS>
+// tm_hi / tm_lo: BF16 hi and lo parts (FORM_BF16X3); tm_hi: FP32 z (FORM_TF32).
+template <int PASS, bool ABS, int FORM>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
                    const __grid_constant__ CUtensorMap tm_lo, const TcArgs p) {
+  using F = Form<FORM>;
+  constexpr int TC_STAGES = F::kStages;
+  constexpr int TC_STAGE_BYTES = F::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  TcSmem& S = *reinterpret_cast<TcSmem*>(smem + (size_t)TC_STAGES * TC_STAGE_BYTES);
+  TcSmem& S = *reinterpret_cast<TcSmem*>(smem + (size_t)TC_RING_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const CorrArgs& a = p.a;
 
@@ -138,13 +156,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   if (warp == 0 && lane == 0) {
     ptx::prefetch_tensormap(&tm_hi);
-    ptx::prefetch_tensormap(&tm_lo);
+    if (FORM == FORM_BF16X3) ptx::prefetch_tensormap(&tm_lo);
   }
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = S.tmem_base;
-  const int nkb = (p.nk16 + 3) / 4;
+  const int nkb = (p.nksteps + 3) / 4;
 
   if (warp == 0) {
     // ------------------------------------------------------------ TMA producer
@@ -166,15 +184,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t full = ptx::smem_u32(&S.full[s]);
           const uint32_t base = ptx::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
           ptx::mbar_arrive_expect_tx(full, TC_STAGE_BYTES);
-          const int k0 = kb * TC_BK;
+          const int k0 = kb * F::kElemsPerBlock;
           const int ra = tile.x * TC_BM, rb = tile.y * TC_BN;
+          // stage layout: A parts, then B parts (B = two 128-row boxes each)
           ptx::tma_load_2d(base, &tm_hi, full, k0, ra);
-          ptx::tma_load_2d(base + TC_A_BYTES, &tm_lo, full, k0, ra);
-          ptx::tma_load_2d(base + 2 * TC_A_BYTES, &tm_hi, full, k0, rb);
-          ptx::tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES / 2, &tm_hi, full, k0, rb + 128);
-          ptx::tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES, &tm_lo, full, k0, rb);
-          ptx::tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES + TC_B_BYTES / 2, &tm_lo, full,
-                           k0, rb + 128);
+          if (FORM == FORM_BF16X3) ptx::tma_load_2d(base + TC_A_BYTES, &tm_lo, full, k0, ra);
+          const uint32_t bb = base + F::kParts * TC_A_BYTES;
+          ptx::tma_load_2d(bb, &tm_hi, full, k0, rb);
+          ptx::tma_load_2d(bb + TC_B_BYTES / 2, &tm_hi, full, k0, rb + 128);
+          if (FORM == FORM_BF16X3) {
+            ptx::tma_load_2d(bb + TC_B_BYTES, &tm_lo, full, k0, rb);
+            ptx::tma_load_2d(bb + TC_B_BYTES + TC_B_BYTES / 2, &tm_lo, full, k0, rb + 128);
+          }
           last_round[s] = (int)round;
         }
       }
@@ -186,7 +207,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = ptx::make_idesc(1, 1, TC_BM, TC_BN);
+      // BF16 x BF16 (kind::f16, format 1) or TF32 x TF32 (kind::tf32, format 2)
+      constexpr uint32_t idesc = FORM == FORM_BF16X3 ? ptx::make_idesc(1, 1, TC_BM, TC_BN)
+                                                     : ptx::make_idesc(2, 2, TC_BM, TC_BN);
       uint32_t f = 0;
       int m = 0;
       bool ok = true;
@@ -208,15 +231,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           ptx::tc_fence_after();
           const uint32_t base = ptx::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
-          const int steps = min(4, p.nk16 - kb * 4);
-          for (int kk = 0; kk < steps; ++kk) {
-            const uint64_t ahi = ptx::sw128_desc(base + kk * 32);
-            const uint64_t alo = ptx::sw128_desc(base + TC_A_BYTES + kk * 32);
-            const uint64_t bhi = ptx::sw128_desc(base + 2 * TC_A_BYTES + kk * 32);
-            const uint64_t blo = ptx::sw128_desc(base + 2 * TC_A_BYTES + TC_B_BYTES + kk * 32);
-            ptx::mma_bf16(d, ahi, bhi, idesc, (kb | kk) != 0);
-            ptx::mma_bf16(d, ahi, blo, idesc, 1);
-            ptx::mma_bf16(d, alo, bhi, idesc, 1);
+          const int steps = min(4, p.nksteps - kb * 4);
+          if (FORM == FORM_BF16X3) {
+            for (int kk = 0; kk < steps; ++kk) {
+              const uint64_t ahi = ptx::sw128_desc(base + kk * 32);
+              const uint64_t alo = ptx::sw128_desc(base + TC_A_BYTES + kk * 32);
+              const uint64_t bhi = ptx::sw128_desc(base + 2 * TC_A_BYTES + kk * 32);
+              const uint64_t blo = ptx::sw128_desc(base + 2 * TC_A_BYTES + TC_B_BYTES + kk * 32);
+              ptx::mma_bf16(d, ahi, bhi, idesc, (kb | kk) != 0);
+              ptx::mma_bf16(d, ahi, blo, idesc, 1);
+              ptx::mma_bf16(d, alo, bhi, idesc, 1);
+            }
+          } else {
+            for (int kk = 0; kk < steps; ++kk) {
+              const uint64_t ad = ptx::sw128_desc(base + kk * 32);
+              const uint64_t bd = ptx::sw128_desc(base + TC_A_BYTES + kk * 32);
+              ptx::mma_tf32(d, ad, bd, idesc, (kb | kk) != 0);
+            }
           }
           ptx::mma_commit(ptx::smem_u32(&S.empty[s]));
         }
@@ -456,16 +487,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D BF16 map over [rows][ld] with a 64 x 128 box, 128-byte swizzle.
-bool make_map(CUtensorMap* m, const void* base, int ld, int rows) {
+// 2-D map over [rows][ld] elements (BF16 or FP32) with a 128-byte x 128-row
+// box, 128-byte swizzle (the K-major layout the MMA descriptors expect).
+bool make_map(CUtensorMap* m, const void* base, int ld, int rows, bool fp32) {
   auto fn = encode_fn();
   if (!fn) return false;
+  const int esz = fp32 ? 4 : 2;
   cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  cuuint32_t box[2] = {TC_BK, TC_BM};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * esz};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), TC_BM};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
-                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+  CUresult r = fn(m, fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -488,28 +522,45 @@ cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cuda
 }
 
 // pass 0 count (+ edge lists), 2 dump (tiles must then hold the one tile to dump),
-// 3 density histogram
-cudaError_t launch_corr_tc(const CorrArgs& a, int pass, const int2* tiles, int ntiles,
+// 3 density histogram; form FORM_BF16X3 or FORM_TF32
+cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st) {
-  if (!a.zhi || !a.zlo || a.ldb % TC_BK != 0) return cudaErrorInvalidValue;
   CUtensorMap mh, ml;
-  if (!make_map(&mh, a.zhi, a.ldb, a.n_pad) || !make_map(&ml, a.zlo, a.ldb, a.n_pad))
-    return cudaErrorInvalidValue;
+  if (form == FORM_BF16X3) {
+    if (!a.zhi || !a.zlo || a.ldb % 64 != 0) return cudaErrorInvalidValue;
+    if (!make_map(&mh, a.zhi, a.ldb, a.n_pad, false) ||
+        !make_map(&ml, a.zlo, a.ldb, a.n_pad, false))
+      return cudaErrorInvalidValue;
+  } else {
+    if (!a.z || a.ldz % 32 != 0) return cudaErrorInvalidValue;
+    if (!make_map(&mh, a.z, a.ldz, a.n_pad, true)) return cudaErrorInvalidValue;
+    ml = mh;
+  }
   TcArgs p;
   p.a = a;
   p.tiles = tiles;
   p.ntiles = ntiles;
-  p.nk16 = (a.T + 15) / 16;
+  const int per_step = form == FORM_BF16X3 ? Form<FORM_BF16X3>::kElemsPerStep
+                                           : Form<FORM_TF32>::kElemsPerStep;
+  p.nksteps = (a.T + per_step - 1) / per_step;
   p.blockbad = blockbad;
   p.dump = dump;
   p.dump_half = dump_half;
   const int g = grid < ntiles ? grid : ntiles;
   if (g <= 0) return cudaSuccess;
   const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
-  auto kern = pass == 0   ? (absm ? corr_tc_kernel<0, true> : corr_tc_kernel<0, false>)
-              : pass == 3 ? corr_tc_kernel<3, false>
-                          : corr_tc_kernel<2, false>;
+  void (*kern)(CUtensorMap, CUtensorMap, TcArgs);
+  if (form == FORM_BF16X3)
+    kern = pass == 0   ? (absm ? corr_tc_kernel<0, true, FORM_BF16X3>
+                               : corr_tc_kernel<0, false, FORM_BF16X3>)
+           : pass == 3 ? corr_tc_kernel<3, false, FORM_BF16X3>
+                       : corr_tc_kernel<2, false, FORM_BF16X3>;
+  else
+    kern = pass == 0   ? (absm ? corr_tc_kernel<0, true, FORM_TF32>
+                               : corr_tc_kernel<0, false, FORM_TF32>)
+           : pass == 3 ? corr_tc_kernel<3, false, FORM_TF32>
+                       : corr_tc_kernel<2, false, FORM_TF32>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)TC_SMEM_BYTES);
   if (e != cudaSuccess) return e;

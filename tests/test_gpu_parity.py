@@ -14,7 +14,7 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-PRECISIONS = ["fp32", "bf16x3"]
+PRECISIONS = ["fp32", "bf16x3", "tf32"]
 
 
 def dev(x):
