@@ -158,11 +158,16 @@ class ClockSampler:
 
 
 def load_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` from one ncu capture
+    (profiles/traffic.txt: `kernel:workload bytes` lines), or None."""
     try:
-        d = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        return d.get(f"{kernel}:{workload}")
-    except Exception:
-        return None
+        for line in open(os.path.join(ROOT, "profiles", "traffic.txt")):
+            f = line.split("#")[0].split()
+            if len(f) == 2 and f[0] == f"{kernel}:{workload}":
+                return int(f[1])
+    except OSError:
+        pass
+    return None
 
 
 def run_reference(args):
