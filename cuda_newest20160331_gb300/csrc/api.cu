@@ -28,12 +28,12 @@ cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* r
                             long long* pre, long long* bsum, long long* total, int32_t* row_ptr,
                             uint32_t* err, cudaStream_t stream);
 size_t ec_state_bytes();
-cudaError_t launch_ec_init(int n, double* u, double* parts, void* st, int grid, int max_iter,
-                           cudaStream_t stream);
+cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
+                           int max_iter, cudaStream_t stream);
 cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const float* val,
-                           const double* vald, long long nnz_used, const double* u, double* un,
-                           double* parts, void* st, int grid, int max_iter, double eps,
-                           cudaStream_t stream);
+                           const double* vald, long long nnz_used, const double* u,
+                           const float2* uf, double* un, float2* unf, double* parts, void* st,
+                           int grid, int max_iter, double eps, cudaStream_t stream);
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done);
 void tc_tile_list(int nb, std::vector<int2>& out);
@@ -41,7 +41,8 @@ cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cuda
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st);
-cudaError_t launch_csr_fill(const CorrArgs& a, int sms, cudaStream_t stream);
+cudaError_t launch_csr_fill(const CorrArgs& a, int sms, int* dense_list, unsigned int* dense_count,
+                            cudaStream_t stream);
 cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream);
 cudaError_t launch_cand_values(const CorrArgs& a, float* vals, int grid, cudaStream_t stream);
 }  // namespace bna
@@ -53,14 +54,15 @@ namespace {
 enum Slot {
   S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
-  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL, S_COUNT
+  S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL,
+  S_DENSE, S_COUNT
 };
 
 // Small device block the host reads once per pass.
 struct DevStatus {
   unsigned long long cand_count;
   uint32_t err;
-  uint32_t pad;
+  uint32_t dense;  // dense sub-tiles queued by the fill pass
   unsigned long long stats[4];
   long long total;
   unsigned long long epool;  // edge-list entries handed out by the count pass
@@ -473,7 +475,8 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     if (s) return s;
     ++passes;
     CK(cudaEventRecord(ctx->ev[2], st));
-    CK(launch_collect_candidates(a, ctx->sms, st));
+    // the tensor-core count pass lists its candidates itself
+    if (prec == BNA_PREC_FP32) CK(launch_collect_candidates(a, ctx->sms, st));
     if (density && k_dens > 0) {
       CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
     } else {
@@ -508,17 +511,27 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     // larger pair is an edge; of the pairs equal to tau*, the first ones in
     // row-major (i < j) order are kept up to k edges.  Every pair that can be
     // tau* or a tie is a candidate with its exact value here.
-    const long long n = (long long)hs->cand_count;
+    // candidate slots (the tensor-core pass leaves unused slots marked kCandNone)
+    const long long slots = std::min<long long>((long long)hs->cand_count, a.cand_cap);
     const long long definite = (long long)hs->stats[2];
+    std::vector<float> v(slots);
+    std::vector<uint2> keys(slots);
+    CK(cudaMemcpyAsync(v.data(), cvals, slots * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(keys.data(), a.cand, slots * sizeof(uint2), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    long long n = 0;
+    for (long long c = 0; c < slots; ++c)
+      if (keys[c].x != kCandNone) {
+        v[n] = v[c];
+        keys[n] = keys[c];
+        ++n;
+      }
+    v.resize(n);
+    keys.resize(n);
     const long long need = k_dens - definite;
     if (need < 1 || need > n)
       return fail(ctx, BNA_INTERNAL, "density window missed the k-th value (k %lld, definite %lld, "
                   "candidates %lld)", k_dens, definite, n);
-    std::vector<float> v(n);
-    std::vector<uint2> keys(n);
-    CK(cudaMemcpyAsync(v.data(), cvals, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(keys.data(), a.cand, n * sizeof(uint2), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
     std::vector<float> w(v);
     std::nth_element(w.begin(), w.begin() + (need - 1), w.end(), std::greater<float>());
     const float tau_star = w[need - 1];
@@ -559,7 +572,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   if (hs->err & ERR_NNZ_INT32 || hs->total > 0x7fffffffLL)
     return fail(ctx, BNA_NNZ_OVERFLOW_INT32, "nnz %lld exceeds int32", hs->total);
   const long long nnz = hs->total;
-  const unsigned long long cand_count = hs->cand_count;
+  const unsigned long long cand_count = hs->stats[3];  // candidates (not slots)
   const unsigned long long band_edges = hs->stats[0], band_1e6 = hs->stats[1];
   int32_t* col;
   ENSURE(S_COL, (size_t)std::max(nnz, 1LL) * 4, col);
@@ -569,7 +582,9 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   a.col_idx = col;
   a.val = val;
   a.nnz = nnz;
-  CK(launch_csr_fill(a, ctx->sms, st));
+  int* dense_list;
+  ENSURE(S_DENSE, (size_t)nst * sizeof(int), dense_list);
+  CK(launch_csr_fill(a, ctx->sms, dense_list, &ds->dense, st));
   CK(cudaEventRecord(ctx->ev[5], st));
   CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -590,10 +605,12 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     stats->band_1e6 = (int64_t)band_1e6;
     stats->ties_dropped = ties_dropped;
     stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
-    // z-score, [block flags], [histogram], per attempt: count, collect, recompute or values,
-    // 4 scan kernels; [decide + 4 scan kernels]; fill
-    stats->kernel_launches = 1 + (prec != BNA_PREC_FP32 ? 1 : 0) +
-                             (density && k_dens > 0 ? 1 + passes * 3 + 5 : passes * 7) + 1;
+    // z-score, [block flags], [histogram], per attempt: count, [collect (FP32 form)],
+    // recompute or values, 4 scan kernels; [decide + 4 scan kernels]; fill (2 kernels)
+    const int collect = prec == BNA_PREC_FP32 ? 1 : 0;
+    stats->kernel_launches =
+        1 + (prec != BNA_PREC_FP32 ? 1 : 0) +
+        (density && k_dens > 0 ? 1 + passes * (2 + collect) + 5 : passes * (6 + collect)) + 2;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);
@@ -725,12 +742,14 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
   const long long nnz_used = 2 * (nnz / 2);  // weighted-net.cu:61
   double *u, *parts;
   void* state;
-  ENSURE(S_EC_U, (size_t)2 * n * sizeof(double), u);
+  // two double iterates, then their two (hi, lo) float copies
+  ENSURE(S_EC_U, (size_t)2 * n * (sizeof(double) + sizeof(float2)), u);
+  float2* uf = reinterpret_cast<float2*>(u + (size_t)2 * n);
   const int grid = std::max(1, ctx->sms * 4);
   ENSURE(S_EC_PARTS, (size_t)grid * 3 * sizeof(double), parts);
   ENSURE(S_EC_STATE, ec_state_bytes(), state);
   CK(cudaMemsetAsync(state, 0, ec_state_bytes(), st));
-  CK(launch_ec_init(n, u, parts, state, grid, max_iter, st));
+  CK(launch_ec_init(n, u, uf, parts, state, grid, max_iter, st));
   EcGraph& g = ctx->ecg;
   const void* key[6] = {rp, ci, val, vald, u, state};
   bool same = g.exec && g.n == n && g.grid == grid && g.max_iter == max_iter && g.eps == eps &&
@@ -743,10 +762,9 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < kGraphIters; ++it) {
-      const double* ucur = u + (size_t)(it & 1) * n;
-      double* unext = u + (size_t)((it + 1) & 1) * n;
-      launch_ec_iter(n, rp, ci, val, vald, nnz_used, ucur, unext, parts, state, grid, max_iter,
-                     eps, cap);
+      const size_t cur = (size_t)(it & 1) * n, nxt = (size_t)((it + 1) & 1) * n;
+      launch_ec_iter(n, rp, ci, val, vald, nnz_used, u + cur, uf + cur, u + nxt, uf + nxt, parts,
+                     state, grid, max_iter, eps, cap);
     }
     cudaGraph_t graph;
     cudaError_t ce = cudaStreamEndCapture(cap, &graph);

@@ -27,6 +27,11 @@ enum : uint32_t {
 // Edge-list pool: the count pass allocates it in chunks of kElistChunk
 // entries per warp (one atomic per chunk) and never writes past ecap.
 constexpr long long kElistChunk = 16384;
+// Candidate list: the tensor-core count pass writes its near-threshold pairs
+// itself, in warp-private chunks of kCandChunk slots; slots a warp leaves
+// unused hold (kCandNone, kCandNone) and are skipped by the consumers.
+constexpr long long kCandChunk = 256;
+constexpr uint32_t kCandNone = 0xFFFFFFFFu;
 
 // Density mode: histogram of the approximate r over [-1, 1) in kHistBins
 // bins (bin = floor((r + 1) * kHistBins / 2)); entry kHistBins counts the

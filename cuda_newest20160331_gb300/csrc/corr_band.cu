@@ -109,6 +109,7 @@ __global__ void cand_values_kernel(CorrArgs a, float* vals) {
   for (long long c = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); c < n;
        c += nwarps) {
     const uint2 p = a.cand[c];
+    if (p.x == kCandNone) continue;  // unused slot of a count-pass chunk
     const float r = exact_r_warp(a, (int)p.x, (int)p.y, lane);
     if (lane == 0) vals[c] = r;
   }
@@ -125,6 +126,7 @@ __global__ void recompute_kernel(CorrArgs a) {
   for (long long c = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); c < n;
        c += nwarps) {
     const uint2 p = a.cand[c];
+    if (p.x == kCandNone) continue;  // unused slot of a count-pass chunk
     const int i = (int)p.x, j = (int)p.y;
     const float r = a.cand_val ? a.cand_val[c] : exact_r_warp(a, i, j, lane);
     if (lane != 0) continue;
@@ -157,7 +159,9 @@ __global__ void recompute_kernel(CorrArgs a) {
 }
 
 // Gather the candidates flagged in the sub-tiles' edge lists into the
-// candidate list (warp per sub-tile, one atomic per warp and round).
+// candidate list (warp per sub-tile, one atomic per warp and round).  Used
+// after the plain FP32 count pass; the tensor-core pass lists its candidates
+// itself.
 __global__ void collect_candidates_kernel(CorrArgs a, long long nst) {
   const int wpb = blockDim.x >> 5;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -205,6 +209,7 @@ __global__ void collect_candidates_kernel(CorrArgs a, long long nst) {
       if (lane == 0 && nvalid - __popc(bal) > 0)
         atomicAdd(&a.stats[2], (unsigned long long)(nvalid - __popc(bal)));
       if (!bal) continue;
+      if (lane == 0) atomicAdd(&a.stats[3], (unsigned long long)__popc(bal));
       unsigned long long base = 0;
       if (lane == 0) base = atomicAdd(a.cand_count, (unsigned long long)__popc(bal));
       base = __shfl_sync(0xffffffffu, base, 0);

@@ -20,8 +20,9 @@
 //               in the sub-tile's compact edge list (warp-private bump
 //               allocator), candidates only flagged; row counts from register
 //               bitmasks, column counts from a 32 x 32 bit transpose across the
-//               warp.  The fill pass (csr_fill.cu) places the listed edges; the
-//               GEMM runs once.
+//               warp; the rare candidates also go to the candidate list
+//               (warp-private chunks).  The fill pass (csr_fill.cu) places the
+//               listed edges; the GEMM runs once.
 //
 // Every wait is bounded (4 s of wall time); on expiry the kernel raises
 // ERR_TIMEOUT, drains its own copies and MMAs, frees TMEM and returns.
@@ -278,6 +279,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint32_t hphase = 0;
     long long wcur = 0, wend = 0;  // this warp's current edge-list chunk [wcur, wend)
     bool wok = true;
+    long long ccur = 0, cend = 0;  // this warp's current candidate chunk [ccur, cend)
+    unsigned long long n_def = 0, n_cand = 0;  // this lane's definite edges and candidates
     int m = 0;
     // tile coordinates and NaN-block flags run one tile ahead
     int2 nxt = make_int2(0, 0);
@@ -335,6 +338,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const bool slow = active && (bad_i || bad_j);
       const bool rowbad = slow && a.bad[gi];
       int rowcount = 0;
+      uint32_t cmk4[4] = {0u, 0u, 0u, 0u};
       if (active) {
         uint32_t vb[2][32];
         ptx::tmem_ld32_async(taddr, vb[0]);
@@ -425,14 +429,53 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (wok) *dst++ = make_uint2(elist_key(il, c * 32 + k, cf), val);
           }
           rowcount += __popc(eb);
+          n_def += __popc(eb);
           S.colmask[h][c * 32 + lane][q] = transpose32(eb, lane);
           wcur += total;
+          cmk4[c] = it & ~eb;  // candidates of this chunk (listed after the tile)
         }
       }
       // the accumulator has been read: hand it back to the MMA warp
       ptx::tc_fence_before();
       ptx::mbar_arrive(ptx::smem_u32(&S.tempty[acc]));
       if (PASS == 2 || PASS == 3) continue;
+      // candidates (rare): warp prefix scan into the warp's candidate chunk
+      if (active && __any_sync(0xffffffffu, (cmk4[0] | cmk4[1] | cmk4[2] | cmk4[3]) != 0u)) {
+        const int nc = __popc(cmk4[0]) + __popc(cmk4[1]) + __popc(cmk4[2]) + __popc(cmk4[3]);
+        int cinc = nc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, cinc, o);
+          if (lane >= o) cinc += y;
+        }
+        const int ctot = __shfl_sync(0xffffffffu, cinc, 31);
+        if (ccur + ctot > cend) {
+          // seal the rest of the chunk, take enough new chunks for this batch
+          for (long long sl = ccur + lane; sl < cend && sl < a.cand_cap; sl += 32)
+            a.cand[sl] = make_uint2(kCandNone, kCandNone);
+          const long long need = (ctot + kCandChunk - 1) / kCandChunk * kCandChunk;
+          unsigned long long cb = 0;
+          if (lane == 0) cb = atomicAdd(a.cand_count, (unsigned long long)need);
+          ccur = (long long)__shfl_sync(0xffffffffu, cb, 0);
+          cend = ccur + need;
+        }
+        long long slot = ccur + (cinc - nc);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          uint32_t w3 = cmk4[c];
+          while (w3) {
+            const int k = __ffs(w3) - 1;
+            w3 &= w3 - 1;
+            if (slot < a.cand_cap)
+              a.cand[slot] = make_uint2((unsigned)gi, (unsigned)(J * 128 + c * 32 + k));
+            else
+              atomicOr(a.err, ERR_BAND_OVERFLOW);
+            ++slot;
+          }
+        }
+        ccur += ctot;
+        n_cand += nc;
+      }
       if (active && lane == 0)
         a.etab[subtile_index(I, J, a.nb) * 4 + q] =
             wok ? make_longlong2(start, wcur - start) : make_longlong2(0, 0);
@@ -451,6 +494,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           a.seg[(size_t)I * a.n_pad + J * 128 + il] = cc;
         }
       }
+    }
+    if (PASS == 0) {
+      for (long long sl = ccur + lane; sl < cend && sl < a.cand_cap; sl += 32)
+        a.cand[sl] = make_uint2(kCandNone, kCandNone);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        n_def += __shfl_xor_sync(0xffffffffu, n_def, o);
+        n_cand += __shfl_xor_sync(0xffffffffu, n_cand, o);
+      }
+      if (lane == 0 && n_def) atomicAdd(&a.stats[2], n_def);
+      if (lane == 0 && n_cand) atomicAdd(&a.stats[3], n_cand);
     }
   }
   ptx::tc_fence_before();

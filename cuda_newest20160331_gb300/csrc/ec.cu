@@ -5,12 +5,21 @@
 // u = A u (cusparseDcsrmv); e1 = ||u - u0||; e2 = ||u + u0|| with three
 // blocking host reductions.  Here one kernel does a whole iteration:
 //   lambda = sqrt(sum u^2)   (sum produced by the previous iteration)
-//   y_i    = (sum_k val_k * u[col_k]) / lambda      (FP64, val read as float)
+//   y_i    = (sum_k val_k * u[col_k]) / lambda
 //   partial sums of y^2, (y - u)^2, (y + u)^2 per block
 // and the last block to finish reduces the partials in a fixed order, so the
 // iteration is deterministic.  A device flag stops later launches once
 // e1 <= eps or e2 <= eps (no host round trip per iteration); the host replays
 // a captured CUDA graph of 32 iterations and reads the flag between graphs.
+//
+// The SpMV runs in float-float ("double-float") arithmetic instead of FP64,
+// whose rate on this GPU is ~1/70 of FP32: the iterate is kept twice, as
+// double (norms, convergence test, output) and as a (hi, lo) float pair for
+// the gather; each product val * (hi + lo) is split exactly with an FMA
+// (TwoProduct, Dekker 1971 / Ogita-Rump-Oishi 2005) and summed with Knuth's
+// TwoSum, so a row sum carries about 48 significant bits (relative error
+// ~2^-38 for rows of ~1000 entries), far inside the 1e-5 tolerance against
+// the FP64 reference.  Row results, norms and the stop test stay in FP64.
 #include <cmath>
 
 #include "common.cuh"
@@ -73,13 +82,28 @@ __device__ __forceinline__ bool last_block_arrives(EcState* st) {
   return last;
 }
 
-__global__ __launch_bounds__(kEcThreads) void ec_init_kernel(int n, double* u, double* parts,
-                                                             EcState* st, int max_iter) {
+// (hi, lo) float pair of a double: hi = RN(x), lo = RN(x - hi).
+__device__ __forceinline__ float2 split_df(double x) {
+  const float hi = __double2float_rn(x);
+  return make_float2(hi, __double2float_rn(x - (double)hi));
+}
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__global__ __launch_bounds__(kEcThreads) void ec_init_kernel(int n, double* u, float2* uf,
+                                                             double* parts, EcState* st,
+                                                             int max_iter) {
   __shared__ double ws[kEcThreads / 32];
   double s = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double v = (double)i;  // init_AD, weighted-net.cu:38-43
     u[i] = v;
+    uf[i] = split_df(v);
     s += v * v;
   }
   s = warp_sum(s);
@@ -107,33 +131,88 @@ __global__ __launch_bounds__(kEcThreads) void ec_init_kernel(int n, double* u, d
   }
 }
 
+// One nonzero: (sh, sl) += v * (x.hi + x.lo), v given as (vh, vl) (vl = 0 for float values).
+template <int VK>
+__device__ __forceinline__ void df_accum(float& sh, float& sl, float vh, float vl, float2 x) {
+  float p, pe;
+  if (VK == 0) {  // binary graph: v = 1
+    p = x.x;
+    pe = x.y;
+  } else {
+    p = __fmul_rn(vh, x.x);
+    pe = __fmaf_rn(vh, x.x, -p);  // exact low part of vh * x.hi
+    pe = __fmaf_rn(vh, x.y, pe);
+    if (VK == 2) pe = __fmaf_rn(vl, x.x, pe);
+  }
+  float s, e;
+  two_sum(sh, p, s, e);
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(e, pe));
+}
+
+// VK: 0 binary (val NULL), 1 float values, 2 double values (split into a float pair).
+template <int VK>
 __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
     int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
     const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
-    const double* __restrict__ u,
-    double* __restrict__ un, double* parts, EcState* st, int max_iter, double eps) {
+    const double* __restrict__ u, const float2* __restrict__ uf, double* __restrict__ un,
+    float2* __restrict__ unf, double* parts, EcState* st, int max_iter, double eps) {
   if (st->done || st->iter >= max_iter) return;
   const double lam = sqrt(st->lam2);
   const double inv = 1.0 / lam;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = gridDim.x * (kEcThreads / 32);
   double a0 = 0, a1 = 0, a2 = 0;
+  auto vpair = [&](long long k, float& vh, float& vl) {
+    vh = 1.0f;
+    vl = 0.0f;
+    if (VK == 1) vh = __ldg(val + k);
+    if (VK == 2) {
+      const float2 d = split_df(__ldg(vald + k));
+      vh = d.x;
+      vl = d.y;
+    }
+  };
   for (int row = blockIdx.x * (kEcThreads / 32) + warp; row < n; row += nwarps) {
     long long b = rp[row], e = rp[row + 1];
     if (e > nnz_used) e = nnz_used;
-    double s = 0;
-    if (val) {
-      for (long long k = b + lane; k < e; k += 32) s += (double)__ldg(val + k) * u[__ldg(ci + k)];
-    } else if (vald) {
-      for (long long k = b + lane; k < e; k += 32) s += __ldg(vald + k) * u[__ldg(ci + k)];
-    } else {
-      for (long long k = b + lane; k < e; k += 32) s += u[__ldg(ci + k)];
+    float sh = 0.0f, sl = 0.0f;
+    long long k = b + lane;
+    // four entries per lane in flight
+    for (; k + 96 < e; k += 128) {
+      int c[4];
+      float vh[4], vl[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        c[m] = __ldg(ci + k + 32 * m);
+        vpair(k + 32 * m, vh[m], vl[m]);
+      }
+      float2 x[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) x[m] = uf[c[m]];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) df_accum<VK>(sh, sl, vh[m], vl[m], x[m]);
     }
-    s = warp_sum(s);
+    for (; k < e; k += 32) {
+      float vh, vl;
+      vpair(k, vh, vl);
+      df_accum<VK>(sh, sl, vh, vl, uf[__ldg(ci + k)]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+      float s2, e2;
+      two_sum(sh, oh, s2, e2);
+      sh = s2;
+      sl = __fadd_rn(sl, __fadd_rn(ol, e2));
+    }
     if (lane == 0) {
+      const double s = (double)sh + (double)sl;
       const double y = s * inv;
       const double old = u[row];
       un[row] = y;
+      unf[row] = split_df(y);
       a0 += y * y;
       const double d = y - old, p = y + old;
       a1 += d * d;
@@ -175,18 +254,25 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
 
 size_t ec_state_bytes() { return sizeof(EcState); }
 
-cudaError_t launch_ec_init(int n, double* u, double* parts, void* st, int grid, int max_iter,
-                           cudaStream_t stream) {
-  ec_init_kernel<<<grid, kEcThreads, 0, stream>>>(n, u, parts, (EcState*)st, max_iter);
+cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
+                           int max_iter, cudaStream_t stream) {
+  ec_init_kernel<<<grid, kEcThreads, 0, stream>>>(n, u, uf, parts, (EcState*)st, max_iter);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const float* val,
-                           const double* vald, long long nnz_used, const double* u, double* un,
-                           double* parts, void* st, int grid, int max_iter, double eps,
-                           cudaStream_t stream) {
-  ec_iter_kernel<<<grid, kEcThreads, 0, stream>>>(n, rp, ci, val, vald, nnz_used, u, un, parts,
-                                                  (EcState*)st, max_iter, eps);
+                           const double* vald, long long nnz_used, const double* u,
+                           const float2* uf, double* un, float2* unf, double* parts, void* st,
+                           int grid, int max_iter, double eps, cudaStream_t stream) {
+  if (val)
+    ec_iter_kernel<1><<<grid, kEcThreads, 0, stream>>>(n, rp, ci, val, vald, nnz_used, u, uf, un,
+                                                       unf, parts, (EcState*)st, max_iter, eps);
+  else if (vald)
+    ec_iter_kernel<2><<<grid, kEcThreads, 0, stream>>>(n, rp, ci, val, vald, nnz_used, u, uf, un,
+                                                       unf, parts, (EcState*)st, max_iter, eps);
+  else
+    ec_iter_kernel<0><<<grid, kEcThreads, 0, stream>>>(n, rp, ci, val, vald, nnz_used, u, uf, un,
+                                                       unf, parts, (EcState*)st, max_iter, eps);
   return cudaGetLastError();
 }
 

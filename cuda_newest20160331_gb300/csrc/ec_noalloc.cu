@@ -13,7 +13,7 @@
 // Limits and sharing rules:
 //   - N <= kNoAllocMaxN (262,144 vertices); larger graphs get
 //     BNA_SCRATCH_LIMIT.  The array holds 2 * kNoAllocMaxN doubles plus block
-//     partials and state (about 4 MB); every GPU that loads the library keeps
+//     partials and state (about 8 MB); every GPU that loads the library keeps
 //     it until the process exits.
 //   - Every call shares the array.  Calls that overlap on a GPU (two host
 //     threads, or two streams running at once) race on it; serialise them.
@@ -27,12 +27,12 @@
 
 namespace bna {
 size_t ec_state_bytes();
-cudaError_t launch_ec_init(int n, double* u, double* parts, void* st, int grid, int max_iter,
-                           cudaStream_t stream);
+cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
+                           int max_iter, cudaStream_t stream);
 cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const float* val,
-                           const double* vald, long long nnz_used, const double* u, double* un,
-                           double* parts, void* st, int grid, int max_iter, double eps,
-                           cudaStream_t stream);
+                           const double* vald, long long nnz_used, const double* u,
+                           const float2* uf, double* un, float2* unf, double* parts, void* st,
+                           int grid, int max_iter, double eps, cudaStream_t stream);
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done);
 }  // namespace bna
@@ -42,8 +42,9 @@ namespace {
 constexpr int kNoAllocMaxN = 1 << 18;
 constexpr int kNoAllocMaxGrid = 1024;
 constexpr size_t kStateDoubles = 16;  // >= sizeof(EcState) / 8
+// two double iterates, their two (hi, lo) float copies, block partials, state
 constexpr size_t kScratchDoubles =
-    2 * (size_t)kNoAllocMaxN + 3 * (size_t)kNoAllocMaxGrid + kStateDoubles;
+    4 * (size_t)kNoAllocMaxN + 3 * (size_t)kNoAllocMaxGrid + kStateDoubles;
 
 // The scratch.  Host code must not take its address directly (that is a host
 // stand-in); the device address comes from cudaGetSymbolAddress below.
@@ -99,15 +100,16 @@ extern "C" int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, doub
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int n = csr_dev->n;
   const int grid = std::max(1, std::min(sms * 4, kNoAllocMaxGrid));
-  double* u = scratch;                                   // 2 * kNoAllocMaxN
-  double* parts = scratch + 2 * (size_t)kNoAllocMaxN;   // 3 * kNoAllocMaxGrid
+  double* u = scratch;                                                   // 2 * kNoAllocMaxN
+  float2* uf = reinterpret_cast<float2*>(scratch + 2 * (size_t)kNoAllocMaxN);  // 2 * kNoAllocMaxN
+  double* parts = scratch + 4 * (size_t)kNoAllocMaxN;                   // 3 * kNoAllocMaxGrid
   void* state = parts + 3 * (size_t)kNoAllocMaxGrid;    // kStateDoubles
   const long long nnz_used = 2 * (csr_dev->nnz / 2);
   // The array keeps the previous call's contents: the state block (with the
   // last-block counter) must start at zero; u and the partials are fully
   // written by the init kernel before they are read.
   cudaError_t e = cudaMemsetAsync(state, 0, ec_state_bytes(), st);
-  if (e == cudaSuccess) e = launch_ec_init(n, u, parts, state, grid, max_iter, st);
+  if (e == cudaSuccess) e = launch_ec_init(n, u, uf, parts, state, grid, max_iter, st);
   if (e != cudaSuccess) return BNA_CUDA_ERROR;
   alignas(16) unsigned char host_state[kStateDoubles * sizeof(double)];
   double lam2 = 0, lam = 0, e1 = 0, e2 = 0;
@@ -116,10 +118,10 @@ extern "C" int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, doub
   for (int launched = 0; launched < max_iter && !done; launched += chunk) {
     for (int k = 0; k < chunk; ++k) {
       const int gi = launched + k;
-      const double* ucur = u + (size_t)(gi & 1) * n;
-      double* unext = u + (size_t)((gi + 1) & 1) * n;
+      const size_t cur = (size_t)(gi & 1) * n, nxt = (size_t)((gi + 1) & 1) * n;
       e = launch_ec_iter(n, csr_dev->row_ptr, csr_dev->col_idx, csr_dev->val, nullptr, nnz_used,
-                         ucur, unext, parts, state, grid, max_iter, eps, st);
+                         u + cur, uf + cur, u + nxt, uf + nxt, parts, state, grid, max_iter, eps,
+                         st);
       if (e != cudaSuccess) return BNA_CUDA_ERROR;
     }
     // pageable stack buffer: the copy is synchronous with respect to the host

@@ -22,20 +22,21 @@
 //     division; the float rounding itself is done on the bits.
 //   The centred sum of squares keeps its sequential double adds.
 //
-// Layout: a block owns 32 voxels; one warp runs their sums, one thread per
-// voxel.  Short series (T <= 360) are read once, coalesced, into shared
-// memory; longer ones are read coalesced from global memory in each pass.
-// The block writes the voxel-major rows (z FP32, BF16 hi = bf16(z),
-// lo = bf16(z - hi)) 32 consecutive t per warp store.  bad[i] = 1 when z has
-// a NaN.
+// Layout: one thread per voxel, 64 voxels per block; every pass reads the
+// time-major input coalesced (a warp reads 128 consecutive bytes per time
+// step, several steps in flight).  Pass 1 finds the smallest ulp exponent and
+// the exact int64 sum together (the accumulator is rescaled when a smaller
+// exponent appears); pass 2 runs the sequential centred sum of squares;
+// pass 3 writes the voxel-major rows (z FP32, BF16 hi = bf16(z),
+// lo = bf16(z - hi)) through a 32-step shared-memory transpose so each warp
+// store covers 32 consecutive t of one voxel.  bad[i] = 1 when z has a NaN.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
 
 namespace bna {
 
-constexpr int kZThreads = 128;
-constexpr int kZV = 32;  // voxels per block
+constexpr int kZV = 64;  // voxels per block = threads per block
 
 // Exact float -> double on the bits (normal floats); other classes by the cvt.
 __device__ __forceinline__ double f2d_exact(float x) {
@@ -64,180 +65,116 @@ __device__ __forceinline__ float zdiv(double d, double nrm, double inv) {
   return __uint_as_float(f);
 }
 
-// s[t * (kZV+1) + v]: BOLD value of voxel v0+v at time t.
-template <bool RESIDENT>
-__global__ __launch_bounds__(kZThreads) void zscore_kernel(const float* __restrict__ bold, int N,
-                                                           int T, int n_pad,
-                                                           float* __restrict__ z, int ldz,
-                                                           uint16_t* __restrict__ zhi,
-                                                           uint16_t* __restrict__ zlo, int ldb,
-                                                           uint8_t* __restrict__ bad) {
-  extern __shared__ float zs[];
-  constexpr int ld = kZV + 1;
-  const int rows = RESIDENT ? T : 32;  // series in smem, or one 32-step chunk
-  float* s = zs;
-  double* st_mean = reinterpret_cast<double*>(zs + (((size_t)rows * ld + 1) & ~(size_t)1));
-  double* st_nrm = st_mean + kZV;
-  double* st_inv = st_nrm + kZV;
+__global__ __launch_bounds__(kZV) void zscore_kernel(const float* __restrict__ bold, int N, int T,
+                                                    int n_pad, float* __restrict__ z, int ldz,
+                                                    uint16_t* __restrict__ zhi,
+                                                    uint16_t* __restrict__ zlo, int ldb,
+                                                    uint8_t* __restrict__ bad) {
+  __shared__ float tile[32][kZV + 1];  // tile[tt][v]: z of voxel v0+v at time t0+tt
+  const int v = threadIdx.x, lane = v & 31, warp = v >> 5;
   const int v0 = blockIdx.x * kZV;
-  const int nv = min(kZV, max(0, N - v0));  // voxels of this block that exist
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // BOLD value of voxel v0+v at time t (shared-memory copy or coalesced global read)
-  auto X = [&](int t, int v) -> float {
-    return RESIDENT ? s[t * ld + v] : __ldg(bold + (size_t)t * N + v0 + v);
-  };
+  const int gv = v0 + v;
+  const bool live = gv < N;
+  const float* col = bold + (live ? gv : 0);  // x_t = col[t * N]
 
-  // 1. coalesced load of the block's series (one 128-byte row per time step)
-  if (RESIDENT) {
-    for (int idx = threadIdx.x; idx < T * kZV; idx += kZThreads) {
-      const int t = idx >> 5, v = idx & 31;
-      s[t * ld + v] = (v < nv) ? __ldg(bold + (size_t)t * N + v0 + v) : 0.0f;
-    }
-    __syncthreads();
-  }
-
-  // 2. mean and centred norm, one thread per voxel
-  if (warp == 0) {
-    const int v = lane;
-    double mean = 0.0, nrm = 1.0, inv = 1.0;
-    if (v < nv) {
-      // smallest ulp exponent among the finite non-zero values
-      int emin = 1 << 20;
-      bool special = false;
-      for (int t = 0; t < T; ++t) {
-        const uint32_t b = __float_as_uint(X(t, v));
-        const int e8 = (int)((b >> 23) & 0xFFu);
-        if (e8 == 0xFF || (e8 == 0 && (b & 0x7FFFFFu))) special = true;  // inf/nan/subnormal
-        if (e8 != 0) emin = min(emin, e8 - 150);  // ulp exponent: value = m * 2^(e8-150)
-      }
-      double s1;
-      bool exact = !special;
-      long long acc = 0;
-      if (exact && emin != (1 << 20)) {
-        // sum |x| in units of 2^emin must stay below 2^53
-        long long mag = 0;
-        for (int t = 0; t < T && exact; ++t) {
-          const uint32_t b = __float_as_uint(X(t, v));
-          const int e8 = (int)((b >> 23) & 0xFFu);
-          if (e8 == 0) continue;
-          const int sh = e8 - 150 - emin;
-          if (sh > 29) {
+  double mean = 0.0, nrm = 1.0, inv = 1.0;
+  if (live) {
+    // 1. exact sum: int64 fixed point in units of 2^e0, e0 = smallest ulp
+    //    exponent so far (the accumulator is shifted when e0 drops); exact
+    //    while every value is normal and sum |x| < 2^53 units of the final e0
+    constexpr int kNone = 1 << 20;
+    int e0 = kNone;
+    long long acc = 0, mag = 0;
+    bool exact = true;
+#pragma unroll 8
+    for (int t = 0; t < T; ++t) {
+      const uint32_t b = __float_as_uint(__ldg(col + (size_t)t * N));
+      const int e8 = (int)((b >> 23) & 0xFFu);
+      const uint32_t mant = b & 0x7FFFFFu;
+      if (e8 == 0xFF || (e8 == 0 && mant)) exact = false;  // inf / nan / subnormal
+      if (e8 == 0 || !exact) continue;
+      const int ue = e8 - 150;  // value = (mant | 2^23) * 2^ue
+      if (ue < e0) {
+        if (e0 != kNone) {
+          const int sh = e0 - ue;
+          if (sh >= 53 || (mag >> (53 - sh)) != 0) {
             exact = false;
-            break;
+            continue;
           }
-          const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u) << sh;
-          mag += m;
-          if (mag >= (1LL << 53)) exact = false;
-          acc += (b >> 31) ? -m : m;
+          acc <<= sh;
+          mag <<= sh;
         }
+        e0 = ue;
       }
-      if (exact) {
-        // exact integer -> double (|acc| < 2^53), then the exact power-of-two scale
-        s1 = (emin == (1 << 20)) ? 0.0 : __dmul_rn(__ll2double_rn(acc), ldexp(1.0, emin));
-      } else {
-        s1 = 0.0;
-        for (int t = 0; t < T; ++t) s1 = __dadd_rn(s1, (double)X(t, v));
+      const int sh = ue - e0;
+      if (sh > 29) {
+        exact = false;
+        continue;
       }
-      mean = __ddiv_rn(s1, (double)T);
-      double s2 = 0.0;
-      for (int t = 0; t < T; ++t) {
-        const double dd = __dsub_rn(f2d_exact(X(t, v)), mean);
-        s2 = __dadd_rn(s2, __dmul_rn(dd, dd));
-      }
-      nrm = __dsqrt_rn(s2);
-      inv = __drcp_rn(nrm);
+      const long long m = (long long)(mant | 0x800000u) << sh;
+      mag += m;
+      if (mag >= (1LL << 53)) exact = false;
+      acc += (b >> 31) ? -m : m;
     }
-    st_mean[v] = mean;
-    st_nrm[v] = nrm;
-    st_inv[v] = inv;
+    double s1;
+    if (exact) {
+      // exact integer -> double (|acc| < 2^53), then the exact power-of-two scale
+      s1 = (e0 == kNone) ? 0.0 : __dmul_rn(__ll2double_rn(acc), ldexp(1.0, e0));
+    } else {
+      s1 = 0.0;
+      for (int t = 0; t < T; ++t) s1 = __dadd_rn(s1, (double)__ldg(col + (size_t)t * N));
+    }
+    mean = __ddiv_rn(s1, (double)T);
+    // 2. centred sum of squares, sequential double adds in time order
+    double s2 = 0.0;
+#pragma unroll 8
+    for (int t = 0; t < T; ++t) {
+      const double dd = __dsub_rn(f2d_exact(__ldg(col + (size_t)t * N)), mean);
+      s2 = __dadd_rn(s2, __dmul_rn(dd, dd));
+    }
+    nrm = __dsqrt_rn(s2);
+    inv = __drcp_rn(nrm);
   }
-  __syncthreads();
 
-  // 3. voxel-major rows
+  // 3. voxel-major rows, 32 steps at a time through the transpose tile
   const int tmax = ldz > ldb ? ldz : ldb;
-  auto emit = [&](size_t gi, int t, float zz) {
-    if (t < ldz) z[gi * ldz + t] = zz;
-    if (zhi != nullptr && t < ldb) {
-      const __nv_bfloat16 hh = __float2bfloat16_rn(zz);
-      const __nv_bfloat16 ll = __float2bfloat16_rn(zz - __bfloat162float(hh));
-      zhi[gi * ldb + t] = __bfloat16_as_ushort(hh);
-      zlo[gi * ldb + t] = __bfloat16_as_ushort(ll);
-    }
-  };
-  if (RESIDENT) {
-    // one warp per voxel row, 32 consecutive t per store
-    for (int v = warp; v < kZV; v += kZThreads / 32) {
-      const size_t gi = (size_t)v0 + v;
-      if (gi >= (size_t)n_pad) break;
-      const double mean = st_mean[v], nrm = st_nrm[v], inv = st_inv[v];
-      bool nan_seen = false;
-      for (int t = lane; t < tmax; t += 32) {
-        float zz = 0.0f;
-        if (v < nv && t < T) {
-          zz = zdiv(__dsub_rn(f2d_exact(s[t * ld + v]), mean), nrm, inv);
-          nan_seen |= (zz != zz);
-        }
-        emit(gi, t, zz);
+  bool nan_seen = false;
+  for (int t0 = 0; t0 < tmax; t0 += 32) {
+#pragma unroll 8
+    for (int tt = 0; tt < 32; ++tt) {
+      const int t = t0 + tt;
+      float zz = 0.0f;
+      if (live && t < T) {
+        zz = zdiv(__dsub_rn(f2d_exact(__ldg(col + (size_t)t * N)), mean), nrm, inv);
+        nan_seen |= (zz != zz);
       }
-      nan_seen = __any_sync(0xffffffffu, nan_seen);
-      if (lane == 0) bad[gi] = nan_seen ? 1 : 0;
+      tile[tt][v] = zz;
     }
-  } else {
-    // 32-step chunks: compute z[t][v] into the smem tile (coalesced reads),
-    // then write each voxel's 32 values with one warp store
-    __shared__ int nan_flag[kZV];
-    if (threadIdx.x < kZV) nan_flag[threadIdx.x] = 0;
-    for (int t0 = 0; t0 < tmax; t0 += 32) {
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < 32 * kZV; idx += kZThreads) {
-        const int tt = idx >> 5, v = idx & 31, t = t0 + tt;
-        float zz = 0.0f;
-        if (v < nv && t < T) {
-          zz = zdiv(__dsub_rn(f2d_exact(__ldg(bold + (size_t)t * N + v0 + v)), st_mean[v]),
-                    st_nrm[v], st_inv[v]);
-          if (zz != zz) nan_flag[v] = 1;
-        }
-        s[tt * ld + v] = zz;
-      }
-      __syncthreads();
-      for (int v = warp; v < kZV; v += kZThreads / 32) {
-        const size_t gi = (size_t)v0 + v;
-        if (gi < (size_t)n_pad) emit(gi, t0 + lane, s[lane * ld + v]);
+    __syncthreads();
+    // warp w writes voxels w, w+2, ...: lane = time step within the chunk
+    for (int vv = warp; vv < kZV; vv += kZV / 32) {
+      const size_t gi = (size_t)v0 + vv;
+      const int t = t0 + lane;
+      const float zz = tile[lane][vv];
+      if (t < ldz) z[gi * ldz + t] = zz;
+      if (zhi != nullptr && t < ldb) {
+        const __nv_bfloat16 hh = __float2bfloat16_rn(zz);
+        const __nv_bfloat16 ll = __float2bfloat16_rn(zz - __bfloat162float(hh));
+        zhi[gi * ldb + t] = __bfloat16_as_ushort(hh);
+        zlo[gi * ldb + t] = __bfloat16_as_ushort(ll);
       }
     }
     __syncthreads();
-    if (threadIdx.x < kZV && (size_t)v0 + threadIdx.x < (size_t)n_pad)
-      bad[v0 + threadIdx.x] = nan_flag[threadIdx.x] ? 1 : 0;
   }
+  if (gv < n_pad) bad[gv] = nan_seen ? 1 : 0;
 }
-
-static size_t zscore_smem(int rows) {
-  return (((size_t)rows * (kZV + 1) + 1) & ~(size_t)1) * 4 + (size_t)kZV * 24;
-}
-
-// Series up to this length stay in shared memory (about 48 KB per block, so
-// several blocks - and their FP64 chains - share an SM); longer ones stream.
-constexpr int kZResidentMaxT = 360;
 
 cudaError_t launch_zscore(const float* bold, int N, int T, int n_pad, float* z, int ldz,
                           uint16_t* zhi, uint16_t* zlo, int ldb, uint8_t* bad,
                           cudaStream_t stream) {
-  if (n_pad % 128 != 0 || ldz % 32 != 0 || (zhi && ldb % 32 != 0)) return cudaErrorInvalidValue;
-  const bool resident = T <= kZResidentMaxT;
-  const size_t smem = zscore_smem(resident ? T : 32);
+  if (n_pad % kZV != 0 || ldz % 32 != 0 || (zhi && ldb % 32 != 0)) return cudaErrorInvalidValue;
   const int grid = n_pad / kZV;
-  const int ldbv = zhi ? ldb : 0;
-  cudaError_t e;
-  if (resident) {
-    e = cudaFuncSetAttribute(zscore_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    zscore_kernel<true><<<grid, kZThreads, smem, stream>>>(bold, N, T, n_pad, z, ldz, zhi, zlo,
-                                                           ldbv, bad);
-  } else {
-    zscore_kernel<false><<<grid, kZThreads, smem, stream>>>(bold, N, T, n_pad, z, ldz, zhi, zlo,
-                                                            ldbv, bad);
-  }
+  zscore_kernel<<<grid, kZV, 0, stream>>>(bold, N, T, n_pad, z, ldz, zhi, zlo, zhi ? ldb : 0, bad);
   return cudaGetLastError();
 }
 

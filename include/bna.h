@@ -181,7 +181,7 @@ int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr_dev, int32_t max_iter, double ep
  * memory is held by its own pool, an embedder that forbids allocation after
  * load).  Same kernels and results as bna_ec, but the working vectors and
  * iteration state live in a fixed __device__ array of the library (about
- * 4 MB, kept by every GPU that loads the library until exit), so the call
+ * 8 MB, kept by every GPU that loads the library until exit), so the call
  * allocates nothing; no context is needed.  Limit: n <= 262,144 vertices,
  * else BNA_SCRATCH_LIMIT.  All calls share that array: calls that overlap on
  * a GPU race, so serialise them.  The first call on a device looks up the
