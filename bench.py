@@ -6,7 +6,13 @@ Default workload: N=45,000 voxels x T=240 (float32, seeded factor model,
 K=40), weighted CSR at 1 % density (tau = the FP64 quantile).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P]
-                  [--workload n45k|small|n180k] [--impl reference]
+                  [--workload n45k|small|n180k|serving] [--impl reference]
+                  [--serve-requests R]
+
+The line's "serve" object is a serving sample: R requests (default 120) with
+Poisson arrivals at 4/s through bna_server (continuous admission by HBM
+budget), latency p50/p99 and each request's slowdown against running alone.
+--workload serving runs the full 1,000-request case and prints its own line.
 
 --gpus N > 1 runs under torchrun: every rank builds its own replica of the
 workload (the path has no cross-GPU exchange: replicas only), barrier + max
@@ -43,6 +49,9 @@ def parse():
     p.add_argument("--impl", default="gb300")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--serve-requests", type=int, default=120)
+    p.add_argument("--serve-slots", type=int, default=4)
+    p.add_argument("--serve-dump", default="", help="write per-request records (JSON) here")
     return p.parse_args()
 
 
@@ -157,6 +166,101 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def serve_run(n_requests: int, slots: int = 4, rate: float = 4.0, seed: int = 5000,
+              budget: int = 160 << 30, dump: str = "") -> dict:
+    """Poisson serving run through bna_server, then every request alone.
+
+    The CSR of each request stays on the device (consumed by the centrality);
+    the centrality vector comes back to a pinned host buffer."""
+    import numpy as np
+    import torch
+    import cuda_newest20160331_gb300 as bna
+    from cuda_newest20160331_gb300 import workloads
+    subjects, reqs = workloads.serving(n_requests, rate, seed)
+    pool = []
+    for (N, T, K, sd) in subjects:
+        b = bna.synth_bold(N, T, K, sd)
+        pool.append(torch.from_numpy(b).pin_memory().numpy())
+    n_max = max(N for N, _, _, _ in subjects)
+    ecbufs = [torch.empty(n_max, dtype=torch.float64).pin_memory().numpy() for _ in range(64)]
+
+    def submit(srv, k, r):
+        N = subjects[r.subject][0]
+        return srv.submit(pool[r.subject], mode=r.mode, value=r.value, precision="bf16x3",
+                          csr_out=False, ec_out=ecbufs[k % 64][:N], tag=k)
+
+    def one_pass(srv, timed_arrivals: bool):
+        replies = [None] * len(reqs)
+        lock = threading.Lock()
+        tickets = []
+        start = time.perf_counter()
+
+        def feeder():
+            for k, r in enumerate(reqs):
+                if timed_arrivals:
+                    d = r.arrival - (time.perf_counter() - start)
+                    if d > 0:
+                        time.sleep(d)
+                t = submit(srv, k, r)
+                with lock:
+                    tickets.append((k, t))
+                if not timed_arrivals:  # alone: wait before the next one
+                    replies[k] = srv.wait(t)
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        if timed_arrivals:
+            done = 0
+            while done < len(reqs):
+                with lock:
+                    pending = tickets[done:]
+                if not pending:
+                    time.sleep(0.001)
+                    continue
+                k, t = pending[0]
+                replies[k] = srv.wait(t)
+                done += 1
+        th.join()
+        return replies, time.perf_counter() - start
+
+    with bna.Server(0, slots=slots, hbm_budget=budget) as srv:
+        # warm-up: every pool subject once (arena growth, graph capture)
+        for j, (N, T, K, sd) in enumerate(subjects):
+            srv.wait(srv.submit(pool[j], mode="density", value=1.0, csr_out=False,
+                                ec_out=ecbufs[0][:N]))
+        mixed, span = one_pass(srv, True)
+        alone, _ = one_pass(srv, False)
+    bad = [r.status for r in mixed + alone if r.status != 0]
+    if dump:
+        with open(dump, "w") as f:
+            json.dump([{"k": k, "N": subjects[r.subject][0], "T": subjects[r.subject][1],
+                        "mode": r.mode, "value": r.value, "arrival": r.arrival,
+                        "status": m.status, "slot": m.slot, "nnz": m.nnz,
+                        "sub": m.t_submit, "start": m.t_start, "done": m.t_done,
+                        "solo": a.latency, "iters": m.ec_iters, "stats": m.stats}
+                       for k, (r, m, a) in enumerate(zip(reqs, mixed, alone))], f)
+    lat = np.array([r.latency for r in mixed]) * 1000.0
+    solo = np.array([r.latency for r in alone]) * 1000.0
+    slow = lat / solo
+    same = all(a.nnz == m.nnz and a.lam == m.lam for a, m in zip(alone, mixed))
+    edges = sum(r.nnz for r in mixed)
+    return {
+        "requests": len(reqs), "rate_per_s": rate, "slots": slots,
+        "budget_gb": budget / 2**30, "errors": len(bad),
+        "error_status": {str(c): bad.count(c) for c in sorted(set(bad))},
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "solo_p50_ms": float(np.percentile(solo, 50)), "solo_p99_ms": float(np.percentile(solo, 99)),
+        "slowdown_p50": float(np.percentile(slow, 50)), "slowdown_p99": float(np.percentile(slow, 99)),
+        "p99_over_median_solo": float(np.percentile(lat, 99) / np.percentile(solo, 50)),
+        "throughput_req_s": len(reqs) / span, "edges_per_s": edges / span,
+        "same_results_alone_and_mixed": same,
+        "sample": f"{len(reqs)} requests from {len(subjects)} seeded subjects "
+                  f"(N {min(s[0] for s in subjects)}..{n_max}, T in {{240,600,1200}}), "
+                  "tau U[0.3,0.6] or density U[0.1,2]%, split-BF16, CSR kept on device, "
+                  "centrality to host",
+    }
+
+
 def load_traffic(kernel: str, workload: str):
     """DRAM bytes per launch of `kernel` on `workload` from one ncu capture
     (profiles/traffic.txt: `kernel:workload bytes` lines), or None."""
@@ -192,7 +296,7 @@ def run_reference(args):
         "ms_per_step": 1000.0 * statistics.median(s["seconds"] for s in samples),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded factor model)",
-        "config": {"workload": f"{w.name}: N={w.N} T={w.T} K={w.K} {w.mode} tau={w.value:.6f}",
+        "config": {"workload": f"{w.name}: N={w.N} T={w.T} K={w.K} {w.mode} {'percent' if w.mode == 'density' else 'tau'}={w.value:.6f}",
                    "l2": "inputs on host (CPU run)"},
         "cpu_baseline": {"value": v, "unit": "edges/s", "cores": cores, "kind": "port",
                          "sample": s0["sample"]},
@@ -219,6 +323,14 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    if args.workload == "serving":
+        sv = serve_run(1000 if args.serve_requests == 120 else args.serve_requests,
+                       slots=args.serve_slots, dump=args.serve_dump)
+        if rank == 0:
+            print(json.dumps({"metric": "serving latency p50/p99 (corr -> CSR -> centrality)",
+                              "value": sv["p99_ms"], "unit": "ms", "higher_is_better": False,
+                              "n_gpus": 1, "serve": sv}), flush=True)
+        return
     w = workloads.get(args.workload)
     precision = args.precision
     bold_h = w.bold()
@@ -357,7 +469,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if precision == "fp32" else precision,
         "data": "synthetic (seeded factor model, device-resident input)",
-        "config": {"workload": f"{w.name}: N={N} T={T} K={w.K} {w.mode} tau={w.value:.6f} "
+        "config": {"workload": f"{w.name}: N={N} T={T} K={w.K} {w.mode} {'percent' if w.mode == 'density' else 'tau'}={w.value:.6f} "
                                f"weighted={w.weighted}",
                    "precision": precision, "parallelism": f"replicas x{world}",
                    "l2": "flushed between steps (2x L2 buffer zeroed outside the timed events)"},
@@ -375,6 +487,9 @@ def main():
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "clocks": clk.summary(),
     }
+    if rank == 0 and args.serve_requests > 0:
+        line["serve"] = serve_run(args.serve_requests, slots=args.serve_slots,
+                                  dump=args.serve_dump)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_sample(w, bold_h, args.cpu_seconds, host_cores())
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -7,6 +7,8 @@ Mapping to the reference (W/ = BNAPlatform-weighted-win64-cuda7.0-20160331/src):
                        (W/CorMat/CUCorMat/CUCorMat/CorMat.cu:17, CorMat.cpp:683-918)
   Builder.ec           Lead_Vector_GPU (W/CUEC/weighted-net.cu:55-221)
   Builder.lead_vector  the same with host buffers and the reference's argument list
+  Server               many subjects on one GPU: continuous admission by HBM budget,
+                       each request CorMat -> CSR -> Lead_Vector (no reference counterpart)
   csr_write / csr_read the .csr format (CorMat.cpp:353-360, weighted-net.cu:275-287)
 
 Device buffers are torch CUDA tensors (torch is plumbing for memory and
@@ -24,8 +26,8 @@ import numpy as np
 from . import _lib as L
 from ._lib import BnaError, lib
 
-__all__ = ["Builder", "CsrResult", "synth_bold", "csr_write", "csr_read", "ec_write",
-           "BnaError", "lib"]
+__all__ = ["Builder", "CsrResult", "Server", "Reply", "synth_bold", "csr_write", "csr_read",
+           "ec_write", "request_bytes", "density_nnz", "BnaError", "lib"]
 
 
 def _check(status: int, ctx=None, ok=(L.BNA_OK,)) -> int:
@@ -121,6 +123,10 @@ class Builder:
 
     def trim(self):
         _check(lib().bna_ctx_trim(self._h), self._h)
+
+    def set_option(self, name: str, value: int):
+        """bna_ctx_set_option: "tiles_per_launch" or "max_nnz" (0 = default)."""
+        _check(lib().bna_ctx_set_option(self._h, L.OPTIONS[name], int(value)), self._h)
 
     @staticmethod
     def _stream(stream):
@@ -245,6 +251,130 @@ class Builder:
                                          ec.ctypes.data, C.byref(lam), C.byref(it)), self._h,
                    ok=(L.BNA_OK, L.BNA_NOT_CONVERGED))
         return ec, lam.value, it.value, s == L.BNA_OK
+
+
+def density_nnz(N: int, percent: float) -> int:
+    """Directed CSR entries of the density rule (the reference's Clength)."""
+    return int(lib().bna_density_nnz(N, float(percent)))
+
+
+def request_bytes(N: int, T: int, mode: str = "r_gt", value: float = 0.5,
+                  precision: str = "bf16x3", weighted: bool = True, cap: int = 0,
+                  ec: bool = True) -> int:
+    """Device-memory estimate the server admits a request by (bna_request_bytes)."""
+    o = _opts(mode, value, precision, weighted, None)
+    return int(lib().bna_request_bytes(N, T, C.byref(o), cap, 1 if ec else 0))
+
+
+@dataclass
+class Reply:
+    status: int
+    tag: int
+    slot: int
+    nnz: int
+    row_ptr: np.ndarray
+    col_idx: np.ndarray
+    val: Optional[np.ndarray]
+    ec: Optional[np.ndarray]
+    lam: float
+    ec_iters: int
+    ec_converged: bool
+    t_submit: float
+    t_start: float
+    t_done: float
+    stats: dict
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.t_submit
+
+
+class Server:
+    """bna_server: worker slots on one GPU admitting requests by HBM budget.
+
+    submit() takes a host BOLD array [T][N] and returns a ticket; the CSR and
+    centrality land in host buffers this object allocates (pinned when
+    `pinned`), handed back by wait()."""
+
+    def __init__(self, device: int = 0, slots: int = 4, hbm_budget: int = 64 << 30,
+                 pinned: bool = True):
+        h = C.c_void_p()
+        _check(lib().bna_server_create(device, slots, int(hbm_budget), C.byref(h)))
+        self._h = h
+        self._pinned = pinned
+        self._live = {}  # ticket -> (request struct, buffers) kept alive until wait()
+
+    def _alloc(self, shape, dtype):
+        if self._pinned:
+            import torch
+            tdt = {np.int32: torch.int32, np.float32: torch.float32, np.float64: torch.float64}
+            t = torch.empty(shape, dtype=tdt[dtype]).pin_memory()
+            return t.numpy()
+        return np.empty(shape, dtype=dtype)
+
+    def submit(self, bold: np.ndarray, mode: str = "r_gt", value: float = 0.5,
+               precision: str = "bf16x3", weighted: bool = True, cap: Optional[int] = None,
+               ec_max_iter: int = 10000, ec_eps: float = 1e-6, tag: int = 0,
+               csr_out: bool = True, ec_out: Optional[np.ndarray] = None) -> int:
+        """csr_out=False keeps the CSR on the device (only the centrality comes
+        back); ec_out: caller's float64 [N] buffer for the centrality."""
+        assert bold.dtype == np.float32 and bold.flags.c_contiguous
+        T, N = bold.shape
+        if cap is None:
+            if mode == "density":
+                cap = max(1, density_nnz(N, value))
+            else:
+                cap = max(1, N * (N - 1) // 20)  # 5 % density
+        rp = self._alloc(N + 1, np.int32) if csr_out else None
+        ci = self._alloc(max(cap, 1), np.int32) if csr_out else None
+        va = self._alloc(max(cap, 1), np.float32) if weighted and csr_out else None
+        ecv = ec_out if ec_out is not None else (
+            self._alloc(N, np.float64) if ec_max_iter > 0 else None)
+        r = L.Request(bold_host=bold.ctypes.data, N=N, T=T,
+                      opts=_opts(mode, value, precision, weighted, None),
+                      ec_max_iter=ec_max_iter, ec_eps=ec_eps,
+                      row_ptr_host=rp.ctypes.data if rp is not None else None,
+                      col_idx_host=ci.ctypes.data if ci is not None else None,
+                      val_host=va.ctypes.data if va is not None else None,
+                      cap=cap, ec_host=ecv.ctypes.data if ecv is not None else None, tag=tag)
+        t = C.c_int64()
+        _check(lib().bna_server_submit(self._h, C.byref(r), C.byref(t)))
+        self._live[t.value] = (r, bold, rp, ci, va, ecv)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> Reply:
+        rep = L.Reply()
+        _check(lib().bna_server_wait(self._h, ticket, float(timeout), C.byref(rep)))
+        r, bold, rp, ci, va, ecv = self._live.pop(ticket)
+        nnz = int(rep.nnz) if rep.status == L.BNA_OK else 0
+        return Reply(status=rep.status, tag=rep.tag, slot=rep.slot, nnz=int(rep.nnz),
+                     row_ptr=rp, col_idx=ci[:nnz] if ci is not None else None,
+                     val=va[:nnz] if va is not None else None,
+                     ec=ecv, lam=rep.lambda_, ec_iters=rep.ec_iters,
+                     ec_converged=bool(rep.ec_converged), t_submit=rep.t_submit,
+                     t_start=rep.t_start, t_done=rep.t_done, stats=rep.stats.as_dict())
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().bna_server_device_bytes(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bna_server_destroy(self._h)
+            self._h = None
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def csr_write(path: str, row_ptr: np.ndarray, col_idx: np.ndarray,

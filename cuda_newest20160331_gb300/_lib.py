@@ -15,6 +15,8 @@ LIB_PATH = os.path.join(PKG, "libbna.so")
 BNA_OK = 0
 BNA_NOT_CONVERGED = 4
 BNA_CAPACITY = 13
+BNA_OVER_BUDGET = 14
+OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1}
 THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4}
 PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2}
 SYNTH_KINDS = {"iid": 0, "blocknet": 1}
@@ -41,6 +43,21 @@ class CorrStats(C.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class Request(C.Structure):
+    _fields_ = [("bold_host", C.c_void_p), ("N", C.c_int32), ("T", C.c_int32),
+                ("opts", CorrOpts), ("ec_max_iter", C.c_int32), ("ec_eps", C.c_double),
+                ("row_ptr_host", C.c_void_p), ("col_idx_host", C.c_void_p),
+                ("val_host", C.c_void_p), ("cap", C.c_int64), ("ec_host", C.c_void_p),
+                ("tag", C.c_int64)]
+
+
+class Reply(C.Structure):
+    _fields_ = [("status", C.c_int32), ("slot", C.c_int32), ("tag", C.c_int64),
+                ("nnz", C.c_int64), ("lambda_", C.c_double), ("ec_iters", C.c_int32),
+                ("ec_converged", C.c_int32), ("t_submit", C.c_double), ("t_start", C.c_double),
+                ("t_done", C.c_double), ("stats", CorrStats)]
 
 
 class SynthParams(C.Structure):
@@ -84,6 +101,15 @@ SIGNATURES = {
     "bna_csr_read": (C.c_int32, [C.c_char_p, C.POINTER(Csr)]),
     "bna_ec_write": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32]),
     "bna_synth_bold": (C.c_int, [C.POINTER(SynthParams), C.c_void_p, C.c_int]),
+    "bna_ctx_set_option": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64]),
+    "bna_server_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
+    "bna_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    "bna_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(Reply)]),
+    "bna_server_device_bytes": (C.c_int64, [C.c_void_p]),
+    "bna_server_destroy": (C.c_int32, [C.c_void_p]),
+    "bna_density_nnz": (C.c_int64, [C.c_int32, C.c_double]),
+    "bna_request_bytes": (C.c_int64, [C.c_int32, C.c_int32, C.POINTER(CorrOpts), C.c_int64,
+                                      C.c_int32]),
 }
 
 _lib = None

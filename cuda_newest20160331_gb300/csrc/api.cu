@@ -15,8 +15,9 @@
 #include "common.cuh"
 
 namespace bna {
+size_t zscore_scratch_bytes(int n_pad);
 cudaError_t launch_zscore(const float* bold, int N, int T, int n_pad, float* z, int ldz,
-                          uint16_t* zhi, uint16_t* zlo, int ldb, uint8_t* bad,
+                          uint16_t* zhi, uint16_t* zlo, int ldb, uint8_t* bad, void* scratch,
                           cudaStream_t stream);
 cudaError_t launch_corr_simt(const CorrArgs& a, int pass, cudaStream_t stream);
 cudaError_t launch_corr_simt_dump(const CorrArgs& a, int I, int J, float* out,
@@ -36,11 +37,18 @@ cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const fl
                            int grid, int max_iter, double eps, cudaStream_t stream);
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done);
+int ec_state_err(const void* host_copy);
+int ec_coop_grid(int n, int sms);
+cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                           const double* vald, long long nnz_used, double* u, float2* uf,
+                           double* parts, void* st, int grid, int max_iter, double eps,
+                           cudaStream_t stream);
 void tc_tile_list(int nb, std::vector<int2>& out);
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st);
+cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t st);
 cudaError_t launch_csr_fill(const CorrArgs& a, int sms, int* dense_list, unsigned int* dense_count,
                             cudaStream_t stream);
 cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream);
@@ -55,7 +63,7 @@ enum Slot {
   S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
   S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL,
-  S_DENSE, S_COUNT
+  S_DENSE, S_WSTATE, S_VSTAT, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -94,6 +102,9 @@ struct bna_ctx {
   EcGraph ecg;
   int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
   int ntiles = 0;
+  int tiles_per_launch = 0;  // BNA_OPT_TILES_PER_LAUNCH
+  cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
+  long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
 };
 
 namespace {
@@ -121,17 +132,20 @@ int32_t fail(bna_ctx* c, int32_t st, const char* fmt, ...) {
 int32_t ensure(bna_ctx* ctx, Slot s, size_t bytes, void** out) {
   if (bytes == 0) bytes = 16;
   if (ctx->cap[s] < bytes) {
+    // stream-ordered on the call's stream: growing one context's arena does
+    // not wait for the work other contexts have on the device
     if (ctx->ptr[s]) {
-      cudaError_t e = cudaFree(ctx->ptr[s]);
+      cudaError_t e = cudaFreeAsync(ctx->ptr[s], ctx->cur);
       ctx->ptr[s] = nullptr;
       ctx->cap[s] = 0;
-      if (e != cudaSuccess) return fail(ctx, BNA_CUDA_ERROR, "cudaFree: %s", cudaGetErrorString(e));
+      if (e != cudaSuccess)
+        return fail(ctx, BNA_CUDA_ERROR, "cudaFreeAsync: %s", cudaGetErrorString(e));
     }
     const size_t want = bytes + bytes / 8;  // headroom so small growth does not reallocate
-    cudaError_t e = cudaMalloc(&ctx->ptr[s], want);
+    cudaError_t e = cudaMallocAsync(&ctx->ptr[s], want, ctx->cur);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      e = cudaMalloc(&ctx->ptr[s], bytes);
+      e = cudaMallocAsync(&ctx->ptr[s], bytes, ctx->cur);
       if (e != cudaSuccess) {
         cudaGetLastError();
         ctx->ptr[s] = nullptr;
@@ -173,8 +187,11 @@ unsigned long long next_pow2(unsigned long long x) {
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-int32_t set_device(bna_ctx* ctx) {
+// Every entry point starts here: device current, and the call's stream
+// recorded for stream-ordered arena growth.
+int32_t set_device(bna_ctx* ctx, cudaStream_t st = nullptr) {
   CK(cudaSetDevice(ctx->device));
+  ctx->cur = st;
   return BNA_OK;
 }
 
@@ -196,7 +213,9 @@ int32_t run_zscore(bna_ctx* ctx, const float* bold, int N, int T, bool need_bf16
     ENSURE(S_ZHI, (size_t)a.n_pad * a.ldb * 2, zhi);
     ENSURE(S_ZLO, (size_t)a.n_pad * a.ldb * 2, zlo);
   }
-  CK(launch_zscore(bold, N, T, a.n_pad, z, a.ldz, zhi, zlo, a.ldb, bad, st));
+  void* vstat;
+  ENSURE(S_VSTAT, zscore_scratch_bytes(a.n_pad), vstat);
+  CK(launch_zscore(bold, N, T, a.n_pad, z, a.ldz, zhi, zlo, a.ldb, bad, vstat, st));
   a.z = z;
   a.zhi = zhi;
   a.zlo = zlo;
@@ -222,17 +241,28 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
   return BNA_OK;
 }
 
+// Edge-list chunk per warp: small problems (few tiles per warp) take small
+// chunks so the pool's minimum size stays modest.
+long long elist_chunk(const bna_ctx* ctx, const CorrArgs& a) {
+  const long long nst = (long long)a.nb * (a.nb + 1) / 2;
+  return nst < (long long)ctx->sms * 8 * 16 ? kElistChunkMin : kElistChunk;
+}
+
 // pass 0: count (+ edge lists); pass 3: density histogram
 int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st) {
   switch (precision) {
     case BNA_PREC_FP32: CK(launch_corr_simt(a, pass, st)); return BNA_OK;
     case BNA_PREC_BF16X3:
-    case BNA_PREC_TF32:
-      CK(launch_corr_tc(a, pass, precision == BNA_PREC_BF16X3 ? 0 : 1,
-                        reinterpret_cast<const int2*>(ctx->ptr[S_TILES]), ctx->ntiles,
-                        reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
-                        ctx->sms, st));
+    case BNA_PREC_TF32: {
+      const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[S_TILES]);
+      const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : ctx->ntiles;
+      for (int t0 = 0; t0 < ctx->ntiles; t0 += per)
+        CK(launch_corr_tc(a, pass, precision == BNA_PREC_BF16X3 ? 0 : 1, tiles + t0,
+                          std::min(per, ctx->ntiles - t0),
+                          reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
+                          ctx->sms, st));
       return BNA_OK;
+    }
     default:
       return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built in this library", precision);
   }
@@ -260,6 +290,7 @@ const char* bna_status_string(int32_t s) {
     case BNA_UNSUPPORTED: return "unsupported";
     case BNA_SCRATCH_LIMIT: return "problem exceeds the fixed scratch of the no-allocation entry point";
     case BNA_CAPACITY: return "output buffers too small";
+    case BNA_OVER_BUDGET: return "request exceeds the server's device-memory budget";
     default: return "unknown status";
   }
 }
@@ -291,15 +322,66 @@ int32_t bna_ctx_create(int32_t device, bna_ctx** out) {
   return BNA_OK;
 }
 
+int64_t bna_density_nnz(int32_t N, double percent) {
+  if (N < 1 || !(percent >= 0.0 && percent <= 100.0)) return -1;
+  const long long M1 = (long long)N * (N - 1) / 2;
+  long long clen = (long long)((double)((float)(2 * M1) * (float)percent) / 100.0);
+  return clen + clen % 2;
+}
+
+int64_t bna_request_bytes(int32_t N, int32_t T, const bna_corr_opts* opts, int64_t cap,
+                          int32_t with_ec) {
+  if (N < 1 || T < 1 || !opts || cap < 0) return -1;
+  // the arena slots bna_corr_csr / bna_ec size (run_zscore, the count pass
+  // buffers, the CSR), plus the request's own BOLD and centrality buffers
+  const long long n_pad = round_up(N, kBlk), nb = n_pad / kBlk;
+  const long long ldz = round_up(T, 32), ldb = round_up(T, 64);
+  const long long nst = nb * (nb + 1) / 2;
+  const long long ntiles = nb * (nb / 2 + 1);
+  const bool density = opts->mode == BNA_THR_DENSITY;
+  long long nnz = cap;
+  if (density) nnz = std::min<long long>(nnz, bna_density_nnz(N, opts->value));
+  const int sms = 160;  // upper bound of this GPU family's SM count, for the pool minimum
+  const long long chunk = nst < (long long)sms * 8 * 16 ? kElistChunkMin : kElistChunk;
+  const long long elist = std::max<long long>((long long)sms * 8 * 2 * chunk, nnz / 2 + nnz / 8);
+  const long long cand = 1LL << 20;
+  long long b = 0;
+  b += (long long)N * T * 4;                                   // BOLD
+  b += n_pad * ldz * 4 + n_pad;                                // z, bad
+  if (opts->precision == BNA_PREC_BF16X3) b += n_pad * ldb * 4;  // z hi / lo
+  b += nb * n_pad * 4 + 2 * n_pad * 8 + 4096 * 8;              // seg, row lengths, block sums
+  b += nst * 64 + nst * 4 + ntiles * 8 + nb;                   // etab, dense list, tiles, flags
+  b += elist * 8;                                              // edge lists
+  b += cand * 8 + 2 * cand * 13 + (density ? cand * 4 : 0);    // candidates, hash, values
+  b += (long long)(N + 1) * 4 + nnz * (opts->weighted ? 8 : 4);  // CSR
+  if (with_ec) b += (long long)N * (2 * 16 + 8) + 64 * 1024;     // iterates, output, partials
+  return b;
+}
+
+int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value) {
+  if (!ctx || value < 0) return fail(ctx, BNA_BAD_ARG, "bna_ctx_set_option: bad arguments");
+  switch (option) {
+    case BNA_OPT_TILES_PER_LAUNCH:
+      if (value > 0x7fffffff) return fail(ctx, BNA_BAD_ARG, "tiles per launch too large");
+      ctx->tiles_per_launch = (int)value;
+      return BNA_OK;
+    case BNA_OPT_MAX_NNZ: ctx->max_nnz = value; return BNA_OK;
+    default: return fail(ctx, BNA_BAD_ARG, "unknown option %d", option);
+  }
+}
+
 int32_t bna_ctx_trim(bna_ctx* ctx) {
   if (!ctx) return BNA_BAD_ARG;
   cudaSetDevice(ctx->device);
+  // the arena is stream-ordered memory: wait for every user, then free it
   cudaDeviceSynchronize();
   for (int s = 0; s < S_COUNT; ++s) {
-    if (ctx->ptr[s]) cudaFree(ctx->ptr[s]);
+    if (ctx->ptr[s]) cudaFreeAsync(ctx->ptr[s], nullptr);
     ctx->ptr[s] = nullptr;
     ctx->cap[s] = 0;
   }
+  cudaStreamSynchronize(nullptr);
+  ctx->tiles_nb = -1;  // the tile list lived in the arena
   if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
   ctx->ecg = EcGraph();
   return BNA_OK;
@@ -332,20 +414,23 @@ int32_t bna_zscore(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T, fl
                    int32_t ldz, void* stream) {
   if (!ctx || !bold_dev || !z_dev || N <= 0 || T <= 0 || ldz < T || ldz % 32 != 0)
     return fail(ctx, BNA_BAD_ARG, "bna_zscore: bad arguments");
-  int32_t s = set_device(ctx);
+  int32_t s = set_device(ctx, as_stream(stream));
   if (s) return s;
   const int n_pad = round_up(N, kBlk);
   uint8_t* bad;
   ENSURE(S_BAD, (size_t)n_pad, bad);
+  void* vstat;
+  ENSURE(S_VSTAT, zscore_scratch_bytes(n_pad), vstat);
   // The kernel writes n_pad rows; the caller's buffer holds N rows, so stage
   // through the arena when N is not a multiple of the block.
   if (n_pad == N) {
-    CK(launch_zscore(bold_dev, N, T, n_pad, z_dev, ldz, nullptr, nullptr, 0, bad,
+    CK(launch_zscore(bold_dev, N, T, n_pad, z_dev, ldz, nullptr, nullptr, 0, bad, vstat,
                      as_stream(stream)));
   } else {
     float* z;
     ENSURE(S_Z, (size_t)n_pad * ldz * sizeof(float), z);
-    CK(launch_zscore(bold_dev, N, T, n_pad, z, ldz, nullptr, nullptr, 0, bad, as_stream(stream)));
+    CK(launch_zscore(bold_dev, N, T, n_pad, z, ldz, nullptr, nullptr, 0, bad, vstat,
+                     as_stream(stream)));
     CK(cudaMemcpyAsync(z_dev, z, (size_t)N * ldz * sizeof(float), cudaMemcpyDeviceToDevice,
                        as_stream(stream)));
   }
@@ -364,7 +449,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   const bool density = opts->mode == BNA_THR_DENSITY;
   if (density && !(opts->value >= 0.0 && opts->value <= 100.0))
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: density %g%% outside [0, 100]", opts->value);
-  int32_t s = set_device(ctx);
+  int32_t s = set_device(ctx, as_stream(stream));
   if (s) return s;
   cudaStream_t st = as_stream(stream);
   const int prec = opts->precision;
@@ -407,11 +492,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     a.th.tau = (float)opts->value;
     a.th.delta = (float)delta;
   } else {
-    const long long M1 = (long long)N * (N - 1) / 2;
-    const float sf = (float)opts->value;
-    long long clen = (long long)((double)((float)(2 * M1) * sf) / 100.0);
-    clen += clen % 2;
-    k_dens = clen / 2;
+    k_dens = bna_density_nnz(N, opts->value) / 2;  // CorMat.cpp:327-329
     if (k_dens == 0) {
       a.th.mode = BNA_THR_R_GT;  // no edge at all
       a.th.tau = 2.0f;
@@ -457,7 +538,8 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   for (int attempt = 0;; ++attempt) {
     a.cand_cap = ctx->cand_cap;
     // the pool hands out one chunk per warp at a time: room for two per warp
-    const long long min_pool = (long long)ctx->sms * 8 * 2 * kElistChunk;
+    a.echunk = elist_chunk(ctx, a);
+    const long long min_pool = (long long)ctx->sms * 8 * 2 * a.echunk;
     if (ctx->elist_cap < min_pool) ctx->elist_cap = min_pool;
     a.ecap = ctx->elist_cap;
     const unsigned long long hcap = next_pow2((unsigned long long)a.cand_cap * 2);
@@ -470,9 +552,13 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     if (density && k_dens > 0) ENSURE(S_CANDVAL, (size_t)a.cand_cap * sizeof(float), cvals);
     CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
     CK(cudaMemsetAsync(a.hkeys, 0xff, hcap * 8, st));
+    const int nwarps = ctx->sms * 8;  // epilogue warps of the tensor-core pass
+    ENSURE(S_WSTATE, (size_t)nwarps * 4 * sizeof(long long), a.wstate);
+    CK(cudaMemsetAsync(a.wstate, 0, (size_t)nwarps * 4 * sizeof(long long), st));
     a.th = count_th;
     s = corr_pass(ctx, a, prec, 0, st);
     if (s) return s;
+    if (prec != BNA_PREC_FP32) CK(launch_seal_candidates(a, nwarps, st));
     ++passes;
     CK(cudaEventRecord(ctx->ev[2], st));
     // the tensor-core count pass lists its candidates itself
@@ -494,7 +580,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
       again = true;
     }
     if ((hs->err & ERR_ELIST) && attempt < 3) {
-      ctx->elist_cap = (long long)(hs->epool + hs->epool / 4) + kElistChunk;
+      ctx->elist_cap = (long long)(hs->epool + hs->epool / 4) + a.echunk;
       again = true;
     }
     if (!again) break;
@@ -572,6 +658,15 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   if (hs->err & ERR_NNZ_INT32 || hs->total > 0x7fffffffLL)
     return fail(ctx, BNA_NNZ_OVERFLOW_INT32, "nnz %lld exceeds int32", hs->total);
   const long long nnz = hs->total;
+  if (ctx->max_nnz > 0 && nnz > ctx->max_nnz) {
+    if (stats) {
+      std::memset(stats, 0, sizeof *stats);
+      stats->nnz = nnz;
+      stats->tau = (double)a.th.tau;
+      stats->delta = delta;
+    }
+    return fail(ctx, BNA_CAPACITY, "CSR needs %lld entries, limit %lld", nnz, ctx->max_nnz);
+  }
   const unsigned long long cand_count = hs->stats[3];  // candidates (not slots)
   const unsigned long long band_edges = hs->stats[0], band_1e6 = hs->stats[1];
   int32_t* col;
@@ -605,12 +700,15 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     stats->band_1e6 = (int64_t)band_1e6;
     stats->ties_dropped = ties_dropped;
     stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
-    // z-score, [block flags], [histogram], per attempt: count, [collect (FP32 form)],
-    // recompute or values, 4 scan kernels; [decide + 4 scan kernels]; fill (2 kernels)
-    const int collect = prec == BNA_PREC_FP32 ? 1 : 0;
+    // z-score, [block flags], [histogram], per attempt: count (one launch per tile chunk),
+    // collect (FP32 form) or seal (tensor-core forms), recompute or values, 4 scan kernels;
+    // [decide + 4 scan kernels]; fill (2 kernels)
+    int chunks = 1;
+    if (prec != BNA_PREC_FP32 && ctx->tiles_per_launch > 0)
+      chunks = (ctx->ntiles + ctx->tiles_per_launch - 1) / ctx->tiles_per_launch;
     stats->kernel_launches =
         1 + (prec != BNA_PREC_FP32 ? 1 : 0) +
-        (density && k_dens > 0 ? 1 + passes * (2 + collect) + 5 : passes * (6 + collect)) + 2;
+        (density && k_dens > 0 ? chunks + passes * (chunks + 2) + 5 : passes * (chunks + 6)) + 2;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);
@@ -705,7 +803,7 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
                              void* stream) {
   if (!ctx || !bold_dev || !out_dev || N < 1 || T < 1)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_tile_values: bad arguments");
-  int32_t s = set_device(ctx);
+  int32_t s = set_device(ctx, as_stream(stream));
   if (s) return s;
   cudaStream_t st = as_stream(stream);
   CorrArgs a{};
@@ -746,10 +844,29 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
   ENSURE(S_EC_U, (size_t)2 * n * (sizeof(double) + sizeof(float2)), u);
   float2* uf = reinterpret_cast<float2*>(u + (size_t)2 * n);
   const int grid = std::max(1, ctx->sms * 4);
-  ENSURE(S_EC_PARTS, (size_t)grid * 3 * sizeof(double), parts);
+  ENSURE(S_EC_PARTS, (size_t)grid * 6 * sizeof(double), parts);
   ENSURE(S_EC_STATE, ec_state_bytes(), state);
   CK(cudaMemsetAsync(state, 0, ec_state_bytes(), st));
   CK(launch_ec_init(n, u, uf, parts, state, grid, max_iter, st));
+  // the whole iteration as one cooperative persistent launch
+  const int cgrid = ec_coop_grid(n, ctx->sms);
+  if (cgrid > 0) {
+    CK(launch_ec_coop(n, rp, ci, val, vald, nnz_used, u, uf, parts, state, cgrid, max_iter, eps,
+                      st));
+    CK(cudaMemcpyAsync(ctx->pinned, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (ec_state_err(ctx->pinned))
+      return fail(ctx, BNA_TIMEOUT, "centrality: a bounded grid barrier expired");
+    double lam2 = 0, lam = 0, e1 = 0, e2 = 0;
+    int it = 0, done = 0;
+    ec_state_read(ctx->pinned, &lam2, &lam, &e1, &e2, &it, &done);
+    CK(cudaMemcpyAsync(ec_dev, u + (size_t)(it & 1) * n, (size_t)n * sizeof(double),
+                       cudaMemcpyDeviceToDevice, st));
+    if (lambda) *lambda = lam;
+    if (iters) *iters = it;
+    return (e1 <= eps || e2 <= eps) ? BNA_OK : BNA_NOT_CONVERGED;
+  }
+  // otherwise: a captured graph of kGraphIters per-iteration launches
   EcGraph& g = ctx->ecg;
   const void* key[6] = {rp, ci, val, vald, u, state};
   bool same = g.exec && g.n == n && g.grid == grid && g.max_iter == max_iter && g.eps == eps &&
@@ -807,7 +924,7 @@ int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr, int32_t max_iter, double eps, d
                double* lambda, int32_t* iters, void* stream) {
   if (!ctx || !csr || !ec_dev || csr->n < 1 || !csr->row_ptr || (csr->nnz > 0 && !csr->col_idx))
     return fail(ctx, BNA_BAD_ARG, "bna_ec: bad arguments");
-  int32_t s = set_device(ctx);
+  int32_t s = set_device(ctx, as_stream(stream));
   if (s) return s;
   return ec_run(ctx, csr->n, csr->row_ptr, csr->col_idx, csr->val, nullptr, csr->nnz, max_iter,
                 eps, ec_dev, lambda, iters, as_stream(stream));

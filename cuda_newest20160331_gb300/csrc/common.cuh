@@ -24,9 +24,12 @@ enum : uint32_t {
   ERR_ELIST = 128u,         // edge-list pool too small (entries not written; pass is rerun)
 };
 
-// Edge-list pool: the count pass allocates it in chunks of kElistChunk
-// entries per warp (one atomic per chunk) and never writes past ecap.
+// Edge-list pool: the tensor-core count pass allocates it in chunks of
+// echunk entries per warp (one atomic per chunk; kElistChunkMin for small
+// problems, kElistChunk otherwise) and never writes past ecap.  A chunk must
+// hold a warp's worst case for one tile (32 rows x 128 columns).
 constexpr long long kElistChunk = 16384;
+constexpr long long kElistChunkMin = 4096;
 // Candidate list: the tensor-core count pass writes its near-threshold pairs
 // itself, in warp-private chunks of kCandChunk slots; slots a warp leaves
 // unused hold (kCandNone, kCandNone) and are skipped by the consumers.
@@ -109,6 +112,8 @@ struct CorrArgs {
   uint2* elist;
   unsigned long long* epool;
   long long ecap;
+  long long echunk;  // entries per warp chunk (kElistChunkMin .. kElistChunk)
+  long long* wstate; // tensor-core count pass: per epilogue warp (wcur, wend, ccur, cend)
   longlong2* etab;
   // density ties that must not become edges (sorted keys), see FormFullGraph_s
   const unsigned long long* drop_keys;

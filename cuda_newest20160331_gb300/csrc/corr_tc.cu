@@ -277,9 +277,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // a pair with a NaN voxel has the exact value 0 (post_block)
     const bool zero_int = (0.0f >= lo_thr) || (0.0f >= lim);
     uint32_t hphase = 0;
-    long long wcur = 0, wend = 0;  // this warp's current edge-list chunk [wcur, wend)
-    bool wok = true;
-    long long ccur = 0, cend = 0;  // this warp's current candidate chunk [ccur, cend)
+    // this warp's current edge-list chunk [wcur, wend) and candidate chunk
+    // [ccur, cend), carried from launch to launch of a pass in a.wstate
+    const int wid = (int)blockIdx.x * 8 + (warp - 2);
+    long long wcur = 0, wend = 0, ccur = 0, cend = 0;
+    if (PASS == 0 && lane < 4) {
+      const long long x = a.wstate[wid * 4 + lane];
+      wcur = lane == 0 ? x : 0;
+      wend = lane == 1 ? x : 0;
+      ccur = lane == 2 ? x : 0;
+      cend = lane == 3 ? x : 0;
+    }
+    if (PASS == 0) {
+      wcur = __shfl_sync(0xffffffffu, wcur, 0);
+      wend = __shfl_sync(0xffffffffu, wend, 1);
+      ccur = __shfl_sync(0xffffffffu, ccur, 2);
+      cend = __shfl_sync(0xffffffffu, cend, 3);
+    }
+    bool wok = wend <= a.ecap;
     unsigned long long n_def = 0, n_cand = 0;  // this lane's definite edges and candidates
     int m = 0;
     // tile coordinates and NaN-block flags run one tile ahead
@@ -312,10 +327,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // room for this warp's worst case (32 rows x 128 columns) in one chunk
         if (wend - wcur < 32 * 128) {
           long long base = 0;
-          if (lane == 0) base = (long long)atomicAdd(a.epool, (unsigned long long)kElistChunk);
+          if (lane == 0) base = (long long)atomicAdd(a.epool, (unsigned long long)a.echunk);
           base = __shfl_sync(0xffffffffu, base, 0);
           wcur = base;
-          wend = base + kElistChunk;
+          wend = base + a.echunk;
           wok = wend <= a.ecap;
           if (!wok && lane == 0) atomicOr(a.err, ERR_ELIST);
         }
@@ -496,8 +511,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
     }
     if (PASS == 0) {
-      for (long long sl = ccur + lane; sl < cend && sl < a.cand_cap; sl += 32)
-        a.cand[sl] = make_uint2(kCandNone, kCandNone);
+      // the chunks stay open for the next launch; seal_candidates_kernel
+      // closes the candidate chunks after the pass
+      if (lane < 4) a.wstate[wid * 4 + lane] = lane == 0 ? wcur : lane == 1 ? wend : lane == 2 ? ccur : cend;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         n_def += __shfl_xor_sync(0xffffffffu, n_def, o);
@@ -516,6 +532,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (PASS == 3)
     for (int b = threadIdx.x; b <= kHistBins; b += blockDim.x)
       if (S.hist[b]) atomicAdd(&a.hist[b], S.hist[b]);
+}
+
+// After the last launch of a count pass: mark the unused slots of every
+// warp's open candidate chunk (warp states are (wcur, wend, ccur, cend)).
+__global__ void seal_candidates_kernel(CorrArgs a, int nwarps) {
+  const int lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nwarps;
+       w += gridDim.x * (blockDim.x >> 5)) {
+    const long long ccur = a.wstate[w * 4 + 2], cend = a.wstate[w * 4 + 3];
+    for (long long sl = ccur + lane; sl < cend && sl < a.cand_cap; sl += 32)
+      if (sl >= 0) a.cand[sl] = make_uint2(kCandNone, kCandNone);
+  }
 }
 
 __global__ void block_bad_kernel(const uint8_t* bad, int nb, uint8_t* blockbad) {
@@ -572,6 +600,11 @@ size_t tc_smem_bytes() { return TC_SMEM_BYTES; }
 
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st) {
   block_bad_kernel<<<nb, 128, 0, st>>>(bad, nb, blockbad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t st) {
+  seal_candidates_kernel<<<(nwarps + 7) / 8, 256, 0, st>>>(a, nwarps);
   return cudaGetLastError();
 }
 

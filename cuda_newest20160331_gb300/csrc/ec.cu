@@ -12,6 +12,14 @@
 // e1 <= eps or e2 <= eps (no host round trip per iteration); the host replays
 // a captured CUDA graph of 32 iterations and reads the flag between graphs.
 //
+// Normally the whole power iteration is one cooperative, persistent launch
+// (ec_coop_kernel): blocks meet at a grid barrier once per iteration and
+// every block then reduces the block partials in the same fixed order, so no
+// launch, tail or host round trip separates the iterations; graphs with many
+// iterations (a graph that never meets the stop test runs the reference's
+// 10,000) cost microseconds per iteration.  The per-iteration kernel above
+// remains for the no-allocation entry point.
+//
 // The SpMV runs in float-float ("double-float") arithmetic instead of FP64,
 // whose rate on this GPU is ~1/70 of FP32: the iterate is kept twice, as
 // double (norms, convergence test, output) and as a (hi, lo) float pair for
@@ -33,7 +41,8 @@ struct EcState {
   int iter;           // completed iterations
   int done;
   unsigned int counter;
-  int pad;
+  int err;                // bounded grid barrier expired (persistent kernel)
+  unsigned int bar_count, bar_gen;  // grid barrier of the persistent kernel
 };
 
 constexpr int kEcThreads = 256;
@@ -150,6 +159,42 @@ __device__ __forceinline__ void df_accum(float& sh, float& sl, float vh, float v
   sl = __fadd_rn(sl, __fadd_rn(e, pe));
 }
 
+// One warp, one row: (sh, sl) += sum over entries [b, e) of val * x[col], eight
+// entries per lane in flight per round (predicated, so a row costs
+// ceil((e - b) / 256) memory round trips).  l2_only: read x through L2 only
+// (the persistent kernel, whose iterate other blocks rewrite in the same launch).
+template <int VK>
+__device__ __forceinline__ void ec_row_accum(const int32_t* __restrict__ ci,
+                                             const float* __restrict__ val,
+                                             const double* __restrict__ vald,
+                                             const float2* uf, long long b, long long e,
+                                             int lane, float& sh, float& sl, bool l2_only) {
+  for (long long k0 = b; k0 < e; k0 += 256) {
+    int c[8];
+    float vh[8], vl[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const long long k = k0 + lane + 32 * m;
+      const bool ok = k < e;
+      c[m] = ok ? __ldg(ci + k) : -1;
+      vh[m] = 1.0f;
+      vl[m] = 0.0f;
+      if (VK == 1) vh[m] = ok ? __ldg(val + k) : 0.0f;
+      if (VK == 2) {
+        const float2 d = split_df(ok ? __ldg(vald + k) : 0.0);
+        vh[m] = d.x;
+        vl[m] = d.y;
+      }
+    }
+    float2 x[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+      x[m] = c[m] < 0 ? make_float2(0.0f, 0.0f) : (l2_only ? __ldcg(uf + c[m]) : uf[c[m]]);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) df_accum<VK>(sh, sl, vh[m], vl[m], x[m]);
+  }
+}
+
 // VK: 0 binary (val NULL), 1 float values, 2 double values (split into a float pair).
 template <int VK>
 __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
@@ -163,41 +208,11 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = gridDim.x * (kEcThreads / 32);
   double a0 = 0, a1 = 0, a2 = 0;
-  auto vpair = [&](long long k, float& vh, float& vl) {
-    vh = 1.0f;
-    vl = 0.0f;
-    if (VK == 1) vh = __ldg(val + k);
-    if (VK == 2) {
-      const float2 d = split_df(__ldg(vald + k));
-      vh = d.x;
-      vl = d.y;
-    }
-  };
   for (int row = blockIdx.x * (kEcThreads / 32) + warp; row < n; row += nwarps) {
     long long b = rp[row], e = rp[row + 1];
     if (e > nnz_used) e = nnz_used;
     float sh = 0.0f, sl = 0.0f;
-    long long k = b + lane;
-    // four entries per lane in flight
-    for (; k + 96 < e; k += 128) {
-      int c[4];
-      float vh[4], vl[4];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        c[m] = __ldg(ci + k + 32 * m);
-        vpair(k + 32 * m, vh[m], vl[m]);
-      }
-      float2 x[4];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) x[m] = uf[c[m]];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) df_accum<VK>(sh, sl, vh[m], vl[m], x[m]);
-    }
-    for (; k < e; k += 32) {
-      float vh, vl;
-      vpair(k, vh, vl);
-      df_accum<VK>(sh, sl, vh, vl, uf[__ldg(ci + k)]);
-    }
+    ec_row_accum<VK>(ci, val, vald, uf, b, e, lane, sh, sl, false);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
@@ -252,6 +267,177 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
   }
 }
 
+// ---- persistent form ----------------------------------------------------------
+
+// Grid barrier for a cooperative launch (all blocks co-resident).  Bounded:
+// a wait longer than limit_ns gives up and returns false.
+__device__ __forceinline__ bool grid_barrier(EcState* st, uint64_t limit_ns) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &st->bar_gen;
+    const unsigned int g = *gen;  // the generation cannot advance before this block arrives
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(&st->bar_count, 1u) == gridDim.x - 1) {
+      st->bar_count = 0;
+      __threadfence();
+      atomicAdd(&st->bar_gen, 1u);
+    } else {
+      uint64_t t0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == g) {
+        uint64_t t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > limit_ns) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <int VK>
+__global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
+    int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+    const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
+    double* u, float2* uf, double* parts, EcState* st, int max_iter, double eps) {
+  __shared__ double ws[kEcThreads / 32][3];
+  __shared__ double red[kEcThreads][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = gridDim.x * (kEcThreads / 32);
+  double lam2 = st->lam2, lam_used = 0.0, e1 = 1.0, e2 = 1.0;
+  int it = 0;
+  while (it < max_iter) {
+    const double lam = sqrt(lam2);
+    const double inv = 1.0 / lam;
+    const size_t cur = (size_t)(it & 1) * n, nxt = (size_t)((it + 1) & 1) * n;
+    // the iterate was written by other blocks: read it from L2 (__ldcg), not L1
+    const double* uc = u + cur;
+    const float2* ufc = uf + cur;
+    double a0 = 0, a1 = 0, a2 = 0;
+    for (int row = blockIdx.x * (kEcThreads / 32) + warp; row < n; row += nwarps) {
+      long long b = __ldg(rp + row), e = __ldg(rp + row + 1);
+      if (e > nnz_used) e = nnz_used;
+      float sh = 0.0f, sl = 0.0f;
+      ec_row_accum<VK>(ci, val, vald, ufc, b, e, lane, sh, sl, true);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+        float s2, e2_;
+        two_sum(sh, oh, s2, e2_);
+        sh = s2;
+        sl = __fadd_rn(sl, __fadd_rn(ol, e2_));
+      }
+      if (lane == 0) {
+        const double y = ((double)sh + (double)sl) * inv;
+        const double old = __ldcg(uc + row);
+        u[nxt + row] = y;
+        uf[nxt + row] = split_df(y);
+        a0 += y * y;
+        const double d = y - old, p = y + old;
+        a1 += d * d;
+        a2 += p * p;
+      }
+    }
+    if (lane == 0) {
+      ws[warp][0] = a0;
+      ws[warp][1] = a1;
+      ws[warp][2] = a2;
+    }
+    __syncthreads();
+    double* pp = parts + (size_t)(it & 1) * gridDim.x * 3;
+    if (threadIdx.x == 0) {
+      double t0 = 0, t1 = 0, t2 = 0;
+      for (int w = 0; w < kEcThreads / 32; ++w) {
+        t0 += ws[w][0];
+        t1 += ws[w][1];
+        t2 += ws[w][2];
+      }
+      pp[blockIdx.x * 3 + 0] = t0;
+      pp[blockIdx.x * 3 + 1] = t1;
+      pp[blockIdx.x * 3 + 2] = t2;
+    }
+    if (!grid_barrier(st, 2000000000ull)) {
+      if (threadIdx.x == 0) atomicOr(&st->err, 1);
+      return;
+    }
+    // every block reduces the partials in the same fixed order
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+      s0 += __ldcg(pp + b * 3 + 0);
+      s1 += __ldcg(pp + b * 3 + 1);
+      s2 += __ldcg(pp + b * 3 + 2);
+    }
+    red[threadIdx.x][0] = s0;
+    red[threadIdx.x][1] = s1;
+    red[threadIdx.x][2] = s2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) {
+        red[threadIdx.x][0] += red[threadIdx.x + w][0];
+        red[threadIdx.x][1] += red[threadIdx.x + w][1];
+        red[threadIdx.x][2] += red[threadIdx.x + w][2];
+      }
+      __syncthreads();
+    }
+    lam_used = lam;
+    lam2 = red[0][0];
+    e1 = sqrt(red[0][1]);
+    e2 = sqrt(red[0][2]);
+    __syncthreads();  // red is rewritten in the next iteration
+    ++it;
+    if (e1 <= eps || e2 <= eps) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->lambda_used = lam_used;
+    st->lam2 = lam2;
+    st->e1 = e1;
+    st->e2 = e2;
+    st->iter = it;
+    st->done = 1;
+  }
+}
+
+// The persistent kernel serves small graphs only (n <= kEcCoopMaxN), with at
+// most one block per SM, so a long iteration (a graph that never meets the
+// stop test runs 10,000 of them) occupies a small share of the GPU.  Larger
+// graphs use per-iteration launches: their gathers then hit in L1, which the
+// persistent kernel must bypass.  Returns 0 for "use per-iteration launches".
+constexpr int kEcCoopMaxN = 16384;
+int ec_coop_grid(int n, int sms) {
+  if (n > kEcCoopMaxN) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ec_coop_kernel<1>, kEcThreads, 0) !=
+          cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int want = (n + 8 * (kEcThreads / 32) - 1) / (8 * (kEcThreads / 32));
+  return want < sms ? (want < 1 ? 1 : want) : sms;
+}
+
+// The whole power iteration: parts holds 2 * grid * 3 doubles.
+cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                           const double* vald, long long nnz_used, double* u, float2* uf,
+                           double* parts, void* st, int grid, int max_iter, double eps,
+                           cudaStream_t stream) {
+  EcState* s = (EcState*)st;
+  void* args[] = {&n, &rp, &ci, &val, &vald, &nnz_used, &u, &uf, &parts, &s, &max_iter, &eps};
+  const void* fn = val    ? (const void*)ec_coop_kernel<1>
+                   : vald ? (const void*)ec_coop_kernel<2>
+                          : (const void*)ec_coop_kernel<0>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kEcThreads), args, 0, stream);
+}
+
 size_t ec_state_bytes() { return sizeof(EcState); }
 
 cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
@@ -277,6 +463,8 @@ cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const fl
 }
 
 // Host view of the state block (same layout as EcState).
+int ec_state_err(const void* host_copy) { return ((const EcState*)host_copy)->err; }
+
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done) {
   const EcState* s = (const EcState*)host_copy;

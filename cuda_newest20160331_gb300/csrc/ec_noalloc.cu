@@ -35,6 +35,12 @@ cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const fl
                            int grid, int max_iter, double eps, cudaStream_t stream);
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done);
+int ec_state_err(const void* host_copy);
+int ec_coop_grid(int n, int sms);
+cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                           const double* vald, long long nnz_used, double* u, float2* uf,
+                           double* parts, void* st, int grid, int max_iter, double eps,
+                           cudaStream_t stream);
 }  // namespace bna
 
 namespace {
@@ -114,6 +120,20 @@ extern "C" int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, doub
   alignas(16) unsigned char host_state[kStateDoubles * sizeof(double)];
   double lam2 = 0, lam = 0, e1 = 0, e2 = 0;
   int it = 0, done = 0;
+  // the same choice as bna_ec: small graphs run as one persistent launch
+  // (its 2 x grid x 3 partials fit the partials region: grid <= SM count)
+  const int cgrid = std::min(ec_coop_grid(n, sms), kNoAllocMaxGrid / 2);
+  if (cgrid > 0) {
+    e = launch_ec_coop(n, csr_dev->row_ptr, csr_dev->col_idx, csr_dev->val, nullptr, nnz_used, u,
+                       uf, parts, state, cgrid, max_iter, eps, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(host_state, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return BNA_CUDA_ERROR;
+    if (ec_state_err(host_state)) return BNA_TIMEOUT;
+    ec_state_read(host_state, &lam2, &lam, &e1, &e2, &it, &done);
+    done = 1;
+  }
   const int chunk = 32;
   for (int launched = 0; launched < max_iter && !done; launched += chunk) {
     for (int k = 0; k < chunk; ++k) {

@@ -1,0 +1,371 @@
+// Serving engine: requests (one subject each: BOLD -> CSR -> centrality) are
+// admitted continuously onto a fixed set of worker slots of one GPU.
+//
+// No reference counterpart: the reference builds one subject per process run
+// (CUCorMat, then CUEC on the written .csr).  Here a long-lived server keeps
+// every slot's working memory on the device and runs several subjects at
+// once:
+//   - admission: a queued request is taken by the first free slot as soon as
+//     its device-memory estimate (bna_request_bytes) fits the budget beside
+//     what the other slots hold; requests are considered in arrival order,
+//     and one that does not fit yet does not block smaller ones behind it
+//     (backfill).  Idle slots give their memory back when a waiting request
+//     needs it;
+//   - overlap: each slot has its own context and streams, so the kernels and
+//     copies of different requests interleave on the device; requests with
+//     less work use a higher-priority stream, and correlation passes are cut
+//     into launches of a bounded number of tiles, so the block scheduler can
+//     serve a small request between the launches of a large one;
+//   - results are independent of the mix: each slot's kernels see only their
+//     own request's buffers, and every reduction has a fixed order.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "bna.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+  int64_t id = 0;
+  bna_request req{};
+  bna_reply reply{};
+  int64_t est = 0;
+  double work = 0;  // N^2 T: selects the stream priority
+  bool done = false;
+};
+
+constexpr int kLevels = 6;  // stream priority levels used (fewer if the device has fewer)
+
+struct Slot {
+  int index = 0;
+  bna_ctx* ctx = nullptr;
+  cudaStream_t stream[kLevels] = {};  // stream[0]: highest priority
+  float* bold = nullptr;
+  size_t bold_cap = 0;
+  double* ec = nullptr;
+  size_t ec_cap = 0;
+  int64_t held = 0;        // device bytes this slot holds (accounting)
+  bool busy = false;
+  bool trim = false;       // asked to give its memory back while idle
+  std::thread th;
+};
+
+// Priority level of a request: one level per decade of correlation work
+// N^2 T above 1e10 (N = 4,096, T = 600 is level 0; N = 180,000, T = 1200 the
+// lowest), so smaller requests are served first wherever their kernels and
+// a larger request's wait for the same SMs.
+int level_of(double work, int levels) {
+  int l = 0;
+  for (double w = 1.0e10; work >= w && l < levels - 1; w *= 10.0) ++l;
+  return l;
+}
+// Tiles per correlation launch (about 1 ms of tensor work at T = 1200).
+constexpr int kTilesPerLaunch = 6144;
+
+}  // namespace
+
+struct bna_server {
+  int device = 0;
+  int64_t budget = 0;
+  Clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv;  // queue, slot and completion changes
+  std::deque<Job*> queue;
+  std::map<int64_t, Job*> jobs;
+  int64_t next_id = 1;
+  int levels = 1;
+  bool stop = false;
+  std::vector<Slot*> slots;
+
+  double now() const {
+    return std::chrono::duration<double>(Clock::now() - t0).count();
+  }
+  int64_t held_by_others(const Slot* s) const {
+    int64_t h = 0;
+    for (const Slot* o : slots)
+      if (o != s) h += o->held;
+    return h;
+  }
+};
+
+namespace {
+
+// Grow-only slot buffer, stream-ordered (no wait for other slots' work).
+int32_t grow(void** p, size_t* cap, size_t bytes, cudaStream_t st) {
+  if (*cap >= bytes) return BNA_OK;
+  if (*p) cudaFreeAsync(*p, st);
+  *p = nullptr;
+  *cap = 0;
+  if (cudaMallocAsync(p, bytes, st) != cudaSuccess) {
+    cudaGetLastError();
+    return BNA_OOM;
+  }
+  *cap = bytes;
+  return BNA_OK;
+}
+
+int64_t slot_bytes(const Slot* s) {
+  return bna_ctx_arena_bytes(s->ctx) + (int64_t)s->bold_cap + (int64_t)s->ec_cap;
+}
+
+void release_slot_memory(Slot* s) {
+  bna_ctx_trim(s->ctx);
+  if (s->bold) cudaFreeAsync(s->bold, s->stream[0]);
+  if (s->ec) cudaFreeAsync(s->ec, s->stream[0]);
+  cudaStreamSynchronize(s->stream[0]);
+  s->bold = nullptr;
+  s->ec = nullptr;
+  s->bold_cap = s->ec_cap = 0;
+}
+
+// One request on one slot.
+void run_job(bna_server* srv, Slot* s, Job* j) {
+  const bna_request& r = j->req;
+  bna_reply& out = j->reply;
+  cudaStream_t st = s->stream[level_of(j->work, srv->levels)];
+  const size_t bytes = (size_t)r.N * r.T * sizeof(float);
+  int32_t rc = grow(reinterpret_cast<void**>(&s->bold), &s->bold_cap, bytes, st);
+  if (rc == BNA_OK && cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) !=
+                          cudaSuccess)
+    rc = BNA_CUDA_ERROR;
+  bna_csr csr{};
+  if (rc == BNA_OK) {
+    // no CSR larger than the caller's buffers is built (a cap of 0 admits
+    // only the empty graph)
+    bna_ctx_set_option(s->ctx, BNA_OPT_MAX_NNZ, r.cap > 0 ? r.cap : 1);
+    rc = bna_corr_csr(s->ctx, s->bold, r.N, r.T, &r.opts, &csr, &out.stats, st);
+    out.nnz = rc == BNA_OK || rc == BNA_CAPACITY ? out.stats.nnz : 0;
+    if (rc == BNA_OK && csr.nnz > r.cap) rc = BNA_CAPACITY;
+  }
+  if (rc == BNA_OK && r.row_ptr_host) {  // without host buffers the CSR stays on the device
+    bool ok = cudaMemcpyAsync(r.row_ptr_host, csr.row_ptr, (size_t)(r.N + 1) * 4,
+                              cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    if (csr.nnz > 0 && r.col_idx_host) {
+      ok = ok && cudaMemcpyAsync(r.col_idx_host, csr.col_idx, (size_t)csr.nnz * 4,
+                                 cudaMemcpyDeviceToHost, st) == cudaSuccess;
+      if (r.val_host && csr.val)
+        ok = ok && cudaMemcpyAsync(r.val_host, csr.val, (size_t)csr.nnz * 4,
+                                   cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    }
+    if (!ok) rc = BNA_CUDA_ERROR;
+  }
+  if (rc == BNA_OK && r.ec_max_iter > 0) {
+    rc = grow(reinterpret_cast<void**>(&s->ec), &s->ec_cap, (size_t)r.N * sizeof(double), st);
+    if (rc == BNA_OK) {
+      double lam = 0;
+      int32_t it = 0;
+      const int32_t e = bna_ec(s->ctx, &csr, r.ec_max_iter, r.ec_eps, s->ec, &lam, &it, st);
+      if (e == BNA_OK || e == BNA_NOT_CONVERGED) {
+        out.lambda = lam;
+        out.ec_iters = it;
+        out.ec_converged = e == BNA_OK;
+        if (r.ec_host && cudaMemcpyAsync(r.ec_host, s->ec, (size_t)r.N * sizeof(double),
+                                         cudaMemcpyDeviceToHost, st) != cudaSuccess)
+          rc = BNA_CUDA_ERROR;
+      } else {
+        rc = e;
+      }
+    }
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess && rc == BNA_OK) rc = BNA_CUDA_ERROR;
+  out.status = rc;
+}
+
+// First queued job that fits beside the other slots' memory (arrival order,
+// with backfill; once the oldest request has waited kMaxBypass seconds, later
+// ones no longer pass it).  Caller holds the lock.
+constexpr double kMaxBypass = 0.5;
+Job* pick(bna_server* srv, Slot* s) {
+  const int64_t others = srv->held_by_others(s);
+  const double now = srv->now();
+  for (auto it = srv->queue.begin(); it != srv->queue.end(); ++it) {
+    Job* j = *it;
+    if (others + std::max(s->held, j->est) <= srv->budget) {
+      srv->queue.erase(it);
+      return j;
+    }
+    if (now - j->reply.t_submit > kMaxBypass) break;
+  }
+  return nullptr;
+}
+
+void worker(bna_server* srv, Slot* s) {
+  cudaSetDevice(srv->device);
+  std::unique_lock<std::mutex> lk(srv->mu);
+  for (;;) {
+    if (s->trim) {
+      s->trim = false;
+      lk.unlock();
+      release_slot_memory(s);
+      lk.lock();
+      s->held = 0;
+      srv->cv.notify_all();
+      continue;
+    }
+    Job* j = pick(srv, s);
+    if (!j) {
+      if (srv->stop && srv->queue.empty()) break;
+      // a waiting request that does not fit: idle slots (this one included)
+      // give their memory back
+      if (!srv->queue.empty())
+        for (Slot* o : srv->slots)
+          if (!o->busy && o->held > 0) o->trim = true;
+      if (s->trim) continue;
+      srv->cv.notify_all();
+      // bounded wait: the bypass limit above changes with time alone
+      srv->cv.wait_for(lk, std::chrono::milliseconds(50));
+      continue;
+    }
+    s->busy = true;
+    s->held = std::max(s->held, j->est);
+    j->reply.t_start = srv->now();
+    j->reply.slot = s->index;
+    lk.unlock();
+    run_job(srv, s, j);
+    lk.lock();
+    j->reply.t_done = srv->now();
+    s->held = slot_bytes(s);
+    s->busy = false;
+    j->done = true;
+    srv->cv.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_bytes,
+                          bna_server** out) {
+  if (!out || slots < 1 || slots > 64 || hbm_budget_bytes <= 0) return BNA_BAD_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return BNA_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return BNA_BAD_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return BNA_CUDA_ERROR;
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return BNA_CUDA_ERROR;
+  bna_server* srv = new bna_server();
+  srv->device = device;
+  srv->budget = hbm_budget_bytes;
+  srv->t0 = Clock::now();
+  // numerically lower = higher priority; greatest <= least
+  srv->levels = std::min(kLevels, least - greatest + 1);
+  int32_t rc = BNA_OK;
+  for (int i = 0; i < slots && rc == BNA_OK; ++i) {
+    Slot* s = new Slot();
+    s->index = i;
+    srv->slots.push_back(s);
+    rc = bna_ctx_create(device, &s->ctx);
+    for (int l = 0; l < srv->levels && rc == BNA_OK; ++l)
+      if (cudaStreamCreateWithPriority(&s->stream[l], cudaStreamNonBlocking, greatest + l) !=
+          cudaSuccess)
+        rc = BNA_CUDA_ERROR;
+    if (rc == BNA_OK) rc = bna_ctx_set_option(s->ctx, BNA_OPT_TILES_PER_LAUNCH, kTilesPerLaunch);
+  }
+  if (rc != BNA_OK) {
+    for (Slot* s : srv->slots) {
+      for (cudaStream_t& q : s->stream)
+        if (q) cudaStreamDestroy(q);
+      if (s->ctx) bna_ctx_destroy(s->ctx);
+      delete s;
+    }
+    delete srv;
+    return rc;
+  }
+  for (Slot* s : srv->slots) s->th = std::thread(worker, srv, s);
+  *out = srv;
+  return BNA_OK;
+}
+
+int32_t bna_server_submit(bna_server* srv, const bna_request* req, int64_t* ticket) {
+  if (!srv || !req || !ticket || !req->bold_host || req->N < 2 || req->T < 1 || req->cap < 0 ||
+      (req->row_ptr_host && req->cap > 0 && !req->col_idx_host))
+    return BNA_BAD_ARG;
+  const int64_t est = bna_request_bytes(req->N, req->T, &req->opts, req->cap,
+                                        req->ec_max_iter > 0 ? 1 : 0);
+  if (est < 0) return BNA_BAD_ARG;
+  if (est > srv->budget) return BNA_OVER_BUDGET;
+  Job* j = new Job();
+  j->req = *req;
+  j->est = est;
+  j->work = (double)req->N * req->N * req->T;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  if (srv->stop) {
+    delete j;
+    return BNA_BAD_ARG;
+  }
+  j->id = srv->next_id++;
+  j->reply.tag = req->tag;
+  j->reply.t_submit = srv->now();
+  srv->jobs[j->id] = j;
+  srv->queue.push_back(j);
+  *ticket = j->id;
+  srv->cv.notify_all();
+  return BNA_OK;
+}
+
+int32_t bna_server_wait(bna_server* srv, int64_t ticket, double timeout_s, bna_reply* reply) {
+  if (!srv || !reply) return BNA_BAD_ARG;
+  std::unique_lock<std::mutex> lk(srv->mu);
+  auto it = srv->jobs.find(ticket);
+  if (it == srv->jobs.end()) return BNA_BAD_ARG;
+  Job* j = it->second;
+  auto done = [&] { return j->done; };
+  if (timeout_s < 0) {
+    srv->cv.wait(lk, done);
+  } else if (!srv->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+    return BNA_TIMEOUT;
+  }
+  *reply = j->reply;
+  srv->jobs.erase(it);
+  delete j;
+  return BNA_OK;
+}
+
+int64_t bna_server_device_bytes(const bna_server* srv) {
+  if (!srv) return -1;
+  bna_server* s = const_cast<bna_server*>(srv);
+  std::lock_guard<std::mutex> lk(s->mu);
+  int64_t h = 0;
+  for (const Slot* o : s->slots) h += o->held;
+  return h;
+}
+
+int32_t bna_server_destroy(bna_server* srv) {
+  if (!srv) return BNA_BAD_ARG;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stop = true;
+    srv->cv.notify_all();
+  }
+  for (Slot* s : srv->slots)
+    if (s->th.joinable()) s->th.join();
+  cudaSetDevice(srv->device);
+  for (Slot* s : srv->slots) {
+    release_slot_memory(s);
+    for (cudaStream_t& q : s->stream)
+      if (q) cudaStreamDestroy(q);
+    bna_ctx_destroy(s->ctx);
+    delete s;
+  }
+  for (auto& kv : srv->jobs) delete kv.second;
+  delete srv;
+  return BNA_OK;
+}
+
+}  // extern "C"

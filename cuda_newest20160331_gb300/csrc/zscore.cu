@@ -7,36 +7,52 @@
 //   z_t  = float((double(x_t) - mean) / norm)
 // so that z_i . z_j is the Pearson r.
 //
-// FP64 throughput on this GPU is ~1/70 of FP32, so the kernel keeps only the
-// double operations whose rounding matters and does the rest exactly with
-// integer arithmetic:
+// FP64 throughput on this GPU is ~1/70 of FP32, so the double operations
+// are limited to those whose rounding matters:
 //   * the time-order double sum of floats equals their exact sum whenever
 //     sum |x_t| < 2^53 units of the smallest ulp among the x_t (every partial
 //     sum is then representable); it is accumulated exactly in int64 fixed
 //     point, with the sequential double sum as fallback otherwise;
 //   * float -> double conversions are exact bit manipulations;
-//   * z = RN_float(d * RN(1/norm)): the double product is within 3 double ulps
-//     of the correctly rounded quotient d / norm, so it rounds to the same
-//     float unless it lies within 8 double ulps of a float rounding midpoint
-//     (or in the float subnormal range) — exactly those elements redo the IEEE
-//     division; the float rounding itself is done on the bits.
-//   The centred sum of squares keeps its sequential double adds.
+//   * the centred sum of squares keeps its sequential double adds;
+//   * z itself is computed in float-float arithmetic (TwoSum / FMA-based
+//     TwoProduct, Knuth and Dekker): q' ~ (x - mean) / norm with a rigorous
+//     error bound B; whenever [q' - B, q' + B] holds no float rounding
+//     midpoint, RN_float of the reference's double quotient is the float part
+//     of q'.  The few elements that fail the test (about 2^-19 of them) take
+//     the exact double path: z = RN_float(d * RN(1/norm)), which rounds like
+//     the correctly rounded quotient unless it lies within 8 double ulps of a
+//     float rounding midpoint (or in the float subnormal range), where the
+//     IEEE division is redone; the float rounding is done on the bits.
 //
-// Layout: one thread per voxel, 64 voxels per block; every pass reads the
-// time-major input coalesced (a warp reads 128 consecutive bytes per time
-// step, several steps in flight).  Pass 1 finds the smallest ulp exponent and
-// the exact int64 sum together (the accumulator is rescaled when a smaller
-// exponent appears); pass 2 runs the sequential centred sum of squares;
-// pass 3 writes the voxel-major rows (z FP32, BF16 hi = bf16(z),
-// lo = bf16(z - hi)) through a 32-step shared-memory transpose so each warp
-// store covers 32 consecutive t of one voxel.  bad[i] = 1 when z has a NaN.
+// Two kernels:
+//   zscore_stats_kernel  one thread per voxel: pass 1 finds the smallest ulp
+//                        exponent and the exact int64 sum together (the
+//                        accumulator is rescaled when a smaller exponent
+//                        appears); pass 2 runs the sequential centred sum of
+//                        squares.  Reads are coalesced (a warp reads 128
+//                        consecutive bytes per time step).
+//   zscore_emit_kernel   one element per thread-step over 32 voxels x 32
+//                        steps tiles: reads coalesced along voxels, computes
+//                        z, and writes the voxel-major rows (z FP32, BF16
+//                        hi = bf16(z), lo = bf16(z - hi)) through a shared-
+//                        memory transpose.  bad[i] = 1 when z has a NaN.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
 
 namespace bna {
 
-constexpr int kZV = 64;  // voxels per block = threads per block
+constexpr int kZStatThreads = 128;
+constexpr int kZEmitT = 256;  // time steps per emit block (8 chunks of 32)
+
+// Per-voxel statistics handed from the stats kernel to the emit kernel.
+struct VoxStat {
+  double mean, nrm, inv;  // reference mean, norm and RN(1 / norm)
+  float m0, m1, m2;       // mean = m0 + m1 + m2 exactly (float split)
+  float ih, il;           // inv ~ ih + il (relative error <= 2^-48)
+  int fast;               // the float-float path applies to this voxel
+};
 
 // Exact float -> double on the bits (normal floats); other classes by the cvt.
 __device__ __forceinline__ double f2d_exact(float x) {
@@ -65,56 +81,63 @@ __device__ __forceinline__ float zdiv(double d, double nrm, double inv) {
   return __uint_as_float(f);
 }
 
-__global__ __launch_bounds__(kZV) void zscore_kernel(const float* __restrict__ bold, int N, int T,
-                                                    int n_pad, float* __restrict__ z, int ldz,
-                                                    uint16_t* __restrict__ zhi,
-                                                    uint16_t* __restrict__ zlo, int ldb,
-                                                    uint8_t* __restrict__ bad) {
-  __shared__ float tile[32][kZV + 1];  // tile[tt][v]: z of voxel v0+v at time t0+tt
-  const int v = threadIdx.x, lane = v & 31, warp = v >> 5;
-  const int v0 = blockIdx.x * kZV;
-  const int gv = v0 + v;
-  const bool live = gv < N;
-  const float* col = bold + (live ? gv : 0);  // x_t = col[t * N]
-
-  double mean = 0.0, nrm = 1.0, inv = 1.0;
-  if (live) {
+__global__ __launch_bounds__(kZStatThreads) void zscore_stats_kernel(
+    const float* __restrict__ bold, int N, int T, int n_pad, VoxStat* __restrict__ vs,
+    uint8_t* __restrict__ bad) {
+  const int gv = blockIdx.x * kZStatThreads + threadIdx.x;
+  if (gv >= n_pad) return;
+  VoxStat o;
+  o.mean = 0.0;
+  o.nrm = 1.0;
+  o.inv = 1.0;
+  o.m0 = o.m1 = o.m2 = 0.0f;
+  o.ih = 1.0f;
+  o.il = 0.0f;
+  o.fast = 1;
+  if (gv < N) {
+    const float* col = bold + gv;  // x_t = col[t * N]
     // 1. exact sum: int64 fixed point in units of 2^e0, e0 = smallest ulp
     //    exponent so far (the accumulator is shifted when e0 drops); exact
     //    while every value is normal and sum |x| < 2^53 units of the final e0
     constexpr int kNone = 1 << 20;
+    constexpr int kPf = 16;  // loads in flight per thread
     int e0 = kNone;
     long long acc = 0, mag = 0;
     bool exact = true;
-#pragma unroll 8
-    for (int t = 0; t < T; ++t) {
-      const uint32_t b = __float_as_uint(__ldg(col + (size_t)t * N));
-      const int e8 = (int)((b >> 23) & 0xFFu);
-      const uint32_t mant = b & 0x7FFFFFu;
-      if (e8 == 0xFF || (e8 == 0 && mant)) exact = false;  // inf / nan / subnormal
-      if (e8 == 0 || !exact) continue;
-      const int ue = e8 - 150;  // value = (mant | 2^23) * 2^ue
-      if (ue < e0) {
-        if (e0 != kNone) {
-          const int sh = e0 - ue;
-          if (sh >= 53 || (mag >> (53 - sh)) != 0) {
-            exact = false;
-            continue;
+    for (int t0 = 0; t0 < T; t0 += kPf) {
+      float xs[kPf];
+#pragma unroll
+      for (int k = 0; k < kPf; ++k) xs[k] = (t0 + k < T) ? __ldg(col + (size_t)(t0 + k) * N) : 0.0f;
+#pragma unroll
+      for (int k = 0; k < kPf; ++k) {
+        const uint32_t b = __float_as_uint(xs[k]);  // padding zeros add nothing
+        const int e8 = (int)((b >> 23) & 0xFFu);
+        const uint32_t mant = b & 0x7FFFFFu;
+        if (e8 == 0xFF || (e8 == 0 && mant)) exact = false;  // inf / nan / subnormal
+        if (e8 == 0 || !exact) continue;
+        const int ue = e8 - 150;  // value = (mant | 2^23) * 2^ue
+        if (ue < e0) {
+          if (e0 != kNone) {
+            const int sh = e0 - ue;
+            if (sh >= 53 || (mag >> (53 - sh)) != 0) {
+              exact = false;
+              continue;
+            }
+            acc <<= sh;
+            mag <<= sh;
           }
-          acc <<= sh;
-          mag <<= sh;
+          e0 = ue;
         }
-        e0 = ue;
+        const int sh = ue - e0;
+        if (sh > 29) {
+          exact = false;
+          continue;
+        }
+        const long long m = (long long)(mant | 0x800000u) << sh;
+        mag += m;
+        if (mag >= (1LL << 53)) exact = false;
+        acc += (b >> 31) ? -m : m;
       }
-      const int sh = ue - e0;
-      if (sh > 29) {
-        exact = false;
-        continue;
-      }
-      const long long m = (long long)(mant | 0x800000u) << sh;
-      mag += m;
-      if (mag >= (1LL << 53)) exact = false;
-      acc += (b >> 31) ? -m : m;
     }
     double s1;
     if (exact) {
@@ -124,35 +147,116 @@ __global__ __launch_bounds__(kZV) void zscore_kernel(const float* __restrict__ b
       s1 = 0.0;
       for (int t = 0; t < T; ++t) s1 = __dadd_rn(s1, (double)__ldg(col + (size_t)t * N));
     }
-    mean = __ddiv_rn(s1, (double)T);
+    const double mean = __ddiv_rn(s1, (double)T);
     // 2. centred sum of squares, sequential double adds in time order
     double s2 = 0.0;
-#pragma unroll 8
-    for (int t = 0; t < T; ++t) {
-      const double dd = __dsub_rn(f2d_exact(__ldg(col + (size_t)t * N)), mean);
-      s2 = __dadd_rn(s2, __dmul_rn(dd, dd));
+    for (int t0 = 0; t0 < T; t0 += kPf) {
+      float xs[kPf];
+#pragma unroll
+      for (int k = 0; k < kPf; ++k) xs[k] = (t0 + k < T) ? __ldg(col + (size_t)(t0 + k) * N) : 0.0f;
+#pragma unroll
+      for (int k = 0; k < kPf; ++k) {
+        if (t0 + k < T) {
+          const double dd = __dsub_rn(f2d_exact(xs[k]), mean);
+          s2 = __dadd_rn(s2, __dmul_rn(dd, dd));
+        }
+      }
     }
-    nrm = __dsqrt_rn(s2);
-    inv = __drcp_rn(nrm);
+    o.mean = mean;
+    o.nrm = __dsqrt_rn(s2);
+    o.inv = __drcp_rn(o.nrm);
+    // float splits for the emit kernel's float-float path
+    o.m0 = __double2float_rn(mean);
+    const double r1 = __dsub_rn(mean, (double)o.m0);
+    o.m1 = __double2float_rn(r1);
+    o.m2 = __double2float_rn(__dsub_rn(r1, (double)o.m1));
+    o.ih = __double2float_rn(o.inv);
+    o.il = __double2float_rn(__dsub_rn(o.inv, (double)o.ih));
+    const double back = __dadd_rn(__dadd_rn((double)o.m0, (double)o.m1), (double)o.m2);
+    const float aih = fabsf(o.ih);
+    o.fast = (back == mean) && isfinite(mean) && o.nrm > 0.0 && isfinite(o.nrm) &&
+             aih >= 1.0e-30f && aih <= 1.0e30f && (fabsf(o.m0) <= 1.0e30f) &&
+             (o.m0 == 0.0f || fabsf(o.m0) >= 1.0e-30f);
   }
+  vs[gv] = o;
+  bad[gv] = 0;
+}
 
-  // 3. voxel-major rows, 32 steps at a time through the transpose tile
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void zs_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// The reference's z of one element: the float-float path when it is provably
+// right, else the exact double path.
+__device__ __forceinline__ float z_of(float x, const VoxStat& v) {
+  if (v.fast && isfinite(x)) {
+    // d = x - mean as (dh, dl): x - m0 exactly (TwoSum), then the small terms
+    float s, e;
+    zs_two_sum(x, -v.m0, s, e);
+    const float t = __fsub_rn(__fsub_rn(e, v.m1), v.m2);
+    float dh, dl;
+    zs_two_sum(s, t, dh, dl);
+    // q' = (dh + dl) * (ih + il): exact head product, FMA-accumulated tail
+    const float ph = __fmul_rn(dh, v.ih);
+    float pe = __fmaf_rn(dh, v.ih, -ph);
+    pe = __fmaf_rn(dh, v.il, pe);
+    pe = __fmaf_rn(dl, v.ih, pe);
+    const float qh = __fadd_rn(ph, pe);
+    const float ql = __fsub_rn(pe, __fsub_rn(qh, ph));
+    // error bound of q' against the reference's double quotient: relative
+    // terms (inv split, dropped dl*il, tail roundings, the reference's two
+    // roundings) below 2^-44 |q|, plus the error of d, below
+    // 2^-46 (|x| + |mean|), times inv
+    const uint32_t qb = __float_as_uint(qh);
+    const uint32_t e8 = (qb >> 23) & 0xFFu;
+    if (e8 >= 25u && e8 <= 253u && (qb & 0x7FFFFFu) != 0u) {
+      const float half_ulp = __uint_as_float((e8 - 24u) << 23);
+      const float bound = fabsf(qh) * 5.6843419e-14f /* 2^-44 */ +
+                          (fabsf(x) + fabsf(v.m0)) * fabsf(v.ih) * 2.8421709e-14f /* 2^-45 */;
+      if (half_ulp - fabsf(ql) > bound) return qh;
+    }
+  }
+  return zdiv(__dsub_rn(f2d_exact(x), v.mean), v.nrm, v.inv);
+}
+
+__global__ __launch_bounds__(256) void zscore_emit_kernel(
+    const float* __restrict__ bold, int N, int T, const VoxStat* __restrict__ vs,
+    float* __restrict__ z, int ldz, uint16_t* __restrict__ zhi, uint16_t* __restrict__ zlo,
+    int ldb, uint8_t* __restrict__ bad) {
+  __shared__ float tile[32][33];  // tile[tt][v]: z of voxel v0+v at time t0+tt
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int v0 = blockIdx.x * 32;
+  const int gv = v0 + lane;
+  const bool live = gv < N;
+  const VoxStat st = vs[gv];  // gv < n_pad: the grid covers n_pad / 32 groups
   const int tmax = ldz > ldb ? ldz : ldb;
+  const int tb = blockIdx.y * kZEmitT;
   bool nan_seen = false;
-  for (int t0 = 0; t0 < tmax; t0 += 32) {
-#pragma unroll 8
-    for (int tt = 0; tt < 32; ++tt) {
-      const int t = t0 + tt;
+  for (int t0 = tb; t0 < tb + kZEmitT && t0 < tmax; t0 += 32) {
+    float xs[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int t = t0 + warp + 8 * k;
+      xs[k] = (live && t < T) ? __ldg(bold + (size_t)t * N + gv) : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int tt = warp + 8 * k, t = t0 + tt;
       float zz = 0.0f;
       if (live && t < T) {
-        zz = zdiv(__dsub_rn(f2d_exact(__ldg(col + (size_t)t * N)), mean), nrm, inv);
+        zz = z_of(xs[k], st);
         nan_seen |= (zz != zz);
       }
-      tile[tt][v] = zz;
+      tile[tt][lane] = zz;
     }
     __syncthreads();
-    // warp w writes voxels w, w+2, ...: lane = time step within the chunk
-    for (int vv = warp; vv < kZV; vv += kZV / 32) {
+    // warp w writes voxels w, w+8, w+16, w+24; lane = time step in the chunk
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int vv = warp + 8 * k;
       const size_t gi = (size_t)v0 + vv;
       const int t = t0 + lane;
       const float zz = tile[lane][vv];
@@ -166,15 +270,24 @@ __global__ __launch_bounds__(kZV) void zscore_kernel(const float* __restrict__ b
     }
     __syncthreads();
   }
-  if (gv < n_pad) bad[gv] = nan_seen ? 1 : 0;
+  if (nan_seen) bad[gv] = 1;
 }
 
+size_t zscore_scratch_bytes(int n_pad) { return (size_t)n_pad * sizeof(VoxStat); }
+
+// scratch: zscore_scratch_bytes(n_pad) bytes of device memory.
 cudaError_t launch_zscore(const float* bold, int N, int T, int n_pad, float* z, int ldz,
-                          uint16_t* zhi, uint16_t* zlo, int ldb, uint8_t* bad,
+                          uint16_t* zhi, uint16_t* zlo, int ldb, uint8_t* bad, void* scratch,
                           cudaStream_t stream) {
-  if (n_pad % kZV != 0 || ldz % 32 != 0 || (zhi && ldb % 32 != 0)) return cudaErrorInvalidValue;
-  const int grid = n_pad / kZV;
-  zscore_kernel<<<grid, kZV, 0, stream>>>(bold, N, T, n_pad, z, ldz, zhi, zlo, zhi ? ldb : 0, bad);
+  if (n_pad % 128 != 0 || ldz % 32 != 0 || (zhi && ldb % 32 != 0) || !scratch)
+    return cudaErrorInvalidValue;
+  VoxStat* vs = static_cast<VoxStat*>(scratch);
+  zscore_stats_kernel<<<n_pad / kZStatThreads, kZStatThreads, 0, stream>>>(bold, N, T, n_pad, vs,
+                                                                           bad);
+  const int ldbv = zhi ? ldb : 0;
+  const int tmax = ldz > ldbv ? ldz : ldbv;
+  const dim3 grid(n_pad / 32, (tmax + kZEmitT - 1) / kZEmitT);
+  zscore_emit_kernel<<<grid, 256, 0, stream>>>(bold, N, T, vs, z, ldz, zhi, zlo, ldbv, bad);
   return cudaGetLastError();
 }
 

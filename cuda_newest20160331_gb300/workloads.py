@@ -6,8 +6,13 @@ not distributed).  Sizes follow the reference's typical runs (N up to
   small      N=4,096   T=240  K=20  r >= 0.5, binary CSR, then centrality
   n45k       N=45,000  T=240  K=40  1 % density: tau = the FP64 quantile
              (tests/golden/workload_tau.json), weighted CSR
+  n45k_density  the same subject through the exact density rule (1 %)
   n180k      N=180,000 T=1200 K=60  block-network loadings (500-voxel blocks),
              tau = 0.4, weighted CSR, then centrality
+  serving    Poisson arrivals at 4 requests/s; each request a subject with N
+             log-uniform in [4,096, 180,000], T in {240, 600, 1200}, threshold
+             r >= tau (tau uniform in [0.3, 0.6]) or a density uniform in
+             [0.1 %, 2 %]; corr -> CSR -> centrality
 """
 from __future__ import annotations
 
@@ -47,7 +52,43 @@ def get(name: str) -> Workload:
         return Workload("small", 4096, 240, 20, 1, "r_ge", 0.5, False)
     if name == "n45k":
         return Workload("n45k", 45000, 240, 40, 2, "r_ge", n45k_tau(), True)
+    if name == "n45k_density":
+        return Workload("n45k_density", 45000, 240, 40, 2, "density", 1.0, True)
     if name == "n180k":
         return Workload("n180k", 180000, 1200, 60, 3, "r_ge", 0.4, True, kind="blocknet",
                         synth={"load_sd": 0.117, "jitter_sd": 0.08, "block": 500, "n_net": 60})
     raise KeyError(name)
+
+
+@dataclass
+class ServeRequest:
+    arrival: float   # seconds after the start of the run
+    subject: int     # index into the subject pool
+    mode: str
+    value: float
+
+
+def serving(n_requests: int, rate: float = 4.0, seed: int = 5000, pool: int = 24,
+            n_min: int = 4096, n_max: int = 180000):
+    """-> (subjects [(N, T, K, seed)], requests [ServeRequest]).
+
+    Requests draw their subject from a pool of `pool` distinct seeded subjects
+    (generating a fresh 180k x 1200 series per request would dominate the
+    run); every request is computed from scratch."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    subjects = []
+    for k in range(pool):
+        N = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        T = int(rng.choice([240, 600, 1200]))
+        subjects.append((N, T, 40, seed + 1 + k))
+    t = 0.0
+    reqs = []
+    for _ in range(n_requests):
+        t += float(rng.exponential(1.0 / rate))
+        subj = int(rng.integers(pool))
+        if rng.random() < 0.5:
+            reqs.append(ServeRequest(t, subj, "r_ge", float(rng.uniform(0.3, 0.6))))
+        else:
+            reqs.append(ServeRequest(t, subj, "density", float(rng.uniform(0.1, 2.0))))
+    return subjects, reqs

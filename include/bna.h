@@ -44,7 +44,8 @@ typedef enum bna_status {
   BNA_INTERNAL = 10,          /* an internal consistency check failed */
   BNA_UNSUPPORTED = 11,
   BNA_SCRATCH_LIMIT = 12,     /* problem larger than bna_ec_noalloc's fixed scratch */
-  BNA_CAPACITY = 13           /* caller's output buffers too small (required size reported) */
+  BNA_CAPACITY = 13,          /* caller's output buffers too small (required size reported) */
+  BNA_OVER_BUDGET = 14        /* request needs more device memory than the server's budget */
 } bna_status;
 
 /* Threshold rules.  r below is the reference's value after post_block
@@ -117,6 +118,18 @@ const char* bna_ctx_last_error(const bna_ctx* ctx);
 int32_t bna_ctx_trim(bna_ctx* ctx);
 /* Bytes currently held by the arena. */
 int64_t bna_ctx_arena_bytes(const bna_ctx* ctx);
+
+/* Context options (bna_ctx_set_option).  No reference counterpart: the
+ * reference runs one subject per process.
+ *   BNA_OPT_TILES_PER_LAUNCH: split each tensor-core correlation pass into
+ *     launches of at most this many 128 x 256 tiles (0 = one launch), so that
+ *     work of other streams - other requests of a server - can be scheduled
+ *     between them;
+ *   BNA_OPT_MAX_NNZ: bna_corr_csr returns BNA_CAPACITY (stats->nnz = the
+ *     required size) instead of building a CSR with more entries (0 = no
+ *     limit). */
+typedef enum bna_option { BNA_OPT_TILES_PER_LAUNCH = 0, BNA_OPT_MAX_NNZ = 1 } bna_option;
+int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value);
 
 /* Z-score, the prologue of CorMat_gpu / CorMat_cpu (W/CorMat/CUCorMat/CUCorMat/CorMat.cu:24-52,
  * CorMat.cpp:923-951): per voxel mean and centred L2 norm in double, summed in time
@@ -204,6 +217,65 @@ int32_t bna_csr_write(const char* path, const bna_csr* csr_host);
 int32_t bna_csr_read(const char* path, bna_csr* csr_host_out);
 /* _ec.nm file (weighted-net.cu:309-318): int32 N; float ec[N]. */
 int32_t bna_ec_write(const char* path, const double* ec_host, int32_t N);
+
+/* Serving engine.  No reference counterpart (the reference builds one
+ * subject per process run).  A server owns `slots` workers on one GPU, each
+ * with its own context and CUDA streams.  Submitted requests wait in arrival
+ * order and are admitted as soon as a slot is free and their device-memory
+ * estimate (bna_request_bytes) fits the HBM budget next to the memory the
+ * other slots hold (continuous batching: requests that arrive while others
+ * run join them on the device; their kernels overlap).  A request larger than
+ * the whole budget is refused at submission (BNA_OVER_BUDGET).  Each request
+ * runs bna_corr_csr and, if ec_max_iter > 0, bna_ec on the resulting CSR;
+ * its results go to the caller's host buffers, like bna_corr_csr_host_into.
+ * Requests with less work run on higher-priority streams, and correlation
+ * passes are split into bounded launches, so a small request does not wait
+ * for a large one to finish.  Results do not depend on what else runs. */
+typedef struct bna_server bna_server;
+typedef struct bna_request {
+  const float* bold_host; /* time-major [T][N]; must stay valid until the reply */
+  int32_t N, T;
+  bna_corr_opts opts;
+  int32_t ec_max_iter;    /* 0: no centrality */
+  double ec_eps;
+  int32_t* row_ptr_host;  /* N + 1, or NULL: the CSR is not copied back (only consumed
+                             on the device by the centrality) */
+  int32_t* col_idx_host;  /* cap */
+  float* val_host;        /* cap, or NULL (binary graph or values not wanted) */
+  int64_t cap;            /* largest CSR (entries) the request may build: the size of the
+                             caller's buffers; also bounds its device memory */
+  double* ec_host;        /* N, or NULL */
+  int64_t tag;            /* caller's value, returned in the reply */
+} bna_request;
+typedef struct bna_reply {
+  int32_t status;         /* bna_status of the request (BNA_CAPACITY: nnz > cap) */
+  int32_t slot;           /* worker that ran it */
+  int64_t tag;
+  int64_t nnz;            /* directed entries (the required cap on BNA_CAPACITY) */
+  double lambda;          /* centrality eigenvalue (0 without centrality) */
+  int32_t ec_iters;
+  int32_t ec_converged;
+  double t_submit, t_start, t_done; /* seconds since the server was created */
+  bna_corr_stats stats;
+} bna_reply;
+int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_bytes,
+                          bna_server** out);
+/* Queue a request; *ticket identifies it for bna_server_wait. */
+int32_t bna_server_submit(bna_server* srv, const bna_request* req, int64_t* ticket);
+/* Block until the request is done (timeout_s < 0: no limit); fills *reply
+ * and forgets the ticket.  BNA_TIMEOUT if it is still running at the limit. */
+int32_t bna_server_wait(bna_server* srv, int64_t ticket, double timeout_s, bna_reply* reply);
+/* Device bytes the server's slots hold right now. */
+int64_t bna_server_device_bytes(const bna_server* srv);
+/* Finish the queued requests and release everything. */
+int32_t bna_server_destroy(bna_server* srv);
+/* Directed entries of the CSR the density rule (BNA_THR_DENSITY) builds for
+ * N voxels at `percent`: Clength of W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:327-328
+ * (the reference's float x double arithmetic, rounded up to even). */
+int64_t bna_density_nnz(int32_t N, double percent);
+/* Upper estimate of the device memory one request needs (admission rule). */
+int64_t bna_request_bytes(int32_t N, int32_t T, const bna_corr_opts* opts, int64_t cap,
+                          int32_t with_ec);
 
 /* Deterministic synthetic BOLD (factor model), float32 time-major [T][N]. */
 typedef enum bna_synth_kind { BNA_SYNTH_IID = 0, BNA_SYNTH_BLOCKNET = 1 } bna_synth_kind;

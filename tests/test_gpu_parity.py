@@ -76,6 +76,25 @@ def test_zscore_bit_exact(builder):
         assert np.array_equal(z[:, :T], ref, equal_nan=True), (N, T)
 
 
+@pytest.mark.parametrize("kind", ["offset", "integer", "scaled"])
+def test_zscore_bit_exact_scanner_like_series(builder, kind):
+    """Scanner-like series: large baselines with small fluctuations (heavy
+    cancellation in x - mean), integer-valued samples (structured values, many
+    exact quotients), and per-voxel scales over many decades."""
+    N, T = 4000, 300
+    rng = np.random.default_rng({"offset": 11, "integer": 12, "scaled": 13}[kind])
+    b = bna.synth_bold(N, T, 20, 99)
+    if kind == "offset":
+        b = (b * rng.uniform(0.5, 20.0, N) + rng.uniform(300.0, 3000.0, N)).astype(np.float32)
+    elif kind == "integer":
+        b = np.rint(b * 40.0 + rng.uniform(500.0, 1500.0, N)).astype(np.float32)
+    else:
+        b = (b * (10.0 ** rng.uniform(-20, 20, N))).astype(np.float32)
+    z = builder.zscore(dev(b)).cpu().numpy()
+    ref = oracle.zscore(b)
+    assert np.array_equal(z[:, :T], ref, equal_nan=True)
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("N,T,mode,tau", [
     (2, 10, "r_gt", -1.0), (127, 33, "r_gt", 0.3), (128, 240, "r_ge", 0.2),

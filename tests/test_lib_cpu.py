@@ -120,3 +120,33 @@ def test_bad_arguments_fail_loudly():
         bna._opts("nope", 0.5, "fp32", True, None)
     p = L.SynthParams(N=-1, T=10, K=1)
     assert bna.lib().bna_synth_bold(C.byref(p), None, 1) == 1
+
+
+def test_request_bytes_estimate_is_monotonic():
+    import cuda_newest20160331_gb300 as bna
+    small = bna.request_bytes(4096, 240)
+    big = bna.request_bytes(45000, 240)
+    bigger_t = bna.request_bytes(45000, 1200)
+    assert 0 < small < big < bigger_t
+    # density mode bounds the CSR by the exact edge count, not the caller's cap
+    d = bna.request_bytes(45000, 240, mode="density", value=1.0, cap=10**10)
+    assert d < bna.request_bytes(45000, 240, cap=10**10)
+
+
+def test_server_without_gpu_reports_no_device():
+    import ctypes as C
+    import torch
+    import cuda_newest20160331_gb300 as bna
+    if torch.cuda.is_available():
+        import pytest
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert bna.lib().bna_server_create(0, 2, 1 << 30, C.byref(h)) == 7  # BNA_NO_DEVICE
+
+
+def test_density_nnz_matches_oracle_rule():
+    import cuda_newest20160331_gb300 as bna
+    import oracle
+    for N, s in [(4096, 1.0), (45000, 1.0), (85701, 1.539), (112510, 1.732), (10, 50.0),
+                 (180000, 0.1), (3, 0.0)]:
+        assert bna.density_nnz(N, s) == 2 * oracle.density_k(N, s), (N, s)
