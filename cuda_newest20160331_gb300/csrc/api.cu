@@ -49,6 +49,15 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* ti
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
                            cudaStream_t st);
 cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t st);
+size_t dens_state_bytes();
+size_t dens_ties_cap();
+void dens_state_read(const void* host, int* err, float* tau, long long* n_exact,
+                     long long* n_ties, int* n_drop);
+cudaError_t dens_set(void* state, long long k, float delta, double A, double B, cudaStream_t st);
+cudaError_t launch_density_select(const CorrArgs& a, void* state, unsigned int* hist,
+                                  uint8_t* cls, int* eidx, float* exact, float* slot_val,
+                                  unsigned long long* ties, unsigned long long* drop, int sms,
+                                  cudaStream_t st);
 cudaError_t launch_csr_fill(const CorrArgs& a, int sms, int* dense_list, unsigned int* dense_count,
                             cudaStream_t stream);
 cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream);
@@ -63,7 +72,8 @@ enum Slot {
   S_BOLD, S_Z, S_ZHI, S_ZLO, S_BAD, S_SEG, S_ROWLEN, S_PRE, S_BSUM, S_ROWPTR, S_COL, S_VAL,
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
   S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL,
-  S_DENSE, S_WSTATE, S_VSTAT, S_COUNT
+  S_DENSE, S_WSTATE, S_VSTAT,
+  S_TILES_SMP, S_DSTATE, S_DHIST, S_DCLS, S_DEIDX, S_DEXACT, S_CANDAPX, S_DTIES, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -85,6 +95,9 @@ struct EcGraph {
 };
 
 constexpr int kGraphIters = 32;
+// Density rule: the histogram that locates the k-th value runs on about this
+// many tiles (every s-th tile) when the problem has at least 4x as many.
+constexpr int kSampleTiles = 2048;
 
 }  // namespace
 
@@ -102,7 +115,9 @@ struct bna_ctx {
   EcGraph ecg;
   int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
   int ntiles = 0;
+  int ntiles_smp = 0;  // sampled tile list (density histogram), same block count
   int tiles_per_launch = 0;  // BNA_OPT_TILES_PER_LAUNCH
+  int klaunch = 0;           // kernels launched by the current bna_corr_csr call
   cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
   long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
 };
@@ -216,6 +231,7 @@ int32_t run_zscore(bna_ctx* ctx, const float* bold, int N, int T, bool need_bf16
   void* vstat;
   ENSURE(S_VSTAT, zscore_scratch_bytes(a.n_pad), vstat);
   CK(launch_zscore(bold, N, T, a.n_pad, z, a.ldz, zhi, zlo, a.ldb, bad, vstat, st));
+  ctx->klaunch += 2;
   a.z = z;
   a.zhi = zhi;
   a.zlo = zlo;
@@ -228,6 +244,7 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
   uint8_t* bb;
   ENSURE(S_BLOCKBAD, (size_t)a.nb, bb);
   CK(launch_block_bad(a.bad, a.nb, bb, st));
+  ctx->klaunch += 1;
   if (ctx->tiles_nb != a.nb) {
     std::vector<int2> t;
     tc_tile_list(a.nb, t);
@@ -235,8 +252,17 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
     ENSURE(S_TILES, t.size() * sizeof(int2), d);
     CK(cudaMemcpyAsync(d, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
+    // every s-th tile: the sample the density histogram may be taken on
+    const int s = std::max<int>(1, (int)t.size() / kSampleTiles);
+    std::vector<int2> smp;
+    for (size_t i = 0; i < t.size(); i += s) smp.push_back(t[i]);
+    int2* ds;
+    ENSURE(S_TILES_SMP, smp.size() * sizeof(int2), ds);
+    CK(cudaMemcpyAsync(ds, smp.data(), smp.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
     ctx->tiles_nb = a.nb;
     ctx->ntiles = (int)t.size();
+    ctx->ntiles_smp = (int)smp.size();
   }
   return BNA_OK;
 }
@@ -248,17 +274,23 @@ long long elist_chunk(const bna_ctx* ctx, const CorrArgs& a) {
   return nst < (long long)ctx->sms * 8 * 16 ? kElistChunkMin : kElistChunk;
 }
 
-// pass 0: count (+ edge lists); pass 3: density histogram
-int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st) {
+// pass 0: count (+ edge lists); pass 3: density histogram (sampled: on the
+// sampled tile list, tensor-core forms)
+int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st,
+                  bool sampled = false) {
   switch (precision) {
-    case BNA_PREC_FP32: CK(launch_corr_simt(a, pass, st)); return BNA_OK;
+    case BNA_PREC_FP32:
+      CK(launch_corr_simt(a, pass, st));
+      ctx->klaunch += 1;
+      return BNA_OK;
     case BNA_PREC_BF16X3:
     case BNA_PREC_TF32: {
-      const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[S_TILES]);
-      const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : ctx->ntiles;
-      for (int t0 = 0; t0 < ctx->ntiles; t0 += per)
+      const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[sampled ? S_TILES_SMP : S_TILES]);
+      const int nt = sampled ? ctx->ntiles_smp : ctx->ntiles;
+      const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : nt;
+      for (int t0 = 0; t0 < nt; t0 += per, ++ctx->klaunch)
         CK(launch_corr_tc(a, pass, precision == BNA_PREC_BF16X3 ? 0 : 1, tiles + t0,
-                          std::min(per, ctx->ntiles - t0),
+                          std::min(per, nt - t0),
                           reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
                           ctx->sms, st));
       return BNA_OK;
@@ -453,6 +485,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   if (s) return s;
   cudaStream_t st = as_stream(stream);
   const int prec = opts->precision;
+  ctx->klaunch = 0;
   CorrArgs a{};
   CK(cudaEventRecord(ctx->ev[0], st));
   s = run_zscore(ctx, bold_dev, N, T, prec == BNA_PREC_BF16X3, a, st);
@@ -487,13 +520,24 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
 
   // ---- threshold of the count pass
   long long k_dens = 0;  // density: exact undirected edge count (CorMat.cpp:327-329)
-  if (!density) {
-    a.th.mode = opts->mode;
-    a.th.tau = (float)opts->value;
-    a.th.delta = (float)delta;
-  } else {
-    k_dens = bna_density_nnz(N, opts->value) / 2;  // CorMat.cpp:327-329
-    if (k_dens == 0) {
+  if (density) k_dens = bna_density_nnz(N, opts->value) / 2;
+  const bool tc = prec != BNA_PREC_FP32;
+  // density with a tensor-core form: the k-th value is selected on the device;
+  // its window comes first from a histogram of sampled tiles, and from the
+  // full histogram if the sample's window missed
+  bool sampled = density && k_dens > 0 && tc && ctx->ntiles >= 4 * kSampleTiles;
+  bool dev_sel = density && k_dens > 0 && tc;
+  double winA = 0, winB = 0;
+  int passes = 0;
+  float* cvals = nullptr;
+  long long ties_dropped = 0;
+  int dens_err = 0;
+  for (int wtry = 0;; ++wtry) {
+    if (!density) {
+      a.th.mode = opts->mode;
+      a.th.tau = (float)opts->value;
+      a.th.delta = (float)delta;
+    } else if (k_dens == 0) {
       a.th.mode = BNA_THR_R_GT;  // no edge at all
       a.th.tau = 2.0f;
       a.th.delta = (float)delta;
@@ -503,96 +547,160 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
       ENSURE(S_HIST, (kHistBins + 1) * sizeof(unsigned int), hist);
       CK(cudaMemsetAsync(hist, 0, (kHistBins + 1) * sizeof(unsigned int), st));
       a.hist = hist;
+      a.cand_apx = nullptr;
       a.th.mode = BNA_THR_R_GE;
       a.th.tau = 0.0f;
       a.th.delta = (float)delta;
-      s = corr_pass(ctx, a, prec, 3, st);
+      s = corr_pass(ctx, a, prec, 3, st, sampled);
       if (s) return s;
+      ++passes;
       std::vector<unsigned int> hh(kHistBins + 1);
       CK(cudaMemcpyAsync(hh.data(), hist, hh.size() * sizeof(unsigned int),
                          cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       const long long specials = hh[kHistBins];
+      // exact counts: the k-th largest r~ lies in bins b2..b1; from a sample
+      // the expected count q n_s gets a margin for the sampling spread
+      double want_hi = (double)k_dens, want_lo = (double)(k_dens - specials);
+      if (sampled) {
+        double ns = 0;
+        for (unsigned int x : hh) ns += x;
+        const double M1 = (double)N * (N - 1) / 2;
+        const double e = (double)k_dens / M1 * ns;
+        const double m = 16.0 * std::sqrt(e) + 256.0;
+        want_hi = e + m;
+        want_lo = e - m - (double)specials;
+      }
       long long cum = 0;
       int b1 = 0, b2 = 0;
       bool f1 = false, f2 = false;
       for (int b = kHistBins - 1; b >= 0; --b) {
         cum += hh[b];
-        if (!f2 && cum >= k_dens - specials) { b2 = b; f2 = true; }
-        if (!f1 && cum >= k_dens) { b1 = b; f1 = true; }
+        if (!f2 && (double)cum >= want_lo) { b2 = b; f2 = true; }
+        if (!f1 && (double)cum >= want_hi) { b1 = b; f1 = true; }
       }
-      if (!f2) b2 = kHistBins - 1;
+      if (!f2 || want_lo <= 0) b2 = kHistBins - 1;
       const double w = 2.0 / kHistBins;
-      const double A = (b1 * w - 1.0) - delta;        // tau* >= A
-      const double B = ((b2 + 1) * w - 1.0) + delta;  // tau* <= B
+      winA = (b1 * w - 1.0) - delta;        // tau* >= A
+      winB = ((b2 + 1) * w - 1.0) + delta;  // tau* <= B
       // count pass band = every pair whose exact r can lie in [A, B]
       a.th.mode = BNA_THR_R_GE;
-      a.th.tau = (float)(0.5 * (A + B));
-      a.th.delta = (float)((0.5 * (B - A) + delta) * (1.0 + 1e-6) + 1e-7);
+      a.th.tau = (float)(0.5 * (winA + winB));
+      a.th.delta = (float)((0.5 * (winB - winA) + delta) * (1.0 + 1e-6) + 1e-7);
     }
-  }
-  const Threshold count_th = a.th;
+    const Threshold count_th = a.th;
 
-  int passes = 0;
-  float* cvals = nullptr;
-  for (int attempt = 0;; ++attempt) {
-    a.cand_cap = ctx->cand_cap;
-    // the pool hands out one chunk per warp at a time: room for two per warp
-    a.echunk = elist_chunk(ctx, a);
-    const long long min_pool = (long long)ctx->sms * 8 * 2 * a.echunk;
-    if (ctx->elist_cap < min_pool) ctx->elist_cap = min_pool;
-    a.ecap = ctx->elist_cap;
-    const unsigned long long hcap = next_pow2((unsigned long long)a.cand_cap * 2);
-    a.hmask = hcap - 1;
-    ENSURE(S_CAND, (size_t)a.cand_cap * sizeof(uint2), a.cand);
-    ENSURE(S_HKEYS, hcap * 8, a.hkeys);
-    ENSURE(S_HVAL, hcap * 4, a.hval);
-    ENSURE(S_HEDGE, hcap, a.hedge);
-    ENSURE(S_ELIST, (size_t)a.ecap * sizeof(uint2), a.elist);
-    if (density && k_dens > 0) ENSURE(S_CANDVAL, (size_t)a.cand_cap * sizeof(float), cvals);
-    CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
-    CK(cudaMemsetAsync(a.hkeys, 0xff, hcap * 8, st));
-    const int nwarps = ctx->sms * 8;  // epilogue warps of the tensor-core pass
-    ENSURE(S_WSTATE, (size_t)nwarps * 4 * sizeof(long long), a.wstate);
-    CK(cudaMemsetAsync(a.wstate, 0, (size_t)nwarps * 4 * sizeof(long long), st));
-    a.th = count_th;
-    s = corr_pass(ctx, a, prec, 0, st);
-    if (s) return s;
-    if (prec != BNA_PREC_FP32) CK(launch_seal_candidates(a, nwarps, st));
-    ++passes;
-    CK(cudaEventRecord(ctx->ev[2], st));
-    // the tensor-core count pass lists its candidates itself
-    if (prec == BNA_PREC_FP32) CK(launch_collect_candidates(a, ctx->sms, st));
-    if (density && k_dens > 0) {
-      CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
-    } else {
-      CK(launch_recompute(a, ctx->sms * 8, st));
-      CK(cudaEventRecord(ctx->ev[3], st));
-      CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
-                         st));
+    for (int attempt = 0;; ++attempt) {
+      a.cand_cap = ctx->cand_cap;
+      // the pool hands out one chunk per warp at a time: room for two per warp
+      a.echunk = elist_chunk(ctx, a);
+      const long long min_pool = (long long)ctx->sms * 8 * 2 * a.echunk;
+      if (ctx->elist_cap < min_pool) ctx->elist_cap = min_pool;
+      a.ecap = ctx->elist_cap;
+      const unsigned long long hcap = next_pow2((unsigned long long)a.cand_cap * 2);
+      a.hmask = hcap - 1;
+      ENSURE(S_CAND, (size_t)a.cand_cap * sizeof(uint2), a.cand);
+      ENSURE(S_HKEYS, hcap * 8, a.hkeys);
+      ENSURE(S_HVAL, hcap * 4, a.hval);
+      ENSURE(S_HEDGE, hcap, a.hedge);
+      ENSURE(S_ELIST, (size_t)a.ecap * sizeof(uint2), a.elist);
+      if (density && k_dens > 0) ENSURE(S_CANDVAL, (size_t)a.cand_cap * sizeof(float), cvals);
+      a.cand_apx = nullptr;
+      if (dev_sel) ENSURE(S_CANDAPX, (size_t)a.cand_cap * sizeof(float), a.cand_apx);
+      CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
+      CK(cudaMemsetAsync(a.hkeys, 0xff, hcap * 8, st));
+      const int nwarps = ctx->sms * 8;  // epilogue warps of the tensor-core pass
+      ENSURE(S_WSTATE, (size_t)nwarps * 4 * sizeof(long long), a.wstate);
+      CK(cudaMemsetAsync(a.wstate, 0, (size_t)nwarps * 4 * sizeof(long long), st));
+      a.th = count_th;
+      s = corr_pass(ctx, a, prec, 0, st);
+      if (s) return s;
+      if (tc) CK(launch_seal_candidates(a, nwarps, st));
+      ctx->klaunch += 1;  // seal or collect
+      ++passes;
+      CK(cudaEventRecord(ctx->ev[2], st));
+      // the tensor-core count pass lists its candidates itself
+      if (!tc) CK(launch_collect_candidates(a, ctx->sms, st));
+      if (dev_sel) {
+        void* dstate;
+        unsigned int* dhist;
+        uint8_t* dcls;
+        int* deidx;
+        float* dexact;
+        unsigned long long* dties;
+        ENSURE(S_DSTATE, dens_state_bytes(), dstate);
+        ENSURE(S_DHIST, 2048 * sizeof(unsigned int), dhist);
+        ENSURE(S_DCLS, (size_t)a.cand_cap, dcls);
+        ENSURE(S_DEIDX, (size_t)a.cand_cap * sizeof(int), deidx);
+        ENSURE(S_DEXACT, (size_t)a.cand_cap * sizeof(float), dexact);
+        ENSURE(S_DTIES, 2 * dens_ties_cap() * sizeof(unsigned long long), dties);
+        CK(dens_set(dstate, k_dens, (float)delta, winA, winB, st));
+        CK(cudaMemsetAsync(dhist, 0, 2048 * sizeof(unsigned int), st));
+        CK(launch_density_select(a, dstate, dhist, dcls, deidx, dexact, cvals, dties,
+                                 dties + dens_ties_cap(), ctx->sms, st));
+        ctx->klaunch += 18 + 4;  // selection and decision, scan
+        CK(cudaEventRecord(ctx->ev[3], st));
+        CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr,
+                           a.err, st));
+        CK(cudaMemcpyAsync(static_cast<char*>(ctx->pinned) + 2048, dstate, dens_state_bytes(),
+                           cudaMemcpyDeviceToHost, st));
+      } else if (density && k_dens > 0) {
+        CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
+        ctx->klaunch += 1;
+      } else {
+        CK(launch_recompute(a, ctx->sms * 8, st));
+        ctx->klaunch += 1 + 4;  // recompute, scan
+        CK(cudaEventRecord(ctx->ev[3], st));
+        CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr,
+                           a.err, st));
+      }
+      CK(cudaEventRecord(ctx->ev[4], st));
+      CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      bool again = false;
+      if ((hs->err & (ERR_BAND_OVERFLOW | ERR_HASH_FULL)) && attempt < 3) {
+        ctx->cand_cap = (long long)(hs->cand_count * 3 / 2) + 1024;
+        again = true;
+      }
+      if ((hs->err & ERR_ELIST) && attempt < 3) {
+        ctx->elist_cap = (long long)(hs->epool + hs->epool / 4) + a.echunk;
+        again = true;
+      }
+      if (!again) break;
     }
-    CK(cudaEventRecord(ctx->ev[4], st));
-    CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    bool again = false;
-    if ((hs->err & (ERR_BAND_OVERFLOW | ERR_HASH_FULL)) && attempt < 3) {
-      ctx->cand_cap = (long long)(hs->cand_count * 3 / 2) + 1024;
-      again = true;
+    if (hs->err & ERR_TIMEOUT) return fail(ctx, BNA_TIMEOUT, "count pass: a bounded wait expired");
+    if (hs->err & ERR_BAND_OVERFLOW)
+      return fail(ctx, BNA_INTERNAL, "candidate list overflow (%llu candidates)", hs->cand_count);
+    if (hs->err & ERR_ELIST)
+      return fail(ctx, BNA_INTERNAL, "edge-list pool overflow (%llu entries)", hs->epool);
+    if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
+    if (dev_sel) {
+      float tau_d = 0;
+      long long n_exact = 0, n_ties = 0;
+      int n_drop = 0;
+      dens_state_read(static_cast<char*>(ctx->pinned) + 2048, &dens_err, &tau_d, &n_exact,
+                      &n_ties, &n_drop);
+      if (dens_err == 1 && sampled) {  // the sampled window missed: full histogram
+        sampled = false;
+        continue;
+      }
+      if (dens_err == 0) {
+        a.th.mode = BNA_THR_DENSITY;
+        a.th.tau = tau_d;
+        ties_dropped = n_drop;
+        if (hs->total != 2 * k_dens)
+          return fail(ctx, BNA_INTERNAL, "density: %lld entries instead of %lld", hs->total,
+                      2 * k_dens);
+      } else {
+        // ties beyond the device sort (or an inconsistency): the host selection
+        dev_sel = false;
+        CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
+        ctx->klaunch += 1;
+      }
     }
-    if ((hs->err & ERR_ELIST) && attempt < 3) {
-      ctx->elist_cap = (long long)(hs->epool + hs->epool / 4) + a.echunk;
-      again = true;
-    }
-    if (!again) break;
+    break;
   }
-  if (hs->err & ERR_TIMEOUT) return fail(ctx, BNA_TIMEOUT, "count pass: a bounded wait expired");
-  if (hs->err & ERR_BAND_OVERFLOW)
-    return fail(ctx, BNA_INTERNAL, "candidate list overflow (%llu candidates)", hs->cand_count);
-  if (hs->err & ERR_ELIST)
-    return fail(ctx, BNA_INTERNAL, "edge-list pool overflow (%llu entries)", hs->epool);
-  if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
-  long long ties_dropped = 0;
-  if (density && k_dens > 0) {
+  if (density && k_dens > 0 && !dev_sel) {
     // FormFullGraph_s (CorMat.cpp:770-808): tau* = the k-th largest r; every
     // larger pair is an edge; of the pairs equal to tau*, the first ones in
     // row-major (i < j) order are kept up to k edges.  Every pair that can be
@@ -629,6 +737,8 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
         ties.push_back(((unsigned long long)keys[c].x << 32) | keys[c].y);
     }
     const long long keep = k_dens - greater;
+    if (keep < 0 || (double)tau_star < winA || (double)tau_star > winB)
+      return fail(ctx, BNA_INTERNAL, "density: the k-th value lies outside its window");
     std::sort(ties.begin(), ties.end());
     std::vector<unsigned long long> drop(ties.begin() + std::min<long long>(keep, ties.size()),
                                          ties.end());
@@ -644,6 +754,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     a.th.tau = tau_star;
     a.cand_val = cvals;
     CK(launch_recompute(a, ctx->sms * 8, st));
+    ctx->klaunch += 1 + 4;  // decide, scan
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
                        st));
@@ -700,15 +811,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     stats->band_1e6 = (int64_t)band_1e6;
     stats->ties_dropped = ties_dropped;
     stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
-    // z-score, [block flags], [histogram], per attempt: count (one launch per tile chunk),
-    // collect (FP32 form) or seal (tensor-core forms), recompute or values, 4 scan kernels;
-    // [decide + 4 scan kernels]; fill (2 kernels)
-    int chunks = 1;
-    if (prec != BNA_PREC_FP32 && ctx->tiles_per_launch > 0)
-      chunks = (ctx->ntiles + ctx->tiles_per_launch - 1) / ctx->tiles_per_launch;
-    stats->kernel_launches =
-        1 + (prec != BNA_PREC_FP32 ? 1 : 0) +
-        (density && k_dens > 0 ? chunks + passes * (chunks + 2) + 5 : passes * (chunks + 6)) + 2;
+    stats->kernel_launches = ctx->klaunch + 2;  // + the fill pass (2 kernels)
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);

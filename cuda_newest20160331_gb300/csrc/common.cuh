@@ -122,6 +122,7 @@ struct CorrArgs {
   unsigned long long* stats;  // [0]=band edges [1]=band within 1e-6 [2]=definite listed edges
   unsigned int* hist;         // density histogram pass: kHistBins + 1 counters
   const float* cand_val;      // density: exact values of the candidates (decide pass)
+  float* cand_apx;            // density (tensor-core count pass): r~ of every candidate slot
 };
 
 // Fill-pass store with a range check (an inconsistent count would otherwise

@@ -11,70 +11,9 @@
 // prefix along b, and row_ptr = exclusive prefix of the row totals
 // (FormCSRGraph's R, CorMat.cpp:889-918).
 #include "common.cuh"
+#include "exact_r.cuh"
 
 namespace bna {
-
-// The reference value of a pair: float(sum_t double(float(z_it * z_jt))), the
-// double sum in time order (CorMat.cpp:955-964).  That sequential sum equals
-// the exact sum of the float products whenever every product is a normal
-// float and sum |p_t| < 2^53 units of the smallest ulp among them (each
-// partial sum is then representable).  A warp evaluates one pair: lanes take
-// t = lane, lane+32, ..., the exact sum is an int64 fixed-point reduction
-// across the warp, and only when the condition fails does lane 0 run the
-// sequential double adds.  Returns the value after post_block's clamp.
-__device__ float exact_r_warp(const CorrArgs& a, int i, int j, int lane) {
-  if (a.bad[i] | a.bad[j]) return 0.0f;  // NaN -> 0 in post_block
-  const float* zi = a.z + (size_t)i * a.ldz;
-  const float* zj = a.z + (size_t)j * a.ldz;
-  const int T = a.T;
-  int emin = 1 << 20;
-  bool special = false;
-  for (int t = lane; t < T; t += 32) {
-    const uint32_t b = __float_as_uint(__fmul_rn(__ldg(zi + t), __ldg(zj + t)));
-    const int e8 = (int)((b >> 23) & 0xFFu);
-    special |= (e8 == 0xFF) || (e8 == 0 && (b & 0x7FFFFFu));
-    if (e8 != 0) emin = min(emin, e8 - 150);
-  }
-  emin = __reduce_min_sync(0xffffffffu, emin);
-  special = __any_sync(0xffffffffu, special);
-  bool exact = !special;
-  long long acc = 0, mag = 0;
-  if (exact && emin != (1 << 20)) {
-    for (int t = lane; t < T; t += 32) {
-      const uint32_t b = __float_as_uint(__fmul_rn(__ldg(zi + t), __ldg(zj + t)));
-      const int e8 = (int)((b >> 23) & 0xFFu);
-      if (e8 == 0) continue;
-      const int sh = e8 - 150 - emin;
-      if (sh > 29) {
-        exact = false;
-        continue;
-      }
-      const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u) << sh;
-      mag += m;
-      acc += (b >> 31) ? -m : m;
-    }
-    exact = __all_sync(0xffffffffu, exact);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      mag += __shfl_xor_sync(0xffffffffu, mag, o);
-    }
-    exact = exact && mag < (1LL << 53);
-  }
-  float r = 0.0f;
-  if (lane == 0) {
-    if (exact) {
-      r = (emin == (1 << 20)) ? 0.0f
-                              : __double2float_rn(__dmul_rn(__ll2double_rn(acc), ldexp(1.0, emin)));
-    } else {
-      double s = 0.0;
-      for (int t = 0; t < T; ++t)
-        s = __dadd_rn(s, (double)__fmul_rn(__ldg(zi + t), __ldg(zj + t)));
-      r = __double2float_rn(s);
-    }
-  }
-  return post_block(__shfl_sync(0xffffffffu, r, 0));
-}
 
 // One pair on one thread, sequential double adds (diagnostics only).
 __device__ __forceinline__ float exact_r(const CorrArgs& a, int i, int j) {
@@ -86,18 +25,6 @@ __device__ __forceinline__ float exact_r(const CorrArgs& a, int i, int j) {
   return post_block(__double2float_rn(s));
 }
 
-__device__ __forceinline__ bool in_sorted(const unsigned long long* keys, int n,
-                                          unsigned long long k) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (keys[mid] < k)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  return lo < n && keys[lo] == k;
-}
 
 // Exact values of the candidates only (density mode: the threshold is
 // selected from them before any decision is made).

@@ -121,7 +121,10 @@ __device__ __forceinline__ bool half_sync(TcSmem& S, int h, uint32_t& phase) {
 }
 
 // tm_hi / tm_lo: BF16 hi and lo parts (FORM_BF16X3); tm_hi: FP32 z (FORM_TF32).
-template <int PASS, bool ABS, int FORM>
+// DENS (count pass of the density rule): candidates are listed per 32-column
+// chunk together with their approximate value (a.cand_apx), which the device
+// selection of the k-th largest value needs.
+template <int PASS, bool ABS, int FORM, bool DENS>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
                    const __grid_constant__ CUtensorMap tm_lo, const TcArgs p) {
@@ -447,7 +450,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           n_def += __popc(eb);
           S.colmask[h][c * 32 + lane][q] = transpose32(eb, lane);
           wcur += total;
-          cmk4[c] = it & ~eb;  // candidates of this chunk (listed after the tile)
+          if (!DENS) {
+            cmk4[c] = it & ~eb;  // candidates of this chunk (listed after the tile)
+          } else if (__any_sync(0xffffffffu, (it & ~eb) != 0u)) {
+            // candidates with their approximate values, listed now (v[] is live)
+            const uint32_t cmk = it & ~eb;
+            const int nc = __popc(cmk);
+            int cinc = nc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int y = __shfl_up_sync(0xffffffffu, cinc, o);
+              if (lane >= o) cinc += y;
+            }
+            const int ctot = __shfl_sync(0xffffffffu, cinc, 31);
+            if (ccur + ctot > cend) {
+              for (long long sl = ccur + lane; sl < cend && sl < a.cand_cap; sl += 32)
+                a.cand[sl] = make_uint2(kCandNone, kCandNone);
+              const long long need = (ctot + kCandChunk - 1) / kCandChunk * kCandChunk;
+              unsigned long long cb = 0;
+              if (lane == 0) cb = atomicAdd(a.cand_count, (unsigned long long)need);
+              ccur = (long long)__shfl_sync(0xffffffffu, cb, 0);
+              cend = ccur + need;
+            }
+            long long slot = ccur + (cinc - nc);
+            uint32_t w3 = cmk;
+            while (w3) {
+              const int k = __ffs(w3) - 1;
+              w3 &= w3 - 1;
+              const bool badk = (badm >> k) & 1u;
+              const float r = badk ? 0.0f : __uint_as_float(pick32(v, k));
+              if (slot < a.cand_cap) {
+                a.cand[slot] = make_uint2((unsigned)gi, (unsigned)(J * 128 + c * 32 + k));
+                a.cand_apx[slot] = r;
+              } else {
+                atomicOr(a.err, ERR_BAND_OVERFLOW);
+              }
+              ++slot;
+            }
+            ccur += ctot;
+            n_cand += nc;
+          }
         }
       }
       // the accumulator has been read: hand it back to the MMA warp
@@ -455,7 +497,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       ptx::mbar_arrive(ptx::smem_u32(&S.tempty[acc]));
       if (PASS == 2 || PASS == 3) continue;
       // candidates (rare): warp prefix scan into the warp's candidate chunk
-      if (active && __any_sync(0xffffffffu, (cmk4[0] | cmk4[1] | cmk4[2] | cmk4[3]) != 0u)) {
+      if (!DENS && active &&
+          __any_sync(0xffffffffu, (cmk4[0] | cmk4[1] | cmk4[2] | cmk4[3]) != 0u)) {
         const int nc = __popc(cmk4[0]) + __popc(cmk4[1]) + __popc(cmk4[2]) + __popc(cmk4[3]);
         int cinc = nc;
 #pragma unroll
@@ -637,17 +680,21 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* ti
   const int g = grid < ntiles ? grid : ntiles;
   if (g <= 0) return cudaSuccess;
   const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
+  const bool dens = pass == 0 && a.cand_apx != nullptr;
+  if (dens && absm) return cudaErrorInvalidValue;  // the density rule is signed
   void (*kern)(CUtensorMap, CUtensorMap, TcArgs);
   if (form == FORM_BF16X3)
-    kern = pass == 0   ? (absm ? corr_tc_kernel<0, true, FORM_BF16X3>
-                               : corr_tc_kernel<0, false, FORM_BF16X3>)
-           : pass == 3 ? corr_tc_kernel<3, false, FORM_BF16X3>
-                       : corr_tc_kernel<2, false, FORM_BF16X3>;
+    kern = pass == 0   ? (dens   ? corr_tc_kernel<0, false, FORM_BF16X3, true>
+                          : absm ? corr_tc_kernel<0, true, FORM_BF16X3, false>
+                                 : corr_tc_kernel<0, false, FORM_BF16X3, false>)
+           : pass == 3 ? corr_tc_kernel<3, false, FORM_BF16X3, false>
+                       : corr_tc_kernel<2, false, FORM_BF16X3, false>;
   else
-    kern = pass == 0   ? (absm ? corr_tc_kernel<0, true, FORM_TF32>
-                               : corr_tc_kernel<0, false, FORM_TF32>)
-           : pass == 3 ? corr_tc_kernel<3, false, FORM_TF32>
-                       : corr_tc_kernel<2, false, FORM_TF32>;
+    kern = pass == 0   ? (dens   ? corr_tc_kernel<0, false, FORM_TF32, true>
+                          : absm ? corr_tc_kernel<0, true, FORM_TF32, false>
+                                 : corr_tc_kernel<0, false, FORM_TF32, false>)
+           : pass == 3 ? corr_tc_kernel<3, false, FORM_TF32, false>
+                       : corr_tc_kernel<2, false, FORM_TF32, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)TC_SMEM_BYTES);
   if (e != cudaSuccess) return e;

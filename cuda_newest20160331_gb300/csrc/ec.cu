@@ -203,8 +203,16 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
     const double* __restrict__ u, const float2* __restrict__ uf, double* __restrict__ un,
     float2* __restrict__ unf, double* parts, EcState* st, int max_iter, double eps) {
   if (st->done || st->iter >= max_iter) return;
-  const double lam = sqrt(st->lam2);
-  const double inv = 1.0 / lam;
+  // lambda and its reciprocal once per block (FP64 sqrt and division are
+  // long instruction sequences on this GPU), shared through shared memory
+  __shared__ double lam_s[2];
+  if (threadIdx.x == 0) {
+    lam_s[0] = sqrt(st->lam2);
+    lam_s[1] = 1.0 / lam_s[0];
+  }
+  __syncthreads();
+  const double lam = lam_s[0];
+  const double inv = lam_s[1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = gridDim.x * (kEcThreads / 32);
   double a0 = 0, a1 = 0, a2 = 0;
@@ -314,9 +322,15 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
   const int nwarps = gridDim.x * (kEcThreads / 32);
   double lam2 = st->lam2, lam_used = 0.0, e1 = 1.0, e2 = 1.0;
   int it = 0;
+  __shared__ double lam_s[2];
   while (it < max_iter) {
-    const double lam = sqrt(lam2);
-    const double inv = 1.0 / lam;
+    if (threadIdx.x == 0) {
+      lam_s[0] = sqrt(lam2);
+      lam_s[1] = 1.0 / lam_s[0];
+    }
+    __syncthreads();
+    const double lam = lam_s[0];
+    const double inv = lam_s[1];
     const size_t cur = (size_t)(it & 1) * n, nxt = (size_t)((it + 1) & 1) * n;
     // the iterate was written by other blocks: read it from L2 (__ldcg), not L1
     const double* uc = u + cur;
@@ -388,11 +402,17 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
       }
       __syncthreads();
     }
+    __shared__ double e_s[2];
+    if (threadIdx.x == 0) {
+      e_s[0] = sqrt(red[0][1]);
+      e_s[1] = sqrt(red[0][2]);
+    }
+    __syncthreads();
     lam_used = lam;
     lam2 = red[0][0];
-    e1 = sqrt(red[0][1]);
-    e2 = sqrt(red[0][2]);
-    __syncthreads();  // red is rewritten in the next iteration
+    e1 = e_s[0];
+    e2 = e_s[1];
+    __syncthreads();  // red, lam_s and e_s are rewritten in the next iteration
     ++it;
     if (e1 <= eps || e2 <= eps) break;
   }

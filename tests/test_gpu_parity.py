@@ -186,6 +186,47 @@ def test_density_edge_cases(builder, precision):
             assert_csr_equal(res, R, C, V, res.stats["delta"])
 
 
+def test_density_sampled_window_matches_oracle(builder):
+    """Large enough for the sampled density histogram (>= 4 x 2048 tiles):
+    the window comes from every s-th tile, the k-th value is selected on the
+    device; the CSR must equal the oracle's for every form."""
+    N, T, pct = 23100, 60, 0.8
+    b = bna.synth_bold(N, T, 20, 31)
+    z = oracle.zscore(b)
+    P = oracle.cormat_packed(z)
+    tau, k, drop = oracle.density(P, N, pct)
+    R, C, V = oracle.threshold_csr(P, N, "r_ge", tau, drop=drop)
+    del P
+    for precision in PRECISIONS:
+        res = builder.corr_csr(dev(b), mode="density", value=pct, precision=precision)
+        assert res.nnz == 2 * k, precision
+        assert np.float32(res.stats["tau"]) == np.float32(tau), precision
+        assert_csr_equal(res, R, C, V, res.stats["delta"])
+
+
+def test_density_sampled_window_miss_falls_back(builder):
+    """A tight cluster of strongly correlated voxels holds more than k pairs:
+    a tile sample that misses it puts the window far too low; the selection
+    must detect that and rerun with the full histogram (same CSR as the plain
+    FP32 form, exactly k edges)."""
+    N, T, pct = 23100, 60, 0.05
+    rng = np.random.default_rng(7)
+    b = bna.synth_bold(N, T, 20, 32)
+    base = rng.standard_normal(T).astype(np.float32)
+    lo = 5000
+    for i in range(lo, lo + 900):
+        b[:, i] = base + np.float32(0.25) * rng.standard_normal(T).astype(np.float32)
+    ref = builder.corr_csr(dev(b), mode="density", value=pct, precision="fp32").numpy()
+    k = bna.density_nnz(N, pct) // 2
+    assert ref.nnz == 2 * k
+    for precision in ("bf16x3", "tf32"):
+        res = builder.corr_csr(dev(b), mode="density", value=pct, precision=precision).numpy()
+        print(precision, "passes", res.stats["passes"])
+        assert res.nnz == 2 * k
+        assert np.array_equal(res.row_ptr, ref.row_ptr)
+        assert np.array_equal(res.col_idx, ref.col_idx)
+
+
 def test_host_buffer_path_equals_device_path(builder):
     b = bna.synth_bold(1000, 64, 10, 13)
     h = builder.corr_csr_host(b, mode="r_gt", value=0.45)
