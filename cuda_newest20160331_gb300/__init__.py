@@ -169,6 +169,28 @@ class Builder:
             va = va.clone() if va is not None else None
         return CsrResult(N, int(out.nnz), rp, ci, va, st.as_dict())
 
+    def rethreshold(self, csr: CsrResult, mode: str, value: float, stream=None,
+                    copy: bool = True) -> CsrResult:
+        """CSR at a higher threshold of the same rule, derived from `csr` (the
+        weighted device CSR of this context's last corr_csr) without another
+        correlation pass (bna_csr_rethreshold)."""
+        import torch
+        c = L.Csr(n=csr.n, nnz=csr.nnz, row_ptr=csr.row_ptr.data_ptr(),
+                  col_idx=csr.col_idx.data_ptr() if csr.nnz else None,
+                  val=csr.val.data_ptr() if csr.val is not None and csr.nnz else None)
+        out = L.Csr()
+        band = C.c_int64()
+        _check(lib().bna_csr_rethreshold(self._h, C.byref(c), L.THR_MODES[mode], float(value),
+                                         C.byref(out), C.byref(band), self._stream(stream)),
+               self._h)
+        dev = csr.row_ptr.device
+        rp = _view(out.row_ptr, csr.n + 1, "<i4", torch, dev)
+        ci = _view(out.col_idx, out.nnz, "<i4", torch, dev)
+        va = _view(out.val, out.nnz, "<f4", torch, dev)
+        if copy:
+            rp, ci, va = rp.clone(), ci.clone(), va.clone()
+        return CsrResult(csr.n, int(out.nnz), rp, ci, va, {"band_1e6": band.value})
+
     def corr_csr_host(self, bold: np.ndarray, mode: str = "r_gt", value: float = 0.5,
                       precision: str = "fp32", weighted: bool = True,
                       delta: Optional[float] = None) -> CsrResult:

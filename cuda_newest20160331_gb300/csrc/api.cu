@@ -47,8 +47,18 @@ void tc_tile_list(int nb, std::vector<int2>& out);
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
-                           cudaStream_t st);
+                           cudaStream_t st, const AvgPass* avg = nullptr);
 cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t st);
+cudaError_t launch_rowlen_scan(const long long* rowlen, int n, long long* pre, long long* bsum,
+                               long long* total, int32_t* row_ptr, uint32_t* err,
+                               cudaStream_t stream);
+cudaError_t launch_rethr_count(const CorrArgs& a, const int32_t* rp, const int32_t* ci,
+                               const float* val, const Threshold& th, uint8_t* keep, float* valx,
+                               long long* rowlen, unsigned long long* band, int sms,
+                               cudaStream_t st);
+cudaError_t launch_rethr_fill(int n, const int32_t* rp, const int32_t* ci, const float* valx,
+                              const uint8_t* keep, const int32_t* rp2, int32_t* ci2, float* val2,
+                              long long nnz2, uint32_t* err, int sms, cudaStream_t st);
 size_t dens_state_bytes();
 size_t dens_ties_cap();
 void dens_state_read(const void* host, int* err, float* tau, long long* n_exact,
@@ -73,7 +83,8 @@ enum Slot {
   S_CAND, S_HKEYS, S_HVAL, S_HEDGE, S_STATUS, S_DROP, S_EC_U, S_EC_PARTS, S_EC_STATE,
   S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL,
   S_DENSE, S_WSTATE, S_VSTAT,
-  S_TILES_SMP, S_DSTATE, S_DHIST, S_DCLS, S_DEIDX, S_DEXACT, S_CANDAPX, S_DTIES, S_COUNT
+  S_TILES_SMP, S_DSTATE, S_DHIST, S_DCLS, S_DEIDX, S_DEXACT, S_CANDAPX, S_DTIES,
+  S_RT_KEEP, S_RT_VALX, S_RT_ROWPTR, S_RT_COL, S_RT_VAL, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -118,6 +129,10 @@ struct bna_ctx {
   int ntiles_smp = 0;  // sampled tile list (density histogram), same block count
   int tiles_per_launch = 0;  // BNA_OPT_TILES_PER_LAUNCH
   int klaunch = 0;           // kernels launched by the current bna_corr_csr call
+  // layout and rule of the last bna_corr_csr (its z-scores stay in the arena):
+  // what bna_csr_rethreshold recomputes exact values from
+  CorrArgs last{};
+  bool last_ok = false;
   cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
   long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
 };
@@ -414,6 +429,7 @@ int32_t bna_ctx_trim(bna_ctx* ctx) {
   }
   cudaStreamSynchronize(nullptr);
   ctx->tiles_nb = -1;  // the tile list lived in the arena
+  ctx->last_ok = false;
   if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
   ctx->ecg = EcGraph();
   return BNA_OK;
@@ -447,6 +463,7 @@ int32_t bna_zscore(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T, fl
   if (!ctx || !bold_dev || !z_dev || N <= 0 || T <= 0 || ldz < T || ldz % 32 != 0)
     return fail(ctx, BNA_BAD_ARG, "bna_zscore: bad arguments");
   int32_t s = set_device(ctx, as_stream(stream));
+  ctx->last_ok = false;  // the arena's z-scores may be rewritten
   if (s) return s;
   const int n_pad = round_up(N, kBlk);
   uint8_t* bad;
@@ -486,6 +503,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   cudaStream_t st = as_stream(stream);
   const int prec = opts->precision;
   ctx->klaunch = 0;
+  ctx->last_ok = false;  // the arena is about to be rewritten
   CorrArgs a{};
   CK(cudaEventRecord(ctx->ev[0], st));
   s = run_zscore(ctx, bold_dev, N, T, prec == BNA_PREC_BF16X3, a, st);
@@ -801,6 +819,9 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   out_dev->row_ptr = row_ptr;
   out_dev->col_idx = col;
   out_dev->val = val;
+  ctx->last = a;
+  ctx->last.th.delta = (float)delta;
+  ctx->last_ok = !density && a.weighted;
   if (stats) {
     std::memset(stats, 0, sizeof *stats);
     stats->tau = density && k_dens == 0 ? INFINITY : (double)a.th.tau;
@@ -907,6 +928,7 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
   if (!ctx || !bold_dev || !out_dev || N < 1 || T < 1)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_tile_values: bad arguments");
   int32_t s = set_device(ctx, as_stream(stream));
+  ctx->last_ok = false;  // the z-scores are rewritten
   if (s) return s;
   cudaStream_t st = as_stream(stream);
   CorrArgs a{};
@@ -932,6 +954,65 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
     }
     default: return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built", precision);
   }
+  return BNA_OK;
+}
+
+int32_t bna_csr_rethreshold(bna_ctx* ctx, const bna_csr* in_dev, int32_t mode, double tau,
+                            bna_csr* out_dev, int64_t* band_1e6, void* stream) {
+  if (!ctx || !in_dev || !out_dev || !in_dev->row_ptr || (in_dev->nnz > 0 && !in_dev->val))
+    return fail(ctx, BNA_BAD_ARG, "bna_csr_rethreshold: bad arguments (a weighted CSR is needed)");
+  if (!ctx->last_ok || in_dev->n != ctx->last.n)
+    return fail(ctx, BNA_BAD_ARG, "bna_csr_rethreshold: the CSR must come from this context's "
+                "last bna_corr_csr (threshold rule, weighted)");
+  const int m0 = ctx->last.th.mode;
+  const bool abs0 = m0 == BNA_THR_ABS_GT || m0 == BNA_THR_ABS_GE;
+  const bool abs1 = mode == BNA_THR_ABS_GT || mode == BNA_THR_ABS_GE;
+  if (mode < BNA_THR_R_GT || mode > BNA_THR_ABS_GE || abs0 != abs1 ||
+      (float)tau < ctx->last.th.tau)
+    return fail(ctx, BNA_BAD_ARG, "bna_csr_rethreshold: the rule must be of the same kind and "
+                "tau not below the built one");
+  int32_t s = set_device(ctx, as_stream(stream));
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  const int N = in_dev->n;
+  const long long nnz_in = in_dev->nnz;
+  CorrArgs a = ctx->last;
+  Threshold th{mode, (float)tau, ctx->last.th.delta};
+  uint8_t* keep;
+  float* valx;
+  long long *rowlen, *pre, *bsum;
+  int32_t* rp2;
+  DevStatus* ds;
+  ENSURE(S_RT_KEEP, (size_t)std::max(nnz_in, 1LL), keep);
+  ENSURE(S_RT_VALX, (size_t)std::max(nnz_in, 1LL) * 4, valx);
+  ENSURE(S_ROWLEN, (size_t)round_up(N, kBlk) * 8, rowlen);
+  ENSURE(S_PRE, (size_t)round_up(N, kBlk) * 8, pre);
+  ENSURE(S_BSUM, (size_t)4096 * 8, bsum);
+  ENSURE(S_RT_ROWPTR, (size_t)(N + 1) * 4, rp2);
+  ENSURE(S_STATUS, sizeof(DevStatus), ds);
+  CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
+  CK(launch_rethr_count(a, in_dev->row_ptr, in_dev->col_idx, in_dev->val, th, keep, valx, rowlen,
+                        &ds->stats[1], ctx->sms, st));
+  CK(launch_rowlen_scan(rowlen, N, pre, bsum, &ds->total, rp2, &ds->err, st));
+  DevStatus* hs = reinterpret_cast<DevStatus*>(ctx->pinned);
+  CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const long long nnz = hs->total;
+  int32_t* ci2;
+  float* va2;
+  ENSURE(S_RT_COL, (size_t)std::max(nnz, 1LL) * 4, ci2);
+  ENSURE(S_RT_VAL, (size_t)std::max(nnz, 1LL) * 4, va2);
+  CK(launch_rethr_fill(N, in_dev->row_ptr, in_dev->col_idx, valx, keep, rp2, ci2, va2, nnz,
+                       &ds->err, ctx->sms, st));
+  CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (hs->err & ERR_RANGE) return fail(ctx, BNA_INTERNAL, "rethreshold: position out of range");
+  out_dev->n = N;
+  out_dev->nnz = nnz;
+  out_dev->row_ptr = rp2;
+  out_dev->col_idx = ci2;
+  out_dev->val = va2;
+  if (band_1e6) *band_1e6 = (int64_t)hs->stats[1];
   return BNA_OK;
 }
 

@@ -54,6 +54,28 @@ struct Threshold {
   float delta;   // band half-width in r units (includes rounding margin)
 };
 
+// Fisher transform of the reference, fishertrans (W/CorMat/CUCorMat/CUCorMat/
+// CorMat.cpp:36-42), in its float arithmetic: r == 1 is moved to float(1 - 1e-6),
+// z = 0.5 log((1 + r) / (1 - r)).
+__device__ __forceinline__ float fisher_z(float r) {
+  if (r == 1.0f) r = 0.99999899f;  // float(1.0 - 1e-6)
+  return 0.5f * logf(__fdiv_rn(__fadd_rn(1.0f, r), __fsub_rn(1.0f, r)));
+}
+
+// Its inverse, inv_fishertrans (CorMat.cpp:44-50): r = (e^(2z) - 1) / (e^(2z) + 1).
+__device__ __forceinline__ float fisher_r(float z) {
+  const float e = expf(__fmul_rn(2.0f, z));
+  return __fdiv_rn(__fsub_rn(e, 1.0f), __fadd_rn(e, 1.0f));
+}
+
+// Multi-subject average pass (tensor-core pass 4) buffers.
+struct AvgPass {
+  float* packed;       // [n(n-1)/2] running sums, upper triangle row-major
+  uint32_t* uncertain; // one bit per pair
+  int fisher;
+  float unc_lim;
+};
+
 // Exact decision on the reference's value r (after post_block clamping).
 __device__ __forceinline__ bool edge_exact(float r, const Threshold& th) {
   switch (th.mode) {
@@ -123,7 +145,16 @@ struct CorrArgs {
   unsigned int* hist;         // density histogram pass: kHistBins + 1 counters
   const float* cand_val;      // density: exact values of the candidates (decide pass)
   float* cand_apx;            // density (tensor-core count pass): r~ of every candidate slot
+  // multi-subject average: the averaged values (packed upper triangle) replace
+  // the GEMM as the source of the plain count pass; uncertain pairs are
+  // candidates
+  const float* avg_packed;
+  const uint32_t* avg_unc;
 };
+
+__host__ __device__ __forceinline__ long long packed_index(int i, int j, int n) {
+  return (long long)i * (2LL * n - i - 1) / 2 + (j - i - 1);  // i < j, row-major
+}
 
 // Fill-pass store with a range check (an inconsistent count would otherwise
 // write outside the CSR).

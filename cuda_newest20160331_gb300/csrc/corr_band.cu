@@ -316,4 +316,16 @@ cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* r
   return cudaGetLastError();
 }
 
+// Exclusive prefix of given row lengths -> row_ptr (no seg step).
+cudaError_t launch_rowlen_scan(const long long* rowlen, int n, long long* pre, long long* bsum,
+                               long long* total, int32_t* row_ptr, uint32_t* err,
+                               cudaStream_t stream) {
+  const int nblk = (n + 4095) / 4096;
+  if (nblk > 4096) return cudaErrorInvalidValue;
+  scan_block_kernel<<<nblk, 1024, 0, stream>>>(rowlen, n, pre, bsum);
+  scan_sums_kernel<<<1, 1024, 0, stream>>>(bsum, nblk, total);
+  scan_finish_kernel<<<(n + 1 + 255) / 256, 256, 0, stream>>>(pre, bsum, n, total, row_ptr, err);
+  return cudaGetLastError();
+}
+
 }  // namespace bna

@@ -23,8 +23,9 @@ constexpr int SK = 16;   // K (time) chunk per stage
 constexpr int SPAD = 4;
 
 // PASS 0 = count (+ edge list), 2 = dump approximate values of one tile,
-// 3 = density histogram.
-template <int PASS>
+// 3 = density histogram.  PACKED: the tile's values come from the averaged
+// packed matrix (multi-subject average) instead of the GEMM.
+template <int PASS, bool PACKED = false>
 __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, int dumpI,
                                                            int dumpJ, float* dump) {
   __shared__ __align__(16) float As[2][SK][SB + SPAD];
@@ -52,7 +53,18 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 
-  const int kt = (a.T + SK - 1) / SK;
+  if (PACKED) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int gi = I * SB + ((i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int gj = J * SB + ((j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+        acc[i][j] = (gi < gj && gj < a.n) ? a.avg_packed[packed_index(gi, gj, a.n)] : 0.f;
+      }
+    }
+  }
+  const int kt = PACKED ? 0 : (a.T + SK - 1) / SK;
   float4 ra0, ra1, rb0, rb1;
   auto gload = [&](int k0) {
     ra0 = __ldg(reinterpret_cast<const float4*>(Ag + (size_t)lr * a.ldz + k0 + lk));
@@ -71,8 +83,10 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
     Bs[b][lk + 2][lr + 64] = rb1.z; Bs[b][lk + 3][lr + 64] = rb1.w;
   };
 
-  gload(0);
-  sstore(0);
+  if (!PACKED) {
+    gload(0);
+    sstore(0);
+  }
   __syncthreads();
   for (int kk = 0; kk < kt; ++kk) {
     const int b = kk & 1;
@@ -166,6 +180,9 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
         acc[i][j] = 0.f;  // NaN voxel: the exact value is 0 (post_block)
         const float x = 0.0f - a.th.tau;
         c = x > a.th.delta ? CLS_EDGE : (x < -a.th.delta ? CLS_NO : CLS_BAND);
+      } else if (PACKED && ((a.avg_unc[packed_index(gi, gj, a.n) >> 5] >>
+                              (packed_index(gi, gj, a.n) & 31)) & 1u)) {
+        c = CLS_BAND;  // some subject's value may be clamped by post_block
       } else {
         c = classify(acc[i][j], a.th);
       }
@@ -247,6 +264,20 @@ cudaError_t launch_corr_simt(const CorrArgs& a, int pass, cudaStream_t stream) {
     corr_simt_kernel<0><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
   else if (pass == 3)
     corr_simt_kernel<3><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// Count pass / density histogram over the averaged packed matrix.
+cudaError_t launch_corr_packed(const CorrArgs& a, int pass, cudaStream_t stream) {
+  const int nt = a.nb;
+  const long long tiles = (long long)nt * (nt + 1) / 2;
+  if (tiles > 0x7fffffffLL || !a.avg_packed || !a.avg_unc) return cudaErrorInvalidValue;
+  if (pass == 0)
+    corr_simt_kernel<0, true><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
+  else if (pass == 3)
+    corr_simt_kernel<3, true><<<(unsigned)tiles, 256, 0, stream>>>(a, nt, 0, 0, nullptr);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

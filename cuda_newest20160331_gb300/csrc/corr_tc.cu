@@ -74,6 +74,13 @@ constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_RING_BYTES + sizeof(TcSmem);
 
 struct TcArgs {
   CorrArgs a;
+  // pass 4 (multi-subject average, post_block with accumulation,
+  // W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:847-883): packed[idx(i, j)] += r~
+  // or its Fisher z; pairs with |r~| >= unc_lim get their uncertain bit
+  float* packed;
+  uint32_t* uncertain;
+  int fisher;
+  float unc_lim;
   const int2* tiles;        // (I, Jp): rows of block I x columns of blocks 2Jp, 2Jp+1
   int ntiles;
   int nksteps;              // MMA K steps = ceil(T / elements per step)
@@ -377,6 +384,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int lo = il - c * 32 + 1;  // first column index k with jl > il
             valid &= (lo <= 0) ? 0xffffffffu : (lo >= 32 ? 0u : (0xffffffffu << lo));
           }
+          if (PASS == 4) {
+            uint32_t badm4 = 0;
+            if (slow)
+              for (int k = 0; k < 32; ++k)
+                if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm4 |= 1u << k;
+            if (gi < a.n) {
+              // packed upper-triangle index of (gi, j): gi (2n - gi - 1) / 2 + j - gi - 1
+              const long long rowbase = (long long)gi * (2LL * a.n - gi - 1) / 2 - gi - 1;
+#pragma unroll
+              for (int k = 0; k < 32; ++k) {
+                if (!((valid >> k) & 1u)) continue;
+                const bool badk = (badm4 >> k) & 1u;
+                const float r = badk ? 0.0f : __uint_as_float(v[k]);
+                const long long idx = rowbase + jb + k;
+                if (!badk && !(fabsf(r) < p.unc_lim))
+                  atomicOr(&p.uncertain[idx >> 5], 1u << (idx & 31));
+                float add = 0.0f;
+                if (r >= -1.0f && r <= 1.0f) add = p.fisher ? fisher_z(r) : r;
+                p.packed[idx] = __fadd_rn(p.packed[idx], add);
+              }
+            }
+            continue;
+          }
           if (PASS == 3) {
             // density histogram of the approximate values (exact 0 for NaN voxels)
             uint32_t badm3 = 0;
@@ -495,7 +525,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // the accumulator has been read: hand it back to the MMA warp
       ptx::tc_fence_before();
       ptx::mbar_arrive(ptx::smem_u32(&S.tempty[acc]));
-      if (PASS == 2 || PASS == 3) continue;
+      if (PASS == 2 || PASS == 3 || PASS == 4) continue;
       // candidates (rare): warp prefix scan into the warp's candidate chunk
       if (!DENS && active &&
           __any_sync(0xffffffffu, (cmk4[0] | cmk4[1] | cmk4[2] | cmk4[3]) != 0u)) {
@@ -655,7 +685,7 @@ cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t s
 // 3 density histogram; form FORM_BF16X3 or FORM_TF32
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
-                           cudaStream_t st) {
+                           cudaStream_t st, const AvgPass* avg) {
   CUtensorMap mh, ml;
   if (form == FORM_BF16X3) {
     if (!a.zhi || !a.zlo || a.ldb % 64 != 0) return cudaErrorInvalidValue;
@@ -677,6 +707,11 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* ti
   p.blockbad = blockbad;
   p.dump = dump;
   p.dump_half = dump_half;
+  p.packed = avg ? avg->packed : nullptr;
+  p.uncertain = avg ? avg->uncertain : nullptr;
+  p.fisher = avg ? avg->fisher : 0;
+  p.unc_lim = avg ? avg->unc_lim : 1.0f;
+  if (pass == 4 && !avg) return cudaErrorInvalidValue;
   const int g = grid < ntiles ? grid : ntiles;
   if (g <= 0) return cudaSuccess;
   const bool absm = (a.th.mode == BNA_THR_ABS_GT || a.th.mode == BNA_THR_ABS_GE);
@@ -688,12 +723,14 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* ti
                           : absm ? corr_tc_kernel<0, true, FORM_BF16X3, false>
                                  : corr_tc_kernel<0, false, FORM_BF16X3, false>)
            : pass == 3 ? corr_tc_kernel<3, false, FORM_BF16X3, false>
+           : pass == 4 ? corr_tc_kernel<4, false, FORM_BF16X3, false>
                        : corr_tc_kernel<2, false, FORM_BF16X3, false>;
   else
     kern = pass == 0   ? (dens   ? corr_tc_kernel<0, false, FORM_TF32, true>
                           : absm ? corr_tc_kernel<0, true, FORM_TF32, false>
                                  : corr_tc_kernel<0, false, FORM_TF32, false>)
            : pass == 3 ? corr_tc_kernel<3, false, FORM_TF32, false>
+           : pass == 4 ? corr_tc_kernel<4, false, FORM_TF32, false>
                        : corr_tc_kernel<2, false, FORM_TF32, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)TC_SMEM_BYTES);

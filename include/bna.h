@@ -168,6 +168,18 @@ int32_t bna_corr_csr_host_into(bna_ctx* ctx, const float* bold_host, int32_t N, 
                                int32_t* col_idx_host, float* val_host, int64_t cap,
                                int64_t* nnz_out, bna_corr_stats* stats);
 
+/* Several thresholds from one correlation pass (the reference thresholds one
+ * correlation matrix once per value of its threshold list,
+ * W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:105-111, 318-341).  in_dev must be the
+ * weighted CSR of this context's last bna_corr_csr (an r or |r| rule); the
+ * result is the CSR of the same kind of rule at tau >= the built threshold,
+ * equal to what bna_corr_csr would build at tau.  Entries within the
+ * recompute band of tau get their exact reference value.  out_dev lives in
+ * the context's arena until the next call; band_1e6 (optional) counts the
+ * entries with |r - tau| <= 1e-6. */
+int32_t bna_csr_rethreshold(bna_ctx* ctx, const bna_csr* in_dev, int32_t mode, double tau,
+                            bna_csr* out_dev, int64_t* band_1e6, void* stream);
+
 /* Approximate correlation values of one BM x BN tile (rows I*128.., columns
  * J*128.. of the z-scored matrix), written row-major to out_dev (128 x 128
  * floats), for measuring max |r - r_fp64| of a precision form.  z_dev as

@@ -327,3 +327,34 @@ def test_ec_not_converged_reports_status(builder):
     ec, lam, it, conv = builder.ec(csr, max_iter=1)
     ec_o, lam_o, it_o, conv_o = oracle.ec(R, C, max_iter=1)
     assert it == it_o == 1 and conv == conv_o
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("mode,taus", [("r_gt", (0.30, 0.35, 0.5)), ("r_ge", (0.32, 0.32, 0.4)),
+                                       ("abs_ge", (0.3, 0.42))])
+def test_rethreshold_equals_direct_build(builder, precision, mode, taus):
+    """Several thresholds from one pass (the reference's threshold list):
+    deriving the CSR at each higher tau from the lowest one gives the CSR a
+    direct build at that tau gives (row_ptr / col_idx bit-exact)."""
+    b = bna.synth_bold(3000, 150, 12, 41)
+    b[:, 17] = 3.0  # zero-variance voxel
+    base = builder.corr_csr(dev(b), mode=mode, value=taus[0], precision=precision)
+    z = oracle.zscore(b)
+    P = oracle.cormat_packed(z)
+    for t in taus[1:]:
+        d = builder.rethreshold(base, mode, t).numpy()
+        R, C, V = oracle.threshold_csr(P, 3000, mode, t)
+        assert np.array_equal(d.row_ptr, R) and np.array_equal(d.col_idx, C), (mode, t)
+        assert np.max(np.abs(d.val - V)) <= base.stats["delta"]
+
+
+def test_rethreshold_refuses_lower_tau_and_other_rules(builder):
+    b = bna.synth_bold(500, 60, 8, 42)
+    base = builder.corr_csr(dev(b), mode="r_gt", value=0.4, precision="bf16x3")
+    for mode, t in [("r_gt", 0.3), ("abs_gt", 0.5)]:
+        with pytest.raises(bna.BnaError) as e:
+            builder.rethreshold(base, mode, t)
+        assert e.value.status == 1
+    dens = builder.corr_csr(dev(b), mode="density", value=2.0, precision="bf16x3")
+    with pytest.raises(bna.BnaError):
+        builder.rethreshold(dens, "r_gt", 0.5)
