@@ -169,6 +169,32 @@ class Builder:
             va = va.clone() if va is not None else None
         return CsrResult(N, int(out.nnz), rp, ci, va, st.as_dict())
 
+    def corr_csr_avg(self, bolds, mode: str = "r_gt", value: float = 0.5,
+                     precision: str = "bf16x3", fisher: bool = False, weighted: bool = True,
+                     delta: Optional[float] = None, stream=None, copy: bool = True) -> CsrResult:
+        """Multi-subject average (to_average y/b, optional Fisher z) -> thresholded
+        CSR.  bolds: torch CUDA float32 [T_k][N] tensors, same N."""
+        import torch
+        N = bolds[0].shape[1]
+        assert all(b.is_cuda and b.dtype == torch.float32 and b.is_contiguous() and
+                   b.shape[1] == N for b in bolds)
+        ptrs = (C.c_void_p * len(bolds))(*[b.data_ptr() for b in bolds])
+        Ts = (C.c_int32 * len(bolds))(*[b.shape[0] for b in bolds])
+        o = _opts(mode, value, precision, weighted, delta)
+        out = L.Csr()
+        st = L.CorrStats()
+        _check(lib().bna_corr_csr_avg(self._h, len(bolds), ptrs, N, Ts, 1 if fisher else 0,
+                                      C.byref(o), C.byref(out), C.byref(st),
+                                      self._stream(stream)), self._h)
+        dev = bolds[0].device
+        rp = _view(out.row_ptr, N + 1, "<i4", torch, dev)
+        ci = _view(out.col_idx, out.nnz, "<i4", torch, dev)
+        va = _view(out.val, out.nnz, "<f4", torch, dev) if out.val else None
+        if copy:
+            rp, ci = rp.clone(), ci.clone()
+            va = va.clone() if va is not None else None
+        return CsrResult(N, int(out.nnz), rp, ci, va, st.as_dict())
+
     def rethreshold(self, csr: CsrResult, mode: str, value: float, stream=None,
                     copy: bool = True) -> CsrResult:
         """CSR at a higher threshold of the same rule, derived from `csr` (the

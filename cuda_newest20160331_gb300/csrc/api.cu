@@ -59,6 +59,13 @@ cudaError_t launch_rethr_count(const CorrArgs& a, const int32_t* rp, const int32
 cudaError_t launch_rethr_fill(int n, const int32_t* rp, const int32_t* ci, const float* valx,
                               const uint8_t* keep, const int32_t* rp2, int32_t* ci2, float* val2,
                               long long nnz2, uint32_t* err, int sms, cudaStream_t st);
+cudaError_t launch_corr_packed(const CorrArgs& a, int pass, cudaStream_t stream);
+cudaError_t launch_avg_finalize(float* packed, long long m, int S, int fisher, int sms,
+                                cudaStream_t st);
+cudaError_t launch_avg_exact(const CorrArgs& a, const void* subj, int S, int fisher, float* out,
+                             int sms, cudaStream_t st);
+size_t avg_subj_bytes();
+void avg_subj_fill(void* host, int s, const float* z, const uint8_t* bad, int ldz, int T);
 size_t dens_state_bytes();
 size_t dens_ties_cap();
 void dens_state_read(const void* host, int* err, float* tau, long long* n_exact,
@@ -84,7 +91,8 @@ enum Slot {
   S_EC_R, S_EC_C, S_EC_V, S_EC_VD, S_DUMP, S_TILES, S_BLOCKBAD, S_DUMPTILE, S_ELIST, S_ETAB, S_HIST, S_CANDVAL,
   S_DENSE, S_WSTATE, S_VSTAT,
   S_TILES_SMP, S_DSTATE, S_DHIST, S_DCLS, S_DEIDX, S_DEXACT, S_CANDAPX, S_DTIES,
-  S_RT_KEEP, S_RT_VALX, S_RT_ROWPTR, S_RT_COL, S_RT_VAL, S_COUNT
+  S_RT_KEEP, S_RT_VALX, S_RT_ROWPTR, S_RT_COL, S_RT_VAL,
+  S_AVG_Z, S_AVG_BAD, S_AVG_PACKED, S_AVG_UNC, S_AVG_BADZ, S_AVG_SUBJ, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -133,6 +141,14 @@ struct bna_ctx {
   // what bna_csr_rethreshold recomputes exact values from
   CorrArgs last{};
   bool last_ok = false;
+  // multi-subject average in progress (bna_corr_csr_avg): subject table on the
+  // device, count, Fisher flag
+  struct Avg {
+    const void* subj;
+    int S;
+    int fisher;
+  };
+  const Avg* avg = nullptr;
   cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
   long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
 };
@@ -293,6 +309,11 @@ long long elist_chunk(const bna_ctx* ctx, const CorrArgs& a) {
 // sampled tile list, tensor-core forms)
 int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st,
                   bool sampled = false) {
+  if (ctx->avg) {  // the averaged matrix is the source
+    CK(launch_corr_packed(a, pass, st));
+    ctx->klaunch += 1;
+    return BNA_OK;
+  }
   switch (precision) {
     case BNA_PREC_FP32:
       CK(launch_corr_simt(a, pass, st));
@@ -486,6 +507,10 @@ int32_t bna_zscore(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T, fl
   return BNA_OK;
 }
 
+static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
+                             const bna_corr_opts* opts, int prec, double delta, bna_csr* out_dev,
+                             bna_corr_stats* stats, cudaStream_t st);
+
 int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
                      const bna_corr_opts* opts, bna_csr* out_dev, bna_corr_stats* stats,
                      void* stream) {
@@ -514,6 +539,17 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   }
   CK(cudaEventRecord(ctx->ev[1], st));
   const double delta = opts->delta > 0 ? opts->delta : default_delta(prec, T);
+  return corr_csr_core(ctx, a, N, T, opts, prec, delta, out_dev, stats, st);
+}
+
+// Everything after the z-scores: count pass(es), candidates, density rule,
+// scan, fill.  With ctx->avg set (multi-subject average) the count pass reads
+// the averaged matrix and candidates get their exact averaged value.
+static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
+                             const bna_corr_opts* opts, int prec, double delta, bna_csr* out_dev,
+                             bna_corr_stats* stats, cudaStream_t st) {
+  const bool density = opts->mode == BNA_THR_DENSITY;
+  int32_t s = BNA_OK;
   a.weighted = opts->weighted ? 1 : 0;
 
   ENSURE(S_SEG, (size_t)a.nb * a.n_pad * sizeof(int32_t), a.seg);
@@ -539,7 +575,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   // ---- threshold of the count pass
   long long k_dens = 0;  // density: exact undirected edge count (CorMat.cpp:327-329)
   if (density) k_dens = bna_density_nnz(N, opts->value) / 2;
-  const bool tc = prec != BNA_PREC_FP32;
+  const bool tc = prec != BNA_PREC_FP32 && !ctx->avg;
   // density with a tensor-core form: the k-th value is selected on the device;
   // its window comes first from a histogram of sampled tiles, and from the
   // full histogram if the sample's window missed
@@ -622,7 +658,8 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
       ENSURE(S_HVAL, hcap * 4, a.hval);
       ENSURE(S_HEDGE, hcap, a.hedge);
       ENSURE(S_ELIST, (size_t)a.ecap * sizeof(uint2), a.elist);
-      if (density && k_dens > 0) ENSURE(S_CANDVAL, (size_t)a.cand_cap * sizeof(float), cvals);
+      if ((density && k_dens > 0) || ctx->avg)
+        ENSURE(S_CANDVAL, (size_t)a.cand_cap * sizeof(float), cvals);
       a.cand_apx = nullptr;
       if (dev_sel) ENSURE(S_CANDAPX, (size_t)a.cand_cap * sizeof(float), a.cand_apx);
       CK(cudaMemsetAsync(ds, 0, sizeof(DevStatus), st));
@@ -663,9 +700,19 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
         CK(cudaMemcpyAsync(static_cast<char*>(ctx->pinned) + 2048, dstate, dens_state_bytes(),
                            cudaMemcpyDeviceToHost, st));
       } else if (density && k_dens > 0) {
-        CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
+        if (ctx->avg)
+          CK(launch_avg_exact(a, ctx->avg->subj, ctx->avg->S, ctx->avg->fisher, cvals, ctx->sms,
+                              st));
+        else
+          CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
         ctx->klaunch += 1;
       } else {
+        if (ctx->avg) {  // exact averaged values, then the decisions on them
+          CK(launch_avg_exact(a, ctx->avg->subj, ctx->avg->S, ctx->avg->fisher, cvals, ctx->sms,
+                              st));
+          a.cand_val = cvals;
+          ctx->klaunch += 1;
+        }
         CK(launch_recompute(a, ctx->sms * 8, st));
         ctx->klaunch += 1 + 4;  // recompute, scan
         CK(cudaEventRecord(ctx->ev[3], st));
@@ -821,7 +868,7 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
   out_dev->val = val;
   ctx->last = a;
   ctx->last.th.delta = (float)delta;
-  ctx->last_ok = !density && a.weighted;
+  ctx->last_ok = !density && a.weighted && !ctx->avg;
   if (stats) {
     std::memset(stats, 0, sizeof *stats);
     stats->tau = density && k_dens == 0 ? INFINITY : (double)a.th.tau;
@@ -955,6 +1002,119 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
     default: return fail(ctx, BNA_UNSUPPORTED, "precision %d is not built", precision);
   }
   return BNA_OK;
+}
+
+int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
+                         const int32_t* T, int32_t fisher, const bna_corr_opts* opts,
+                         bna_csr* out_dev, bna_corr_stats* stats, void* stream) {
+  if (!ctx || nsub < 1 || !bold_dev || !T || N < 2 || !opts || !out_dev)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad arguments");
+  for (int k = 0; k < nsub; ++k)
+    if (!bold_dev[k] || T[k] < 1)
+      return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: subject %d: bad arguments", k);
+  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
+      (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad threshold rule");
+  const int prec = opts->precision;
+  if (prec != BNA_PREC_BF16X3 && prec != BNA_PREC_TF32)
+    return fail(ctx, BNA_UNSUPPORTED, "bna_corr_csr_avg: a tensor-core form is required");
+  int32_t s = set_device(ctx, as_stream(stream));
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  ctx->klaunch = 0;
+  ctx->last_ok = false;
+  const int n_pad = round_up(N, kBlk), nb = n_pad / kBlk;
+  const long long M1 = (long long)N * (N - 1) / 2;
+  size_t zoff_total = 0;
+  int ldb_max = 0;
+  std::vector<size_t> zoff(nsub);
+  for (int k = 0; k < nsub; ++k) {
+    zoff[k] = zoff_total;
+    zoff_total += (size_t)n_pad * round_up(T[k], 32);
+    ldb_max = std::max(ldb_max, round_up(T[k], 64));
+  }
+  float *zall, *packed;
+  uint8_t *badall, *badz;
+  uint32_t* unc;
+  void* subj_dev;
+  void* vstat;
+  uint16_t *zhi = nullptr, *zlo = nullptr;
+  ENSURE(S_AVG_Z, zoff_total * sizeof(float), zall);
+  ENSURE(S_AVG_BAD, (size_t)nsub * n_pad, badall);
+  ENSURE(S_AVG_PACKED, (size_t)M1 * sizeof(float), packed);
+  ENSURE(S_AVG_UNC, (size_t)((M1 + 31) / 32) * sizeof(uint32_t), unc);
+  ENSURE(S_AVG_BADZ, (size_t)n_pad, badz);
+  ENSURE(S_AVG_SUBJ, (size_t)nsub * avg_subj_bytes(), subj_dev);
+  ENSURE(S_VSTAT, zscore_scratch_bytes(n_pad), vstat);
+  if (prec == BNA_PREC_BF16X3) {
+    ENSURE(S_ZHI, (size_t)n_pad * ldb_max * 2, zhi);
+    ENSURE(S_ZLO, (size_t)n_pad * ldb_max * 2, zlo);
+  }
+  CK(cudaMemsetAsync(packed, 0, (size_t)M1 * sizeof(float), st));
+  CK(cudaMemsetAsync(unc, 0, (size_t)((M1 + 31) / 32) * sizeof(uint32_t), st));
+  CK(cudaMemsetAsync(badz, 0, (size_t)n_pad, st));
+  CK(cudaEventRecord(ctx->ev[0], st));
+  std::vector<char> subj_host((size_t)nsub * avg_subj_bytes());
+  double dsum = 0;
+  for (int k = 0; k < nsub; ++k) {
+    // subject k: z-scores (kept for the exact recompute), then its values
+    // added into the packed sums in file order (pass 4)
+    CorrArgs as{};
+    as.n = N;
+    as.n_pad = n_pad;
+    as.nb = nb;
+    as.T = T[k];
+    as.ldz = round_up(T[k], 32);
+    as.ldb = round_up(T[k], 64);
+    as.z = zall + zoff[k];
+    as.zhi = zhi;
+    as.zlo = zlo;
+    as.bad = badall + (size_t)k * n_pad;
+    CK(launch_zscore(bold_dev[k], N, T[k], n_pad, const_cast<float*>(as.z), as.ldz, zhi, zlo,
+                     as.ldb, const_cast<uint8_t*>(as.bad), vstat, st));
+    ctx->klaunch += 2;
+    s = tc_prepare(ctx, as, st);
+    if (s) return s;
+    const double dk = opts->delta > 0 ? opts->delta : default_delta(prec, T[k]);
+    dsum += dk;
+    as.th.mode = BNA_THR_R_GE;
+    as.th.tau = 2.0f;
+    as.th.delta = (float)dk;
+    AvgPass ap{packed, unc, fisher ? 1 : 0, fisher ? 0.9f : (float)(1.0 - dk)};
+    const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[S_TILES]);
+    const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : ctx->ntiles;
+    for (int t0 = 0; t0 < ctx->ntiles; t0 += per, ++ctx->klaunch)
+      CK(launch_corr_tc(as, 4, prec == BNA_PREC_BF16X3 ? 0 : 1, tiles + t0,
+                        std::min(per, ctx->ntiles - t0),
+                        reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
+                        ctx->sms, st, &ap));
+    avg_subj_fill(subj_host.data(), k, as.z, as.bad, as.ldz, T[k]);
+  }
+  CK(cudaMemcpyAsync(subj_dev, subj_host.data(), subj_host.size(), cudaMemcpyHostToDevice, st));
+  CK(launch_avg_finalize(packed, M1, nsub, fisher ? 1 : 0, ctx->sms, st));
+  ctx->klaunch += 1;
+  CK(cudaEventRecord(ctx->ev[1], st));
+  // bound of |average~ - average| (per-subject bounds, the float sums and
+  // division; with Fisher z the transform's slope below |r| = 0.91, larger
+  // |r~| being uncertain pairs that are always recomputed)
+  const double dmean = dsum / nsub;
+  const double u24 = std::ldexp(1.0, -24);
+  const double davg = fisher ? 6.0 * dmean + 4e-6 + (nsub + 2) * 4.0 * u24
+                             : dmean + (nsub + 1) * u24 + 4.0 * u24;
+  CorrArgs a{};
+  a.n = N;
+  a.n_pad = n_pad;
+  a.nb = nb;
+  a.T = 1;
+  a.ldz = 32;
+  a.bad = badz;
+  a.avg_packed = packed;
+  a.avg_unc = unc;
+  const bna_ctx::Avg ac{subj_dev, nsub, fisher ? 1 : 0};
+  ctx->avg = &ac;
+  s = corr_csr_core(ctx, a, N, 1, opts, prec, davg, out_dev, stats, st);
+  ctx->avg = nullptr;
+  return s;
 }
 
 int32_t bna_csr_rethreshold(bna_ctx* ctx, const bna_csr* in_dev, int32_t mode, double tau,

@@ -13,11 +13,11 @@ namespace bna {
 // t = lane, lane+32, ..., the exact sum is an int64 fixed-point reduction
 // across the warp, and only when the condition fails does lane 0 run the
 // sequential double adds.  Returns the value after post_block's clamp.
-__device__ __forceinline__ float exact_r_warp(const CorrArgs& a, int i, int j, int lane) {
-  if (a.bad[i] | a.bad[j]) return 0.0f;  // NaN -> 0 in post_block
-  const float* zi = a.z + (size_t)i * a.ldz;
-  const float* zj = a.z + (size_t)j * a.ldz;
-  const int T = a.T;
+__device__ __forceinline__ float exact_r_warp_z(const float* z, const uint8_t* bad, int ldz,
+                                                int T, int i, int j, int lane) {
+  if (bad[i] | bad[j]) return 0.0f;  // NaN -> 0 in post_block
+  const float* zi = z + (size_t)i * ldz;
+  const float* zj = z + (size_t)j * ldz;
   int emin = 1 << 20;
   bool special = false;
   for (int t = lane; t < T; t += 32) {
@@ -65,6 +65,10 @@ __device__ __forceinline__ float exact_r_warp(const CorrArgs& a, int i, int j, i
     }
   }
   return post_block(__shfl_sync(0xffffffffu, r, 0));
+}
+
+__device__ __forceinline__ float exact_r_warp(const CorrArgs& a, int i, int j, int lane) {
+  return exact_r_warp_z(a.z, a.bad, a.ldz, a.T, i, j, lane);
 }
 
 // Binary search in ascending keys[0..n).

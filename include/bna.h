@@ -168,6 +168,18 @@ int32_t bna_corr_csr_host_into(bna_ctx* ctx, const float* bold_host, int32_t N, 
                                int32_t* col_idx_host, float* val_host, int64_t cap,
                                int64_t* nnz_out, bna_corr_stats* stats);
 
+/* Multi-subject average, the reference's to_average modes (y / b with f or n,
+ * W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:418-670): every subject's r (post_block:
+ * only values in [-1, 1] count; with fisher = 1 its Fisher z, fishertrans
+ * :36-42) is added in subject order into one matrix, divided by nsub (then
+ * inv_fishertrans :44-50), and thresholded like one subject's matrix (opts:
+ * any rule, a tensor-core form).  bold_dev[k] is subject k's time-major
+ * [T[k]][N] series (same voxels for all subjects).  Device memory: the packed
+ * averaged matrix (N(N-1)/2 floats) and every subject's z-scores. */
+int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
+                         const int32_t* T, int32_t fisher, const bna_corr_opts* opts,
+                         bna_csr* out_dev, bna_corr_stats* stats, void* stream);
+
 /* Several thresholds from one correlation pass (the reference thresholds one
  * correlation matrix once per value of its threshold list,
  * W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:105-111, 318-341).  in_dev must be the

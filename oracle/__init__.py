@@ -53,6 +53,8 @@ def lib():
         o.orc_rows_mt_f32_count.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
                                             C.c_int]
         o.orc_rows_mt_f32_count.restype = C.c_int64
+        o.orc_avg_accumulate.argtypes = [P, C.c_int64, C.c_int, P]
+        o.orc_avg_finalize.argtypes = [P, C.c_int64, C.c_int, C.c_int]
         _o = o
     return _o
 
@@ -111,6 +113,19 @@ def cormat_packed(z: np.ndarray, threads: int = 0) -> np.ndarray:
     out = np.empty(N * (N - 1) // 2, np.float32)
     lib().orc_cormat_packed(_p(z), N, T, _p(out), threads or (os.cpu_count() or 1))
     return out
+
+
+def avg_packed(bolds, fisher: bool = False, threads: int = 0) -> np.ndarray:
+    """Multi-subject average of the reference (packed, post_block accumulation
+    in subject order, division, optional Fisher transforms)."""
+    N = bolds[0].shape[1]
+    m = N * (N - 1) // 2
+    acc = np.zeros(m, np.float32)
+    for b in bolds:
+        P = cormat_packed(zscore(b), threads)
+        lib().orc_avg_accumulate(_p(P), m, 1 if fisher else 0, _p(acc))
+    lib().orc_avg_finalize(_p(acc), m, len(bolds), 1 if fisher else 0)
+    return acc
 
 
 def threshold_csr(packed: np.ndarray, N: int, mode: str, tau: float, drop=None,

@@ -14,6 +14,9 @@
  *                       |r| rule of U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:198
  *   orc_density         FormFullGraph_s + select   CorMat.cpp:705-822, 327-329
  *   orc_ec              Lead_Vector_GPU            W/CUEC/weighted-net.cu:55-221 (FP64)
+ *   orc_avg_accumulate  multi-subject average      CorMat.cpp:847-883 (post_block with
+ *   orc_avg_finalize                               accumulation, fishertrans :36-42),
+ *                                                  :652-666 (division, inv_fishertrans :44-50)
  *   orc_cormat_mt_f32   CorMat_cpu_MT/Cross_term   U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:283-383
  *                       (float accumulation; used as the multi-core CPU baseline)
  * Built with -ffp-contract=off so every operation rounds like the reference's
@@ -411,4 +414,33 @@ int64_t orc_rows_mt_f32_count(const float* bold, int N, int L, int row0, int row
   free(bt);
   free(m2);
   return total;
+}
+
+/* fishertrans / inv_fishertrans (CorMat.cpp:36-50) in the reference's float
+ * arithmetic: log and exp of a float argument are the float functions there
+ * (C++ overloads), logf / expf here. */
+static float orc_fisher_z(float r) {
+  if (r == 1.0f) r = (float)((double)r - 1e-6);
+  return (float)(0.5 * (double)logf((1.0f + r) / (1.0f - r)));
+}
+static float orc_fisher_r(float z) {
+  float r = expf(2.0f * z);
+  return (r - 1.0f) / (r + 1.0f);
+}
+
+/* One subject's post_block'd packed r (values outside [-1, 1] already 0,
+ * which adds nothing) added into acc in float: post_block's accumulation. */
+void orc_avg_accumulate(const float* packed_r, long long m, int fisher, float* acc) {
+  for (long long i = 0; i < m; ++i) {
+    const float r = packed_r[i];
+    if (r >= -1.0f && r <= 1.0f) acc[i] += fisher ? orc_fisher_z(r) : r;
+  }
+}
+
+/* acc / nsub, then inv_fishertrans when fisher (CorMat.cpp:652-666). */
+void orc_avg_finalize(float* acc, long long m, int nsub, int fisher) {
+  for (long long i = 0; i < m; ++i) {
+    acc[i] /= (float)nsub;
+    if (fisher) acc[i] = orc_fisher_r(acc[i]);
+  }
 }

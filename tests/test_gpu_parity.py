@@ -358,3 +358,54 @@ def test_rethreshold_refuses_lower_tau_and_other_rules(builder):
     dens = builder.corr_csr(dev(b), mode="density", value=2.0, precision="bf16x3")
     with pytest.raises(bna.BnaError):
         builder.rethreshold(dens, "r_gt", 0.5)
+
+
+def _avg_subjects(N=1500, Ts=(120, 200, 160), seed=60):
+    out = []
+    for k, T in enumerate(Ts):
+        b = bna.synth_bold(N, T, 15, seed + k)
+        out.append(b)
+    out[1][:, 5] = 1.0  # a zero-variance voxel in one subject
+    return out
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("mode,value", [("r_gt", 0.25), ("density", 1.5)])
+def test_average_matches_oracle(builder, precision, mode, value):
+    """to_average y/yn: subjects' r summed in order, divided; thresholded.
+    Plain average: float arithmetic only, so the CSR is bit-exact."""
+    bolds = _avg_subjects()
+    N = bolds[0].shape[1]
+    A = oracle.avg_packed(bolds)
+    res = builder.corr_csr_avg([dev(b) for b in bolds], mode=mode, value=value,
+                               precision=precision)
+    if mode == "density":
+        tau, k, drop = oracle.density(A, N, value)
+        R, C, V = oracle.threshold_csr(A, N, "r_ge", tau, drop=drop)
+        assert res.nnz == 2 * k
+    else:
+        R, C, V = oracle.threshold_csr(A, N, mode, value)
+    assert_csr_equal(res, R, C, V, res.stats["delta"])
+
+
+def test_average_fisher_matches_oracle(builder):
+    """to_average yf: Fisher z averaged, transformed back.  log/exp come from
+    different math libraries on the two sides, so pairs within 1e-5 of tau
+    may differ; every other pair must agree."""
+    bolds = _avg_subjects(seed=70)
+    N = bolds[0].shape[1]
+    tau = 0.25
+    A = oracle.avg_packed(bolds, fisher=True)
+    R, C, V = oracle.threshold_csr(A, N, "r_gt", tau)
+    g = builder.corr_csr_avg([dev(b) for b in bolds], mode="r_gt", value=tau, fisher=True,
+                             precision="bf16x3").numpy()
+
+    def pairs(rp, ci):
+        rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+        return set(zip(rows.tolist(), ci.tolist()))
+    diff = pairs(g.row_ptr, g.col_idx) ^ pairs(R, C)
+    for i, j in diff:
+        a, b = min(i, j), max(i, j)
+        v = A[a * (2 * N - a - 1) // 2 + b - a - 1]
+        assert abs(v - tau) <= 1e-5, (i, j, v)
+    assert len(diff) <= 10

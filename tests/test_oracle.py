@@ -151,3 +151,35 @@ def test_float_accumulating_mt_tool_close_to_reference():
         bb = np.ascontiguousarray(b)
         r.ref_u_cormat_cpu_mt(out.ctypes.data, bb.ctypes.data, 300, 120, 4)
         assert np.array_equal(out, P)
+
+
+@pytest.mark.parametrize("fisher", [0, 1])
+def test_avg_accumulation_matches_reference_post_block(fisher):
+    """The averaging restatement adds a subject like the reference's
+    post_block with accumulation (CorMat.cpp:847-883, fishertrans :36-42),
+    including values outside [-1, 1], NaN, and r = +-1 exactly."""
+    r = oracle.ref_w()
+    if r is None:
+        pytest.skip("reference tree not present on this host")
+    import cuda_newest20160331_gb300 as bna
+    N, B = 300, 128
+    nbk = (N + B - 1) // B
+    m = N * (N - 1) // 2
+    iu, ju = np.triu_indices(N, 1)
+    acc_ref = np.zeros(m, np.float32)
+    acc_orc = np.zeros(m, np.float32)
+    for s in range(3):
+        P = oracle.cormat_packed(oracle.zscore(bna.synth_bold(N, 40, 8, 90 + s)))
+        P[:: 97] = 1.0
+        P[5:: 211] = -1.0
+        P[7:: 389] = 1.5
+        P[11:: 401] = np.nan
+        # the reference's blocked layout of the upper-triangle tiles
+        blocked = np.zeros(nbk * (nbk + 1) // 2 * B * B, np.float32)
+        br, bc = iu // B, ju // B
+        off = (br * (2 * nbk - br + 1) // 2 + bc - br) * B * B
+        blocked[off + (iu % B) * B + (ju % B)] = P
+        r.ref_w_post_block(acc_ref.ctypes.data, blocked.ctypes.data, N, B, fisher)
+        clamp = np.where((P >= -1) & (P <= 1), P, np.float32(0)).astype(np.float32)
+        oracle.lib().orc_avg_accumulate(clamp.ctypes.data, m, fisher, acc_orc.ctypes.data)
+    assert np.array_equal(acc_ref, acc_orc)
