@@ -27,7 +27,8 @@ from . import _lib as L
 from ._lib import BnaError, lib
 
 __all__ = ["Builder", "CsrResult", "Server", "Reply", "synth_bold", "csr_write", "csr_read",
-           "ec_write", "request_bytes", "density_nnz", "BnaError", "lib"]
+           "ec_write", "request_bytes", "density_nnz", "nifti_mask", "nifti_bold", "BnaError",
+           "lib"]
 
 
 def _check(status: int, ctx=None, ok=(L.BNA_OK,)) -> int:
@@ -423,6 +424,30 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def nifti_mask(path: str, cut: float):
+    """-> (sel uint8 [total], N, dims) for the voxels with mask >= cut (bna_nifti_mask)."""
+    dims = (C.c_int32 * 3)()
+    total = C.c_int64()
+    n = C.c_int32()
+    _check(lib().bna_nifti_mask(os.fsencode(path), float(cut), dims, C.byref(total), C.byref(n),
+                                None))
+    sel = np.empty(total.value, np.uint8)
+    _check(lib().bna_nifti_mask(os.fsencode(path), float(cut), dims, C.byref(total), C.byref(n),
+                                sel.ctypes.data))
+    return sel, n.value, tuple(dims)
+
+
+def nifti_bold(path: str, sel: np.ndarray, N: int) -> np.ndarray:
+    """Time-major float32 [T][N] series of the selected voxels (bna_nifti_bold)."""
+    T = C.c_int32()
+    _check(lib().bna_nifti_bold(os.fsencode(path), sel.ctypes.data, len(sel), N, None,
+                                C.byref(T)))
+    out = np.empty((T.value, N), np.float32)
+    _check(lib().bna_nifti_bold(os.fsencode(path), sel.ctypes.data, len(sel), N,
+                                out.ctypes.data, C.byref(T)))
+    return out
 
 
 def csr_write(path: str, row_ptr: np.ndarray, col_idx: np.ndarray,

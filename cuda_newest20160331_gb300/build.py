@@ -20,6 +20,7 @@ ROOT = os.path.dirname(PKG)
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libbna.so")
+BIN = os.path.join(PKG, "bin")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -88,6 +89,19 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "shared",
               "-Xlinker", f"-rpath,{libdir}", "-lpthread"], verbose)
         os.replace(tmp, LIB)
+    # command-line drop-ins (cli/*.cpp -> bin/bna_<name>), linked to libbna.so
+    os.makedirs(BIN, exist_ok=True)
+    tools = []
+    for src in sorted(glob.glob(os.path.join(PKG, "cli", "*.cpp"))):
+        exe = os.path.join(BIN, "bna_" + os.path.splitext(os.path.basename(src))[0])
+        if _stale(exe, src, deps + [LIB]):
+            tools.append(["g++", "-O2", "-std=c++17", src, "-o", exe, "-I", INCLUDE,
+                          "-I", os.path.join(cuda, "include"), "-L", PKG, "-lbna",
+                          "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                          "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath," + os.path.join(cuda, "lib64")])
+    if tools:
+        with ThreadPoolExecutor(max_workers=len(tools)) as ex:
+            list(ex.map(lambda c: _run(c, verbose), tools))
     return LIB
 
 

@@ -1004,25 +1004,13 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
   return BNA_OK;
 }
 
-int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
-                         const int32_t* T, int32_t fisher, const bna_corr_opts* opts,
-                         bna_csr* out_dev, bna_corr_stats* stats, void* stream) {
-  if (!ctx || nsub < 1 || !bold_dev || !T || N < 2 || !opts || !out_dev)
-    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad arguments");
-  for (int k = 0; k < nsub; ++k)
-    if (!bold_dev[k] || T[k] < 1)
-      return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: subject %d: bad arguments", k);
-  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
-      (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
-    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad threshold rule");
-  const int prec = opts->precision;
-  if (prec != BNA_PREC_BF16X3 && prec != BNA_PREC_TF32)
-    return fail(ctx, BNA_UNSUPPORTED, "bna_corr_csr_avg: a tensor-core form is required");
-  int32_t s = set_device(ctx, as_stream(stream));
-  if (s) return s;
-  cudaStream_t st = as_stream(stream);
-  ctx->klaunch = 0;
-  ctx->last_ok = false;
+// The multi-subject sums: every subject's z-scores (kept in the arena for the
+// exact recompute; their table goes to subj_dev) and pass 4 over all tiles,
+// into packed / unc (zeroed here), then the division / inverse transform.
+static int32_t avg_accumulate(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev,
+                              int32_t N, const int32_t* T, int fisher, int prec, double delta_opt,
+                              float* packed, uint32_t* unc, void** subj_dev_out, double* dsum,
+                              cudaStream_t st) {
   const int n_pad = round_up(N, kBlk), nb = n_pad / kBlk;
   const long long M1 = (long long)N * (N - 1) / 2;
   size_t zoff_total = 0;
@@ -1033,17 +1021,13 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
     zoff_total += (size_t)n_pad * round_up(T[k], 32);
     ldb_max = std::max(ldb_max, round_up(T[k], 64));
   }
-  float *zall, *packed;
-  uint8_t *badall, *badz;
-  uint32_t* unc;
+  float* zall;
+  uint8_t* badall;
   void* subj_dev;
   void* vstat;
   uint16_t *zhi = nullptr, *zlo = nullptr;
   ENSURE(S_AVG_Z, zoff_total * sizeof(float), zall);
   ENSURE(S_AVG_BAD, (size_t)nsub * n_pad, badall);
-  ENSURE(S_AVG_PACKED, (size_t)M1 * sizeof(float), packed);
-  ENSURE(S_AVG_UNC, (size_t)((M1 + 31) / 32) * sizeof(uint32_t), unc);
-  ENSURE(S_AVG_BADZ, (size_t)n_pad, badz);
   ENSURE(S_AVG_SUBJ, (size_t)nsub * avg_subj_bytes(), subj_dev);
   ENSURE(S_VSTAT, zscore_scratch_bytes(n_pad), vstat);
   if (prec == BNA_PREC_BF16X3) {
@@ -1052,13 +1036,10 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
   }
   CK(cudaMemsetAsync(packed, 0, (size_t)M1 * sizeof(float), st));
   CK(cudaMemsetAsync(unc, 0, (size_t)((M1 + 31) / 32) * sizeof(uint32_t), st));
-  CK(cudaMemsetAsync(badz, 0, (size_t)n_pad, st));
-  CK(cudaEventRecord(ctx->ev[0], st));
   std::vector<char> subj_host((size_t)nsub * avg_subj_bytes());
-  double dsum = 0;
+  *dsum = 0;
   for (int k = 0; k < nsub; ++k) {
-    // subject k: z-scores (kept for the exact recompute), then its values
-    // added into the packed sums in file order (pass 4)
+    // subject k: z-scores, then its values added into the sums in file order
     CorrArgs as{};
     as.n = N;
     as.n_pad = n_pad;
@@ -1073,10 +1054,10 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
     CK(launch_zscore(bold_dev[k], N, T[k], n_pad, const_cast<float*>(as.z), as.ldz, zhi, zlo,
                      as.ldb, const_cast<uint8_t*>(as.bad), vstat, st));
     ctx->klaunch += 2;
-    s = tc_prepare(ctx, as, st);
+    int32_t s = tc_prepare(ctx, as, st);
     if (s) return s;
-    const double dk = opts->delta > 0 ? opts->delta : default_delta(prec, T[k]);
-    dsum += dk;
+    const double dk = delta_opt > 0 ? delta_opt : default_delta(prec, T[k]);
+    *dsum += dk;
     as.th.mode = BNA_THR_R_GE;
     as.th.tau = 2.0f;
     as.th.delta = (float)dk;
@@ -1093,6 +1074,53 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
   CK(cudaMemcpyAsync(subj_dev, subj_host.data(), subj_host.size(), cudaMemcpyHostToDevice, st));
   CK(launch_avg_finalize(packed, M1, nsub, fisher ? 1 : 0, ctx->sms, st));
   ctx->klaunch += 1;
+  CK(cudaStreamSynchronize(st));  // subj_host is released at return
+  *subj_dev_out = subj_dev;
+  return BNA_OK;
+}
+
+static int32_t avg_check(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
+                         const int32_t* T, int prec) {
+  if (!ctx || nsub < 1 || !bold_dev || !T || N < 2)
+    return fail(ctx, BNA_BAD_ARG, "multi-subject call: bad arguments");
+  for (int k = 0; k < nsub; ++k)
+    if (!bold_dev[k] || T[k] < 1)
+      return fail(ctx, BNA_BAD_ARG, "subject %d: bad arguments", k);
+  if (prec != BNA_PREC_BF16X3 && prec != BNA_PREC_TF32)
+    return fail(ctx, BNA_UNSUPPORTED, "multi-subject call: a tensor-core form is required");
+  return BNA_OK;
+}
+
+int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
+                         const int32_t* T, int32_t fisher, const bna_corr_opts* opts,
+                         bna_csr* out_dev, bna_corr_stats* stats, void* stream) {
+  if (!opts || !out_dev) return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad arguments");
+  int32_t s = avg_check(ctx, nsub, bold_dev, N, T, opts->precision);
+  if (s) return s;
+  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
+      (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad threshold rule");
+  const int prec = opts->precision;
+  s = set_device(ctx, as_stream(stream));
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  ctx->klaunch = 0;
+  ctx->last_ok = false;
+  const int n_pad = round_up(N, kBlk), nb = n_pad / kBlk;
+  const long long M1 = (long long)N * (N - 1) / 2;
+  float* packed;
+  uint32_t* unc;
+  uint8_t* badz;
+  ENSURE(S_AVG_PACKED, (size_t)M1 * sizeof(float), packed);
+  ENSURE(S_AVG_UNC, (size_t)((M1 + 31) / 32) * sizeof(uint32_t), unc);
+  ENSURE(S_AVG_BADZ, (size_t)n_pad, badz);
+  CK(cudaMemsetAsync(badz, 0, (size_t)n_pad, st));
+  CK(cudaEventRecord(ctx->ev[0], st));
+  void* subj_dev = nullptr;
+  double dsum = 0;
+  s = avg_accumulate(ctx, nsub, bold_dev, N, T, fisher, prec, opts->delta, packed, unc,
+                     &subj_dev, &dsum, st);
+  if (s) return s;
   CK(cudaEventRecord(ctx->ev[1], st));
   // bound of |average~ - average| (per-subject bounds, the float sums and
   // division; with Fisher z the transform's slope below |r| = 0.91, larger
@@ -1115,6 +1143,26 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
   s = corr_csr_core(ctx, a, N, 1, opts, prec, davg, out_dev, stats, st);
   ctx->avg = nullptr;
   return s;
+}
+
+int32_t bna_corr_packed(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
+                        const int32_t* T, int32_t fisher, int32_t precision, float* packed_dev,
+                        void* stream) {
+  int32_t s = avg_check(ctx, nsub, bold_dev, N, T, precision);
+  if (s) return s;
+  if (!packed_dev) return fail(ctx, BNA_BAD_ARG, "bna_corr_packed: packed_dev is NULL");
+  s = set_device(ctx, as_stream(stream));
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  ctx->klaunch = 0;
+  ctx->last_ok = false;
+  const long long M1 = (long long)N * (N - 1) / 2;
+  uint32_t* unc;
+  ENSURE(S_AVG_UNC, (size_t)((M1 + 31) / 32) * sizeof(uint32_t), unc);
+  void* subj_dev = nullptr;
+  double dsum = 0;
+  return avg_accumulate(ctx, nsub, bold_dev, N, T, fisher, precision, 0.0, packed_dev, unc,
+                        &subj_dev, &dsum, st);
 }
 
 int32_t bna_csr_rethreshold(bna_ctx* ctx, const bna_csr* in_dev, int32_t mode, double tau,

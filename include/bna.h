@@ -180,6 +180,27 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
                          const int32_t* T, int32_t fisher, const bna_corr_opts* opts,
                          bna_csr* out_dev, bna_corr_stats* stats, void* stream);
 
+/* The packed correlation matrix itself, the reference's .cormat content
+ * (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:301-310: r of every pair i < j,
+ * row-major, after post_block): approximate values of the chosen tensor-core
+ * form (within its error bound of the reference's r).  With nsub > 1 the
+ * multi-subject average of bna_corr_csr_avg.  packed_dev holds N(N-1)/2
+ * floats of device memory. */
+int32_t bna_corr_packed(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
+                        const int32_t* T, int32_t fisher, int32_t precision, float* packed_dev,
+                        void* stream);
+
+/* NIfTI-1 ingest (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:141-242).  Mask:
+ * datatype 2 or 16, a voxel is kept when mask >= cut; sel_out (total bytes,
+ * NULL to query the sizes) marks the kept voxels.  Series: float or double
+ * samples (bitpix 32 / 64) gathered for the kept voxels into bold_out, the
+ * time-major [T][N] layout (NULL: only *T_out is set).  BNA_CORRUPT_FILE for
+ * other types or short files. */
+int32_t bna_nifti_mask(const char* path, double cut, int32_t dims_out[3], int64_t* total_out,
+                       int32_t* n_out, uint8_t* sel_out);
+int32_t bna_nifti_bold(const char* path, const uint8_t* sel, int64_t total, int32_t N,
+                       float* bold_out, int32_t* T_out);
+
 /* Several thresholds from one correlation pass (the reference thresholds one
  * correlation matrix once per value of its threshold list,
  * W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:105-111, 318-341).  in_dev must be the

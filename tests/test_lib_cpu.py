@@ -150,3 +150,65 @@ def test_density_nnz_matches_oracle_rule():
     for N, s in [(4096, 1.0), (45000, 1.0), (85701, 1.539), (112510, 1.732), (10, 50.0),
                  (180000, 0.1), (3, 0.0)]:
         assert bna.density_nnz(N, s) == 2 * oracle.density_k(N, s), (N, s)
+
+
+def test_nifti_ingest_gathers_like_the_reference(tmp_path):
+    """Mask >= cut in linear voxel order, BOLD[t*N + i] time-major; float and
+    double series, uint8 and float masks (CorMat.cpp:141-242)."""
+    import numpy as np
+    import cuda_newest20160331_gb300 as bna
+    from nifti_util import write_nifti
+    rng = np.random.default_rng(3)
+    Z, Y, X, T = 4, 5, 6, 7
+    mask = rng.random((Z, Y, X)).astype(np.float32)
+    series = rng.standard_normal((T, Z, Y, X))
+    for mdt in (2, 16):
+        m = (mask * 2).astype(np.uint8) if mdt == 2 else mask
+        write_nifti(tmp_path / "mask.nii", m, mdt)
+        cut = 0.5
+        sel, N, dims = bna.nifti_mask(str(tmp_path / "mask.nii"), cut)
+        flat = m.reshape(-1).astype(np.float32)
+        assert dims == (X, Y, Z) and N == int((flat >= np.float32(cut)).sum())
+        for ddt in (16, 64):
+            write_nifti(tmp_path / "s.nii", series, ddt)
+            bold = bna.nifti_bold(str(tmp_path / "s.nii"), sel, N)
+            ref = series.reshape(T, -1)[:, flat >= np.float32(cut)].astype(np.float32)
+            assert bold.shape == (T, N) and np.array_equal(bold, ref)
+
+
+def test_nifti_rejects_other_types_and_short_files(tmp_path):
+    import numpy as np
+    import pytest
+    import cuda_newest20160331_gb300 as bna
+    from nifti_util import write_nifti
+    write_nifti(tmp_path / "m.nii", np.ones((2, 2, 2), np.float64), 64)
+    with pytest.raises(bna.BnaError) as e:
+        bna.nifti_mask(str(tmp_path / "m.nii"), 0.5)
+    assert e.value.status == 9  # BNA_CORRUPT_FILE
+    write_nifti(tmp_path / "m.nii", np.ones((2, 2, 2), np.uint8), 2)
+    sel, N, _ = bna.nifti_mask(str(tmp_path / "m.nii"), 0.5)
+    write_nifti(tmp_path / "s.nii", np.ones((3, 2, 2, 2), np.float32), 16)
+    raw = (tmp_path / "s.nii").read_bytes()
+    (tmp_path / "s.nii").write_bytes(raw[:-5])
+    with pytest.raises(bna.BnaError) as e:
+        bna.nifti_bold(str(tmp_path / "s.nii"), sel, N)
+    assert e.value.status == 9
+
+
+def test_cli_usage_and_argument_errors(tmp_path):
+    """bna_cormat / bna_cuec print the reference's usage and errors and exit 1
+    before touching a device."""
+    import os
+    import subprocess
+    import cuda_newest20160331_gb300 as bna
+    b = os.path.join(os.path.dirname(bna.__file__), "bin")
+    r = subprocess.run([os.path.join(b, "bna_cormat")], capture_output=True, text=True)
+    assert r.returncode == 1 and "Input format" in r.stderr
+    r = subprocess.run([os.path.join(b, "bna_cormat"), str(tmp_path), "m.nii", "0.5", "n",
+                        "q", "r", "0.3"], capture_output=True, text=True)
+    assert r.returncode == 1 and "to_save_cor_matrix type error" in r.stdout
+    r = subprocess.run([os.path.join(b, "bna_cormat"), str(tmp_path), "m.nii", "0.5", "n",
+                        "n", "x", "0.3"], capture_output=True, text=True)
+    assert r.returncode == 1 and "threshold type error" in r.stdout
+    r = subprocess.run([os.path.join(b, "bna_cuec")], capture_output=True, text=True)
+    assert r.returncode == 1
