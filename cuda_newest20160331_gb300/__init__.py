@@ -170,6 +170,35 @@ class Builder:
             va = va.clone() if va is not None else None
         return CsrResult(N, int(out.nnz), rp, ci, va, st.as_dict())
 
+    def corr_csr_batch(self, bolds, mode: str = "r_gt", value: float = 0.5,
+                       precision: str = "bf16x3", weighted: bool = True,
+                       delta: Optional[float] = None, stream=None, copy: bool = True):
+        """A batch of subjects (bna_corr_csr_batch): one persistent count pass
+        over all subjects' tiles.  bolds: torch CUDA float32 [T_k][N_k] tensors.
+        -> list of CsrResult."""
+        import torch
+        n = len(bolds)
+        ptrs = (C.c_void_p * n)(*[b.data_ptr() for b in bolds])
+        Ns = (C.c_int32 * n)(*[b.shape[1] for b in bolds])
+        Ts = (C.c_int32 * n)(*[b.shape[0] for b in bolds])
+        o = _opts(mode, value, precision, weighted, delta)
+        outs = (L.Csr * n)()
+        sts = (L.CorrStats * n)()
+        _check(lib().bna_corr_csr_batch(self._h, n, ptrs, Ns, Ts, C.byref(o), outs, sts,
+                                        self._stream(stream)), self._h)
+        res = []
+        for k in range(n):
+            dev = bolds[k].device
+            N = bolds[k].shape[1]
+            rp = _view(outs[k].row_ptr, N + 1, "<i4", torch, dev)
+            ci = _view(outs[k].col_idx, outs[k].nnz, "<i4", torch, dev)
+            va = _view(outs[k].val, outs[k].nnz, "<f4", torch, dev) if outs[k].val else None
+            if copy:
+                rp, ci = rp.clone(), ci.clone()
+                va = va.clone() if va is not None else None
+            res.append(CsrResult(N, int(outs[k].nnz), rp, ci, va, sts[k].as_dict()))
+        return res
+
     def corr_csr_avg(self, bolds, mode: str = "r_gt", value: float = 0.5,
                      precision: str = "bf16x3", fisher: bool = False, weighted: bool = True,
                      delta: Optional[float] = None, stream=None, copy: bool = True) -> CsrResult:
@@ -285,6 +314,16 @@ class Builder:
                                 C.byref(lam), C.byref(it), self._stream(stream)), self._h,
                    ok=(L.BNA_OK, L.BNA_NOT_CONVERGED))
         return ec, lam.value, it.value, s == L.BNA_OK
+
+    def degree(self, csr: CsrResult, stream=None):
+        """Degree of every vertex of a device CSR (bna_degree): float32 [n]."""
+        import torch
+        c = L.Csr(n=csr.n, nnz=csr.nnz, row_ptr=csr.row_ptr.data_ptr(),
+                  col_idx=csr.col_idx.data_ptr() if csr.nnz else None,
+                  val=csr.val.data_ptr() if csr.val is not None and csr.nnz else None)
+        deg = torch.empty(csr.n, dtype=torch.float32, device=csr.row_ptr.device)
+        _check(lib().bna_degree(C.byref(c), C.c_void_p(deg.data_ptr()), self._stream(stream)))
+        return deg
 
     def lead_vector(self, R: np.ndarray, Cc: np.ndarray, V: Optional[np.ndarray] = None):
         """Lead_Vector_GPU(R, C, V, N, ec) with host arrays -> (ec, lambda, iters, converged)."""

@@ -108,6 +108,9 @@ SIGNATURES = {
     "bna_server_device_bytes": (C.c_int64, [C.c_void_p]),
     "bna_server_destroy": (C.c_int32, [C.c_void_p]),
     "bna_density_nnz": (C.c_int64, [C.c_int32, C.c_double]),
+    "bna_corr_csr_batch": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.POINTER(CorrOpts), C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
     "bna_corr_csr_avg": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                      C.c_int32, C.POINTER(CorrOpts), C.POINTER(Csr),
                                      C.POINTER(CorrStats), C.c_void_p]),
@@ -117,6 +120,7 @@ SIGNATURES = {
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_void_p]),
     "bna_nifti_bold": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
                                    C.POINTER(C.c_int32)]),
+    "bna_degree": (C.c_int32, [C.POINTER(Csr), C.c_void_p, C.c_void_p]),
     "bna_csr_rethreshold": (C.c_int32, [C.c_void_p, C.POINTER(Csr), C.c_int32, C.c_double,
                                         C.POINTER(Csr), C.POINTER(C.c_int64), C.c_void_p]),
     "bna_request_bytes": (C.c_int64, [C.c_int32, C.c_int32, C.POINTER(CorrOpts), C.c_int64,

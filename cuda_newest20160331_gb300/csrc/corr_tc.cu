@@ -29,6 +29,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -68,6 +69,16 @@ struct TcSmem {
   volatile uint32_t abort;
   uint32_t colmask[2][128][4];
   unsigned int hist[kHistBins + 1];  // density histogram pass
+  CorrArgs eargs[8];                 // each epilogue warp's current subject's arguments
+};
+
+// One subject of a multi-subject count pass: its operand maps (TMA reads them
+// from global memory), arguments, NaN-block flags and K steps.
+struct TcSubj {  // 64-byte aligned through its CUtensorMap members
+  CUtensorMap hi, lo;
+  CorrArgs a;
+  const uint8_t* blockbad;
+  int nksteps;
 };
 
 constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_RING_BYTES + sizeof(TcSmem);
@@ -81,6 +92,9 @@ struct TcArgs {
   uint32_t* uncertain;
   int fisher;
   float unc_lim;
+  // multi-subject count pass: tiles4 = (I, J-pair, subject), subj the table
+  const int4* tiles4;
+  const TcSubj* subj;
   const int2* tiles;        // (I, Jp): rows of block I x columns of blocks 2Jp, 2Jp+1
   int ntiles;
   int nksteps;              // MMA K steps = ceil(T / elements per step)
@@ -131,7 +145,8 @@ __device__ __forceinline__ bool half_sync(TcSmem& S, int h, uint32_t& phase) {
 // DENS (count pass of the density rule): candidates are listed per 32-column
 // chunk together with their approximate value (a.cand_apx), which the device
 // selection of the k-th largest value needs.
-template <int PASS, bool ABS, int FORM, bool DENS>
+// MULTI: the tiles of several subjects in one persistent launch (count pass).
+template <int PASS, bool ABS, int FORM, bool DENS, bool MULTI = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
                    const __grid_constant__ CUtensorMap tm_lo, const TcArgs p) {
@@ -165,7 +180,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     ptx::tmem_alloc(ptx::smem_u32(&S.tmem_base), TC_TMEM_COLS);
     ptx::tmem_relinquish();
   }
-  if (warp == 0 && lane == 0) {
+  if (!MULTI && warp == 0 && lane == 0) {
     ptx::prefetch_tensormap(&tm_hi);
     if (FORM == FORM_BF16X3) ptx::prefetch_tensormap(&tm_lo);
   }
@@ -182,8 +197,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int last_round[TC_STAGES];
       for (int s = 0; s < TC_STAGES; ++s) last_round[s] = -1;
       for (int t = blockIdx.x; t < p.ntiles && !S.abort; t += gridDim.x) {
-        const int2 tile = p.tiles[t];
-        for (int kb = 0; kb < nkb; ++kb, ++f) {
+        int2 tile;
+        const CUtensorMap* mh = &tm_hi;
+        const CUtensorMap* ml = &tm_lo;
+        int nkb_t = nkb;
+        if (MULTI) {
+          const int4 t4 = p.tiles4[t];
+          tile = make_int2(t4.x, t4.y);
+          mh = &p.subj[t4.z].hi;
+          ml = &p.subj[t4.z].lo;
+          nkb_t = (p.subj[t4.z].nksteps + 3) / 4;
+        } else {
+          tile = p.tiles[t];
+        }
+        for (int kb = 0; kb < nkb_t; ++kb, ++f) {
           const int s = f % TC_STAGES;
           const uint32_t round = f / TC_STAGES;
           const uint32_t empty = ptx::smem_u32(&S.empty[s]);
@@ -198,14 +225,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const int k0 = kb * F::kElemsPerBlock;
           const int ra = tile.x * TC_BM, rb = tile.y * TC_BN;
           // stage layout: A parts, then B parts (B = two 128-row boxes each)
-          ptx::tma_load_2d(base, &tm_hi, full, k0, ra);
-          if (FORM == FORM_BF16X3) ptx::tma_load_2d(base + TC_A_BYTES, &tm_lo, full, k0, ra);
+          ptx::tma_load_2d(base, mh, full, k0, ra);
+          if (FORM == FORM_BF16X3) ptx::tma_load_2d(base + TC_A_BYTES, ml, full, k0, ra);
           const uint32_t bb = base + F::kParts * TC_A_BYTES;
-          ptx::tma_load_2d(bb, &tm_hi, full, k0, rb);
-          ptx::tma_load_2d(bb + TC_B_BYTES / 2, &tm_hi, full, k0, rb + 128);
+          ptx::tma_load_2d(bb, mh, full, k0, rb);
+          ptx::tma_load_2d(bb + TC_B_BYTES / 2, mh, full, k0, rb + 128);
           if (FORM == FORM_BF16X3) {
-            ptx::tma_load_2d(bb + TC_B_BYTES, &tm_lo, full, k0, rb);
-            ptx::tma_load_2d(bb + TC_B_BYTES + TC_B_BYTES / 2, &tm_lo, full, k0, rb + 128);
+            ptx::tma_load_2d(bb + TC_B_BYTES, ml, full, k0, rb);
+            ptx::tma_load_2d(bb + TC_B_BYTES + TC_B_BYTES / 2, ml, full, k0, rb + 128);
           }
           last_round[s] = (int)round;
         }
@@ -233,7 +260,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         ptx::tc_fence_after();
         const uint32_t d = tmem + (uint32_t)(acc * TC_BN);
-        for (int kb = 0; kb < nkb; ++kb, ++f) {
+        const int nkb_t = MULTI ? (p.subj[p.tiles4[t].z].nksteps + 3) / 4 : nkb;
+        const int nks_t = MULTI ? p.subj[p.tiles4[t].z].nksteps : p.nksteps;
+        for (int kb = 0; kb < nkb_t; ++kb, ++f) {
           const int s = f % TC_STAGES;
           const uint32_t round = f / TC_STAGES;
           if (!ptx::mbar_wait(ptx::smem_u32(&S.full[s]), round & 1u, kWaitNs)) {
@@ -242,7 +271,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           ptx::tc_fence_after();
           const uint32_t base = ptx::smem_u32(smem + (size_t)s * TC_STAGE_BYTES);
-          const int steps = min(4, p.nksteps - kb * 4);
+          const int steps = min(4, nks_t - kb * 4);
           if (FORM == FORM_BF16X3) {
             for (int kk = 0; kk < steps; ++kk) {
               const uint64_t ahi = ptx::sw128_desc(base + kk * 32);
@@ -278,53 +307,102 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int q = warp & 3;         // TMEM lane quadrant
     const int h = (warp - 2) >> 2;  // which 128-column half of the tile
     const int il = q * 32 + lane;   // row within the tile
-    const float tau = a.th.tau, delta = a.th.delta, lim = 1.0f - a.th.delta;
-    const float lo_thr = tau - delta;
-    // Near +1 is always covered by x >= tau - delta when tau < 1 - delta; near
-    // -1 can be an edge only through post_block's 0 for tau <= 0 in the signed
-    // rules (|r| rules cover -1 like +1).
-    const bool simple = (tau < lim) && (ABS || lo_thr > 0.0f);
-    // a pair with a NaN voxel has the exact value 0 (post_block)
-    const bool zero_int = (0.0f >= lo_thr) || (0.0f >= lim);
+    // this warp's copy of the current subject's arguments (shared memory)
+    CorrArgs& a = S.eargs[warp - 2];
+    float tau = 0, delta = 0, lim = 0, lo_thr = 0;
+    bool simple = false, zero_int = false;
     uint32_t hphase = 0;
     // this warp's current edge-list chunk [wcur, wend) and candidate chunk
     // [ccur, cend), carried from launch to launch of a pass in a.wstate
     const int wid = (int)blockIdx.x * 8 + (warp - 2);
     long long wcur = 0, wend = 0, ccur = 0, cend = 0;
-    if (PASS == 0 && lane < 4) {
-      const long long x = a.wstate[wid * 4 + lane];
-      wcur = lane == 0 ? x : 0;
-      wend = lane == 1 ? x : 0;
-      ccur = lane == 2 ? x : 0;
-      cend = lane == 3 ? x : 0;
-    }
-    if (PASS == 0) {
-      wcur = __shfl_sync(0xffffffffu, wcur, 0);
-      wend = __shfl_sync(0xffffffffu, wend, 1);
-      ccur = __shfl_sync(0xffffffffu, ccur, 2);
-      cend = __shfl_sync(0xffffffffu, cend, 3);
-    }
-    bool wok = wend <= a.ecap;
+    bool wok = true;
     unsigned long long n_def = 0, n_cand = 0;  // this lane's definite edges and candidates
+    int cur_s = -1;
+    // switch to subject s: arguments, thresholds and chunk state
+    auto enter = [&](int s) {
+      if (lane == 0) a = MULTI ? p.subj[s].a : p.a;
+      __syncwarp();
+      cur_s = s;
+      tau = a.th.tau;
+      delta = a.th.delta;
+      lim = 1.0f - a.th.delta;
+      lo_thr = tau - delta;
+      // Near +1 is always covered by x >= tau - delta when tau < 1 - delta; near
+      // -1 can be an edge only through post_block's 0 for tau <= 0 in the signed
+      // rules (|r| rules cover -1 like +1).
+      simple = (tau < lim) && (ABS || lo_thr > 0.0f);
+      // a pair with a NaN voxel has the exact value 0 (post_block)
+      zero_int = (0.0f >= lo_thr) || (0.0f >= lim);
+      if (PASS == 0) {
+        long long x = 0;
+        if (lane < 4) x = a.wstate[wid * 4 + lane];
+        wcur = __shfl_sync(0xffffffffu, x, 0);
+        wend = __shfl_sync(0xffffffffu, x, 1);
+        ccur = __shfl_sync(0xffffffffu, x, 2);
+        cend = __shfl_sync(0xffffffffu, x, 3);
+      }
+      wok = wend <= a.ecap;
+    };
+    // leave the current subject: its chunks stay open for the next launch or
+    // visit (seal_candidates_kernel closes the candidate chunks after the
+    // pass); the warp's counts go to its statistics
+    auto leave = [&]() {
+      if (PASS == 0 && cur_s >= 0) {
+        if (lane < 4)
+          a.wstate[wid * 4 + lane] = lane == 0 ? wcur : lane == 1 ? wend : lane == 2 ? ccur : cend;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          n_def += __shfl_xor_sync(0xffffffffu, n_def, o);
+          n_cand += __shfl_xor_sync(0xffffffffu, n_cand, o);
+        }
+        if (lane == 0 && n_def) atomicAdd(&a.stats[2], n_def);
+        if (lane == 0 && n_cand) atomicAdd(&a.stats[3], n_cand);
+        n_def = n_cand = 0;
+      }
+      __syncwarp();
+    };
     int m = 0;
     // tile coordinates and NaN-block flags run one tile ahead
+    auto tile_at = [&](int t, int2& tl, int& ts) {
+      if (MULTI) {
+        const int4 t4 = p.tiles4[t];
+        tl = make_int2(t4.x, t4.y);
+        ts = t4.z;
+      } else {
+        tl = p.tiles[t];
+        ts = 0;
+      }
+    };
+    auto flags_of = [&](int2 tl, int ts, uint8_t& fi, uint8_t& fj) {
+      const uint8_t* bbad = MULTI ? p.subj[ts].blockbad : p.blockbad;
+      const int nbs = MULTI ? p.subj[ts].a.nb : p.a.nb;
+      fi = bbad[tl.x];
+      const int jj = 2 * tl.y + h;
+      fj = jj < nbs ? bbad[jj] : 0;
+    };
     int2 nxt = make_int2(0, 0);
+    int nxt_s = 0;
     uint8_t nbi = 0, nbj = 0;
     if ((int)blockIdx.x < p.ntiles) {
-      nxt = p.tiles[blockIdx.x];
-      nbi = p.blockbad[nxt.x];
-      const int jj = 2 * nxt.y + h;
-      nbj = jj < a.nb ? p.blockbad[jj] : 0;
+      tile_at(blockIdx.x, nxt, nxt_s);
+      flags_of(nxt, nxt_s, nbi, nbj);
+      enter(nxt_s);
+    } else {
+      enter(MULTI ? 0 : 0);
     }
     for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++m) {
       if (S.abort) break;
       const int2 tile = nxt;
+      const int tile_s = nxt_s;
       const bool bad_i = nbi != 0, bad_j = nbj != 0;
       if (t + (int)gridDim.x < p.ntiles) {
-        nxt = p.tiles[t + gridDim.x];
-        nbi = p.blockbad[nxt.x];
-        const int jj = 2 * nxt.y + h;
-        nbj = jj < a.nb ? p.blockbad[jj] : 0;
+        tile_at(t + gridDim.x, nxt, nxt_s);
+        flags_of(nxt, nxt_s, nbi, nbj);
+      }
+      if (MULTI && tile_s != cur_s) {
+        leave();
+        enter(tile_s);
       }
       const int I = tile.x, J = 2 * tile.y + h;
       const int acc = m & 1;
@@ -583,18 +661,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
       }
     }
-    if (PASS == 0) {
-      // the chunks stay open for the next launch; seal_candidates_kernel
-      // closes the candidate chunks after the pass
-      if (lane < 4) a.wstate[wid * 4 + lane] = lane == 0 ? wcur : lane == 1 ? wend : lane == 2 ? ccur : cend;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        n_def += __shfl_xor_sync(0xffffffffu, n_def, o);
-        n_cand += __shfl_xor_sync(0xffffffffu, n_cand, o);
-      }
-      if (lane == 0 && n_def) atomicAdd(&a.stats[2], n_def);
-      if (lane == 0 && n_cand) atomicAdd(&a.stats[3], n_cand);
-    }
+    leave();
   }
   ptx::tc_fence_before();
   __syncthreads();
@@ -673,6 +740,63 @@ size_t tc_smem_bytes() { return TC_SMEM_BYTES; }
 
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st) {
   block_bad_kernel<<<nb, 128, 0, st>>>(bad, nb, blockbad);
+  return cudaGetLastError();
+}
+
+size_t tc_subj_bytes() { return sizeof(TcSubj); }
+
+// Table entry s (host memory, tc_subj_bytes() per entry) of a multi-subject
+// count pass: the subject's operand maps, arguments and NaN-block flags.
+bool tc_subj_fill(void* host, int s, const CorrArgs& a, const uint8_t* blockbad, int form) {
+  TcSubj* e = static_cast<TcSubj*>(host) + s;
+  std::memset(e, 0, sizeof *e);
+  if (form == FORM_BF16X3) {
+    if (!a.zhi || !a.zlo || a.ldb % 64 != 0) return false;
+    if (!make_map(&e->hi, a.zhi, a.ldb, a.n_pad, false) ||
+        !make_map(&e->lo, a.zlo, a.ldb, a.n_pad, false))
+      return false;
+    e->nksteps = (a.T + Form<FORM_BF16X3>::kElemsPerStep - 1) / Form<FORM_BF16X3>::kElemsPerStep;
+  } else {
+    if (!a.z || a.ldz % 32 != 0) return false;
+    if (!make_map(&e->hi, a.z, a.ldz, a.n_pad, true)) return false;
+    e->lo = e->hi;
+    e->nksteps = (a.T + Form<FORM_TF32>::kElemsPerStep - 1) / Form<FORM_TF32>::kElemsPerStep;
+  }
+  e->a = a;
+  e->blockbad = blockbad;
+  return true;
+}
+
+// Count pass over the tiles of several subjects in one persistent launch:
+// tiles4 = (I, J-pair, subject); subj_dev = the device copy of the table;
+// batch.err receives timeouts of the producer and MMA warps.
+cudaError_t launch_corr_tc_multi(const CorrArgs& batch, const void* subj_dev, const int4* tiles4,
+                                 int ntiles, int form, bool dens, bool absm, int grid,
+                                 cudaStream_t st) {
+  if (dens && absm) return cudaErrorInvalidValue;
+  TcArgs p{};
+  p.a = batch;
+  p.tiles4 = tiles4;
+  p.subj = static_cast<const TcSubj*>(subj_dev);
+  p.ntiles = ntiles;
+  p.nksteps = 0;
+  const int g = grid < ntiles ? grid : ntiles;
+  if (g <= 0) return cudaSuccess;
+  void (*kern)(CUtensorMap, CUtensorMap, TcArgs);
+  if (form == FORM_BF16X3)
+    kern = dens ? corr_tc_kernel<0, false, FORM_BF16X3, true, true>
+           : absm ? corr_tc_kernel<0, true, FORM_BF16X3, false, true>
+                  : corr_tc_kernel<0, false, FORM_BF16X3, false, true>;
+  else
+    kern = dens ? corr_tc_kernel<0, false, FORM_TF32, true, true>
+           : absm ? corr_tc_kernel<0, true, FORM_TF32, false, true>
+                  : corr_tc_kernel<0, false, FORM_TF32, false, true>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TC_SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  CUtensorMap dummy;
+  std::memset(&dummy, 0, sizeof dummy);
+  kern<<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(dummy, dummy, p);
   return cudaGetLastError();
 }
 

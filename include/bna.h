@@ -168,6 +168,19 @@ int32_t bna_corr_csr_host_into(bna_ctx* ctx, const float* bold_host, int32_t N, 
                                int32_t* col_idx_host, float* val_host, int64_t cap,
                                int64_t* nnz_out, bna_corr_stats* stats);
 
+/* A batch of subjects (voxel counts and series lengths may differ), each
+ * built like bna_corr_csr with the same options; with a tensor-core form the
+ * count passes of all subjects run as one persistent launch over their
+ * concatenated tiles, and the other stages of all subjects are queued with
+ * one host synchronisation per stage.  No reference counterpart (the
+ * reference runs subjects one after another, CorMat.cpp:196-416).
+ * out_dev[k] / stats[k] (stats may be NULL) describe subject k; its CSR
+ * stays valid until the next batch call on this context (a context keeps one
+ * subject context per batch position). */
+int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev,
+                           const int32_t* N, const int32_t* T, const bna_corr_opts* opts,
+                           bna_csr* out_dev, bna_corr_stats* stats, void* stream);
+
 /* Multi-subject average, the reference's to_average modes (y / b with f or n,
  * W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:418-670): every subject's r (post_block:
  * only values in [-1, 1] count; with fisher = 1 its Fisher z, fishertrans
@@ -253,6 +266,13 @@ int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, double eps, dou
  * V may be NULL (binary graph).  ec_host has N doubles. */
 int32_t bna_lead_vector(bna_ctx* ctx, const int32_t* R, const int32_t* C, const double* V,
                         int64_t N, double* ec_host, double* lambda, int32_t* iters);
+
+/* Degree of every vertex of a device CSR (the reference's Degree tool,
+ * W/Degree/Degree/Degree.cpp:80-84): the float sum of each row's values in
+ * column order (bit-identical to the reference's loop); the row length for a
+ * binary CSR (val NULL).  deg_dev: n floats of device memory; asynchronous
+ * on `stream`, on the current device. */
+int32_t bna_degree(const bna_csr* csr_dev, float* deg_dev, void* stream);
 
 /* .csr file (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:353-360 writer,
  * W/CUEC/weighted-net.cu:275-287 reader): int32 Rlength=N+1; int32 R[N+1];

@@ -90,3 +90,27 @@ def test_cormat_density_mode(tmp_path):
     assert re.search(rf"_cor{np.float32(tau):.3f}_weighted", f[0])
     rp, ci, va = bna.csr_read(f[0])
     assert len(ci) == 2 * k
+
+
+def test_degree_tool_and_api(tmp_path, builder):
+    """Degree (W/Degree/Degree/Degree.cpp:80-84): float sum of each row's
+    values in column order, bit-identical; binary graphs: row lengths."""
+    import torch
+    b = bna.synth_bold(2000, 120, 12, 77)
+    res = builder.corr_csr(torch.from_numpy(b).cuda(), mode="r_gt", value=0.3,
+                           precision="bf16x3")
+    g = res.numpy()
+    ref = np.zeros(2000, np.float32)
+    for k in range(2000):  # the reference's sequential float loop
+        for v in g.val[g.row_ptr[k]:g.row_ptr[k + 1]]:
+            ref[k] = np.float32(ref[k] + v)
+    assert np.array_equal(builder.degree(res).cpu().numpy(), ref)
+    bna.csr_write(str(tmp_path / "g.csr"), g.row_ptr, g.col_idx, g.val)
+    _run("bna_degree", tmp_path)
+    d = np.fromfile(tmp_path / "g_deg.nm", np.float32, offset=4)
+    assert np.array_equal(d, ref)
+    binres = builder.corr_csr(torch.from_numpy(b).cuda(), mode="r_gt", value=0.3,
+                              precision="bf16x3", weighted=False)
+    assert np.array_equal(builder.degree(binres).cpu().numpy(),
+                          np.diff(g.row_ptr).astype(np.float32))
+

@@ -409,3 +409,33 @@ def test_average_fisher_matches_oracle(builder):
         v = A[a * (2 * N - a - 1) // 2 + b - a - 1]
         assert abs(v - tau) <= 1e-5, (i, j, v)
     assert len(diff) <= 10
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("mode,value", [("r_ge", 0.35), ("abs_gt", 0.4), ("density", 1.2)])
+def test_batch_equals_single_subject_builds(builder, precision, mode, value):
+    """Subjects of different sizes in one persistent count pass: every CSR
+    equals the one the single-subject path builds (bit-exact, values too)."""
+    import torch
+    shapes = [(1500, 100), (3100, 240), (700, 60), (5000, 180), (2222, 333)]
+    bolds = [dev(bna.synth_bold(N, T, 12, 400 + k)) for k, (N, T) in enumerate(shapes)]
+    bolds[1][:, 9] = 2.0  # a zero-variance voxel
+    batch = builder.corr_csr_batch(bolds, mode=mode, value=value, precision=precision)
+    for k, b in enumerate(bolds):
+        one = builder.corr_csr(b, mode=mode, value=value, precision=precision).numpy()
+        got = batch[k].numpy()
+        assert got.nnz == one.nnz, k
+        assert np.array_equal(got.row_ptr, one.row_ptr) and np.array_equal(got.col_idx, one.col_idx)
+        assert np.array_equal(got.val, one.val), k
+
+
+def test_batch_density_with_sampled_window(builder):
+    import torch
+    shapes = [(24000, 60), (2000, 120)]
+    bolds = [dev(bna.synth_bold(N, T, 12, 500 + k)) for k, (N, T) in enumerate(shapes)]
+    batch = builder.corr_csr_batch(bolds, mode="density", value=0.9, precision="bf16x3")
+    for k, b in enumerate(bolds):
+        one = builder.corr_csr(b, mode="density", value=0.9, precision="bf16x3").numpy()
+        got = batch[k].numpy()
+        assert got.nnz == one.nnz == bna.density_nnz(shapes[k][0], 0.9)
+        assert np.array_equal(got.row_ptr, one.row_ptr) and np.array_equal(got.col_idx, one.col_idx)
