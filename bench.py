@@ -6,7 +6,8 @@ Default workload: N=45,000 voxels x T=240 (float32, seeded factor model,
 K=40), weighted CSR at 1 % density (tau = the FP64 quantile).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P]
-                  [--workload n45k|small|n180k|serving] [--impl reference]
+                  [--workload n45k|small|n180k|n45k_density|batch64|serving]
+                  [--impl reference]
                   [--serve-requests R]
 
 The line's "serve" object is a serving sample: R requests (default 120) with
@@ -261,6 +262,56 @@ def serve_run(n_requests: int, slots: int = 4, rate: float = 4.0, seed: int = 50
     }
 
 
+def batch_run(n_subjects: int, precision: str = "auto", plain: bool = True) -> dict:
+    """The batch workload: all subjects through bna_corr_csr_batch (one
+    persistent count pass over every subject's tiles), against each subject
+    built alone with the plain FP32 form."""
+    import numpy as np
+    import torch
+    import cuda_newest20160331_gb300 as bna
+    from cuda_newest20160331_gb300 import workloads
+    subs = workloads.batch_subjects(n_subjects)
+    bolds = [torch.from_numpy(bna.synth_bold(N, T, K, sd)).cuda() for (N, T, K, sd) in subs]
+    b = bna.Builder(0)
+    stream = torch.cuda.current_stream()
+    # warm-up: the autotuner's choice, arenas grown
+    res = b.corr_csr_batch(bolds, mode="density", value=1.0, precision=precision, copy=False)
+    chosen = res[0].stats
+    times = []
+    for _ in range(2):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        res = b.corr_csr_batch(bolds, mode="density", value=1.0, precision=precision, copy=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t0) * 1000.0)
+    batch_ms = min(times)
+    nnz = sum(r.nnz for r in res)
+    exact = all(r.nnz == bna.density_nnz(N, 1.0) for r, (N, _, _, _) in zip(res, subs))
+    out = {"subjects": n_subjects, "batch_ms": batch_ms,
+           "subjects_per_s": n_subjects / (batch_ms / 1000.0), "edges_per_s": nnz / (batch_ms / 1000.0),
+           "exact_edge_counts": exact, "precision": precision,
+           "flop_algorithmic": float(sum(N * (N - 1) / 2 * 2 * T for (N, T, _, _) in subs)),
+           "sample": f"{n_subjects} subjects, N {min(s[0] for s in subs)}..{max(s[0] for s in subs)}, "
+                     f"T {min(s[1] for s in subs)}..{max(s[1] for s in subs)}, density 1 %, weighted"}
+    out["tflops_algorithmic"] = out["flop_algorithmic"] / (batch_ms / 1000.0) / 1e12
+    if plain:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for bold in bolds:
+            b.corr_csr(bold, mode="density", value=1.0, precision="fp32", copy=False)
+        torch.cuda.synchronize()
+        pms = (time.perf_counter() - t0) * 1000.0
+        out["plain_fp32_each_alone_ms"] = pms
+        out["plain_fp32_subjects_per_s"] = n_subjects / (pms / 1000.0)
+        out["speedup_vs_plain_fp32"] = pms / batch_ms
+    b.close()
+    return out
+
+
 def load_traffic(kernel: str, workload: str):
     """DRAM bytes per launch of `kernel` on `workload` from one ncu capture
     (profiles/traffic.txt: `kernel:workload bytes` lines), or None."""
@@ -323,6 +374,14 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    if args.workload == "batch64":
+        bt = batch_run(64, precision=args.precision if args.precision != "bf16x3" else "auto",
+                       plain=not args.no_plain)
+        if rank == 0:
+            print(json.dumps({"metric": "subjects/s, 64-subject batch at 1 % density",
+                              "value": bt["subjects_per_s"], "unit": "subjects/s",
+                              "higher_is_better": True, "n_gpus": 1, "batch": bt}), flush=True)
+        return
     if args.workload == "serving":
         sv = serve_run(1000 if args.serve_requests == 120 else args.serve_requests,
                        slots=args.serve_slots, dump=args.serve_dump)

@@ -125,6 +125,16 @@ class Builder:
     def trim(self):
         _check(lib().bna_ctx_trim(self._h), self._h)
 
+    def autotune(self, N: int, T: int, mode: str = "r_gt", value: float = 0.5,
+                 weighted: bool = True):
+        """bna_autotune: -> (chosen precision name, {form: ms})."""
+        o = _opts(mode, value, "auto", weighted, None)
+        best = C.c_int32()
+        ms = (C.c_float * 2)()
+        _check(lib().bna_autotune(self._h, N, T, C.byref(o), C.byref(best), ms), self._h)
+        names = {v: k for k, v in L.PRECISIONS.items()}
+        return names[best.value], {"bf16x3": ms[0], "tf32": ms[1]}
+
     def set_option(self, name: str, value: int):
         """bna_ctx_set_option: "tiles_per_launch" or "max_nnz" (0 = default)."""
         _check(lib().bna_ctx_set_option(self._h, L.OPTIONS[name], int(value)), self._h)

@@ -18,7 +18,7 @@ BNA_CAPACITY = 13
 BNA_OVER_BUDGET = 14
 OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1}
 THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4}
-PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2}
+PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2, "auto": 3}
 SYNTH_KINDS = {"iid": 0, "blocknet": 1}
 
 
@@ -108,6 +108,8 @@ SIGNATURES = {
     "bna_server_device_bytes": (C.c_int64, [C.c_void_p]),
     "bna_server_destroy": (C.c_int32, [C.c_void_p]),
     "bna_density_nnz": (C.c_int64, [C.c_int32, C.c_double]),
+    "bna_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CorrOpts),
+                                 C.POINTER(C.c_int32), C.c_void_p]),
     "bna_corr_csr_batch": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.POINTER(CorrOpts), C.c_void_p, C.c_void_p,
                                        C.c_void_p]),

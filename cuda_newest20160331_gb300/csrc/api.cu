@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "common.cuh"
@@ -162,6 +163,9 @@ struct bna_ctx {
   size_t hist_host_cap = 0;
   std::vector<int> batch_nb;
   int batch_ntiles = 0;
+  // autotuner choices: bucket key -> precision
+  std::map<long long, int> tune;
+  bool tune_loaded = false;
   cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
   long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
 };
@@ -465,7 +469,8 @@ int64_t bna_request_bytes(int32_t N, int32_t T, const bna_corr_opts* opts, int64
   long long b = 0;
   b += (long long)N * T * 4;                                   // BOLD
   b += n_pad * ldz * 4 + n_pad;                                // z, bad
-  if (opts->precision == BNA_PREC_BF16X3) b += n_pad * ldb * 4;  // z hi / lo
+  if (opts->precision == BNA_PREC_BF16X3 || opts->precision == BNA_PREC_AUTO)
+    b += n_pad * ldb * 4;  // z hi / lo
   b += nb * n_pad * 4 + 2 * n_pad * 8 + 4096 * 8;              // seg, row lengths, block sums
   b += nst * 64 + nst * 4 + ntiles * 8 + nb;                   // etab, dense list, tiles, flags
   b += elist * 8;                                              // edge lists
@@ -563,6 +568,101 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
                              const bna_corr_opts* opts, int prec, double delta, bna_csr* out_dev,
                              bna_corr_stats* stats, cudaStream_t st);
 
+// Autotuner bucket: half-octaves of N and T, and the rule kind.
+static long long tune_key(int N, int T, int mode) {
+  const int nb = (int)std::floor(2.0 * std::log2((double)std::max(N, 2)));
+  const int tb = (int)std::floor(2.0 * std::log2((double)std::max(T, 2)));
+  return ((long long)nb << 24) | ((long long)tb << 8) | (mode == BNA_THR_DENSITY ? 1 : 0);
+}
+
+static void tune_load(bna_ctx* ctx) {
+  if (ctx->tune_loaded) return;
+  ctx->tune_loaded = true;
+  const char* path = std::getenv("BNA_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  long long key;
+  int prec;
+  while (std::fscanf(f, "%lld %d%*[^\n]", &key, &prec) == 2)
+    if (prec == BNA_PREC_BF16X3 || prec == BNA_PREC_TF32) ctx->tune[key] = prec;
+  std::fclose(f);
+}
+
+static int32_t resolve_precision(bna_ctx* ctx, int N, int T, const bna_corr_opts* opts,
+                                 int* prec) {
+  *prec = opts->precision;
+  if (opts->precision != BNA_PREC_AUTO) return BNA_OK;
+  tune_load(ctx);
+  auto it = ctx->tune.find(tune_key(N, T, opts->mode));
+  if (it != ctx->tune.end()) {
+    *prec = it->second;
+    return BNA_OK;
+  }
+  int32_t best = BNA_PREC_BF16X3;
+  const int32_t s = bna_autotune(ctx, N, T, opts, &best, nullptr);
+  if (s) return s;
+  *prec = best;
+  return BNA_OK;
+}
+
+int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
+                     int32_t* precision_out, float* ms_out) {
+  if (!ctx || N < 2 || T < 2 || !opts || !precision_out)
+    return fail(ctx, BNA_BAD_ARG, "bna_autotune: bad arguments");
+  tune_load(ctx);
+  int32_t s = set_device(ctx);
+  if (s) return s;
+  // a seeded synthetic subject of this size (the factor model of the workloads)
+  std::vector<float> h((size_t)N * T);
+  bna_synth_params sp{};
+  sp.N = N;
+  sp.T = T;
+  sp.K = 40;
+  sp.kind = BNA_SYNTH_IID;
+  sp.seed = 0x5eedULL;
+  sp.phi = 0.7;
+  sp.load_sd = 0.3;
+  if (bna_synth_bold(&sp, h.data(), 0) != 0) return fail(ctx, BNA_INTERNAL, "synthetic subject");
+  float* bold = nullptr;
+  CK(cudaMalloc(&bold, h.size() * sizeof(float)));
+  cudaError_t ce = cudaMemcpy(bold, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) {
+    cudaFree(bold);
+    return fail(ctx, BNA_CUDA_ERROR, "bna_autotune: %s", cudaGetErrorString(ce));
+  }
+  const int forms[2] = {BNA_PREC_BF16X3, BNA_PREC_TF32};
+  float best_ms[2] = {INFINITY, INFINITY};
+  for (int f = 0; f < 2 && s == BNA_OK; ++f) {
+    bna_corr_opts o = *opts;
+    o.precision = forms[f];
+    for (int rep = 0; rep < 3 && s == BNA_OK; ++rep) {  // first run warms up
+      bna_csr c{};
+      bna_corr_stats st{};
+      s = bna_corr_csr(ctx, bold, N, T, &o, &c, &st, nullptr);
+      if (s == BNA_OK && rep > 0) best_ms[f] = std::min(best_ms[f], st.ms_total);
+    }
+  }
+  cudaFree(bold);
+  if (s) return s;
+  const int32_t best = best_ms[1] < best_ms[0] ? BNA_PREC_TF32 : BNA_PREC_BF16X3;
+  const long long key = tune_key(N, T, opts->mode);
+  ctx->tune[key] = best;
+  const char* path = std::getenv("BNA_TUNE_CACHE");
+  if (path && *path) {
+    if (FILE* f = std::fopen(path, "a")) {
+      std::fprintf(f, "%lld %d %d %d %.4f %.4f\n", key, best, N, T, best_ms[0], best_ms[1]);
+      std::fclose(f);
+    }
+  }
+  *precision_out = best;
+  if (ms_out) {
+    ms_out[0] = best_ms[0];
+    ms_out[1] = best_ms[1];
+  }
+  return BNA_OK;
+}
+
 int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
                      const bna_corr_opts* opts, bna_csr* out_dev, bna_corr_stats* stats,
                      void* stream) {
@@ -570,15 +670,17 @@ int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: bad arguments");
   if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown threshold mode %d", opts->mode);
-  if (opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_TF32)
+  if (opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_AUTO)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown precision %d", opts->precision);
   const bool density = opts->mode == BNA_THR_DENSITY;
   if (density && !(opts->value >= 0.0 && opts->value <= 100.0))
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: density %g%% outside [0, 100]", opts->value);
-  int32_t s = set_device(ctx, as_stream(stream));
+  int prec = opts->precision;
+  int32_t s = resolve_precision(ctx, N, T, opts, &prec);
+  if (s) return s;
+  s = set_device(ctx, as_stream(stream));
   if (s) return s;
   cudaStream_t st = as_stream(stream);
-  const int prec = opts->precision;
   ctx->klaunch = 0;
   ctx->last_ok = false;  // the arena is about to be rewritten
   CorrArgs a{};
@@ -1118,8 +1220,15 @@ static int32_t avg_check(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
 int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_dev, int32_t N,
                          const int32_t* T, int32_t fisher, const bna_corr_opts* opts,
                          bna_csr* out_dev, bna_corr_stats* stats, void* stream) {
-  if (!opts || !out_dev) return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad arguments");
-  int32_t s = avg_check(ctx, nsub, bold_dev, N, T, opts->precision);
+  if (!opts || !out_dev || !T || nsub < 1)
+    return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad arguments");
+  int prec_r = opts->precision;
+  int32_t s = resolve_precision(ctx, N, T[0], opts, &prec_r);
+  if (s) return s;
+  bna_corr_opts opts_r = *opts;
+  opts_r.precision = prec_r;
+  opts = &opts_r;
+  s = avg_check(ctx, nsub, bold_dev, N, T, opts->precision);
   if (s) return s;
   if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
       (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
@@ -1352,10 +1461,20 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
     if (!bold_dev[k] || N[k] < 1 || T[k] < 1)
       return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_batch: subject %d: bad arguments", k);
   if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
-      opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_TF32 ||
+      opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_AUTO ||
       (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_batch: bad options");
-  int32_t s = set_device(ctx, as_stream(stream));
+  // one form for the batch: the autotuner's choice for its largest subject
+  int kmax = 0;
+  for (int k = 1; k < nsub; ++k)
+    if ((double)N[k] * N[k] * T[k] > (double)N[kmax] * N[kmax] * T[kmax]) kmax = k;
+  int prec_r = opts->precision;
+  int32_t s = resolve_precision(ctx, N[kmax], T[kmax], opts, &prec_r);
+  if (s) return s;
+  bna_corr_opts opts_r = *opts;
+  opts_r.precision = prec_r;
+  opts = &opts_r;
+  s = set_device(ctx, as_stream(stream));
   if (s) return s;
   cudaStream_t st = as_stream(stream);
   while ((int)ctx->kids.size() < nsub) {

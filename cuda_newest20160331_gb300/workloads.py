@@ -9,6 +9,8 @@ not distributed).  Sizes follow the reference's typical runs (N up to
   n45k_density  the same subject through the exact density rule (1 %)
   n180k      N=180,000 T=1200 K=60  block-network loadings (500-voxel blocks),
              tau = 0.4, weighted CSR, then centrality
+  batch64    64 subjects, N uniform in [20,000, 70,000], T uniform in [150, 1200],
+             seeds 1000 + s, 1 % density each, weighted CSRs, in one batch
   serving    Poisson arrivals at 4 requests/s; each request a subject with N
              log-uniform in [4,096, 180,000], T in {240, 600, 1200}, threshold
              r >= tau (tau uniform in [0.3, 0.6]) or a density uniform in
@@ -92,3 +94,12 @@ def serving(n_requests: int, rate: float = 4.0, seed: int = 5000, pool: int = 24
         else:
             reqs.append(ServeRequest(t, subj, "density", float(rng.uniform(0.1, 2.0))))
     return subjects, reqs
+
+
+def batch_subjects(n: int = 64, seed: int = 1000, n_lo: int = 20000, n_hi: int = 70000,
+                   t_lo: int = 150, t_hi: int = 1200):
+    """-> [(N, T, K, seed)] of the batch workload (subject s uses seed + s)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(n_lo, n_hi + 1)), int(rng.integers(t_lo, t_hi + 1)), 40, seed + s)
+            for s in range(n)]

@@ -70,7 +70,9 @@ typedef enum bna_thr_mode {
 typedef enum bna_precision {
   BNA_PREC_FP32 = 0,   /* plain FP32 CUDA-core GEMM */
   BNA_PREC_BF16X3 = 1, /* split BF16 (hi*hi + hi*lo + lo*hi) on tcgen05 tensor cores, FP32 accumulate */
-  BNA_PREC_TF32 = 2    /* TF32 on tcgen05 tensor cores, FP32 accumulate */
+  BNA_PREC_TF32 = 2,   /* TF32 on tcgen05 tensor cores, FP32 accumulate */
+  BNA_PREC_AUTO = 3    /* the tensor-core form bna_autotune picked for the size (tuned on
+                          first use of a size bucket) */
 } bna_precision;
 
 typedef struct bna_csr {
@@ -130,6 +132,19 @@ int64_t bna_ctx_arena_bytes(const bna_ctx* ctx);
  *     limit). */
 typedef enum bna_option { BNA_OPT_TILES_PER_LAUNCH = 0, BNA_OPT_MAX_NNZ = 1 } bna_option;
 int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value);
+
+/* Autotuner (no reference counterpart).  The two tensor-core forms differ in
+ * their tile shape along K (64 BF16 values x 3 products vs 32 TF32 values x 1
+ * per 128-byte stage row, 2 vs 4 pipeline stages) and in the width of the
+ * exact-recompute band; which one builds a CSR faster depends on N, T and the
+ * rule.  bna_autotune times both on a seeded synthetic subject of size N x T
+ * under `opts` (rule and value), remembers the faster one for the size bucket
+ * (half-octaves of N and T) and rule kind, and returns it; BNA_PREC_AUTO
+ * calls resolve through these choices.  With the environment variable
+ * BNA_TUNE_CACHE set, choices are read from and appended to that file.
+ * ms_out (optional, 2 floats): the times of split-BF16 and TF32. */
+int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
+                     int32_t* precision_out, float* ms_out);
 
 /* Z-score, the prologue of CorMat_gpu / CorMat_cpu (W/CorMat/CUCorMat/CUCorMat/CorMat.cu:24-52,
  * CorMat.cpp:923-951): per voxel mean and centred L2 norm in double, summed in time

@@ -439,3 +439,30 @@ def test_batch_density_with_sampled_window(builder):
         got = batch[k].numpy()
         assert got.nnz == one.nnz == bna.density_nnz(shapes[k][0], 0.9)
         assert np.array_equal(got.row_ptr, one.row_ptr) and np.array_equal(got.col_idx, one.col_idx)
+
+
+def test_autotune_picks_a_form_and_auto_resolves(builder, tmp_path, monkeypatch):
+    """The autotuner times both tensor-core forms and remembers the faster one;
+    precision "auto" then builds with it (the same CSR as any form)."""
+    monkeypatch.setenv("BNA_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    t = bna.Builder(0)
+    try:
+        best, ms = t.autotune(3000, 200, mode="r_gt", value=0.4)
+        assert best in ("bf16x3", "tf32") and ms["bf16x3"] > 0 and ms["tf32"] > 0
+        assert (ms[best] <= min(ms.values()))
+        lines = (tmp_path / "tune.txt").read_text().split("\n")
+        assert len([x for x in lines if x.strip()]) == 1
+        b = dev(bna.synth_bold(3000, 200, 12, 77))
+        auto = t.corr_csr(b, mode="r_gt", value=0.4, precision="auto").numpy()
+        ref = t.corr_csr(b, mode="r_gt", value=0.4, precision="fp32").numpy()
+        assert np.array_equal(auto.row_ptr, ref.row_ptr) and np.array_equal(auto.col_idx, ref.col_idx)
+    finally:
+        t.close()
+    # a fresh context reads the choice from the cache file instead of tuning
+    t2 = bna.Builder(0)
+    try:
+        t2.corr_csr(b, mode="r_gt", value=0.4, precision="auto")
+        lines = (tmp_path / "tune.txt").read_text().split("\n")
+        assert len([x for x in lines if x.strip()]) == 1
+    finally:
+        t2.close()
