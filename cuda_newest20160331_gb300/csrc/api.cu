@@ -83,6 +83,9 @@ cudaError_t launch_density_select(const CorrArgs& a, void* state, unsigned int* 
                                   cudaStream_t st);
 cudaError_t launch_csr_fill(const CorrArgs& a, int sms, int* dense_list, unsigned int* dense_count,
                             cudaStream_t stream);
+cudaError_t launch_csr_fill_dense(const CorrArgs& a, int sms, int* dense_list,
+                                  unsigned int* dense_count, cudaStream_t stream);
+cudaError_t launch_csr_fill_rows(const CorrArgs& a, int sms, int I0, int I1, cudaStream_t stream);
 cudaError_t launch_collect_candidates(const CorrArgs& a, int sms, cudaStream_t stream);
 cudaError_t launch_cand_values(const CorrArgs& a, float* vals, int grid, cudaStream_t stream);
 }  // namespace bna
@@ -124,6 +127,9 @@ constexpr int kGraphIters = 32;
 // Density rule: the histogram that locates the k-th value runs on about this
 // many tiles (every s-th tile) when the problem has at least 4x as many.
 constexpr int kSampleTiles = 2048;
+// Row-block chunks of the fill pass when the CSR goes to host buffers: chunk
+// c's rows are copied out while chunk c + 1 is filled.
+constexpr int kFillChunks = 8;
 
 }  // namespace
 
@@ -168,6 +174,19 @@ struct bna_ctx {
   bool tune_loaded = false;
   cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
   long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
+  // host destination of the CSR (bna_corr_csr_host_into): row_ptr is copied
+  // with the scan's status, and the fill pass runs in row-block chunks whose
+  // entries are copied out on copy_stream while the next chunk fills
+  struct Sink {
+    int32_t* row_ptr;
+    int32_t* col;
+    float* val;
+    long long cap;
+    bool done;  // the CSR has been copied (row_ptr, col, val)
+  };
+  Sink* sink = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_ev[kFillChunks + 1] = {};
 };
 
 namespace {
@@ -525,6 +544,9 @@ int32_t bna_ctx_destroy(bna_ctx* ctx) {
   bna_ctx_trim(ctx);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->chunk_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   delete ctx;
   return BNA_OK;
@@ -846,6 +868,9 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
                            a.err, st));
       }
       CK(cudaEventRecord(ctx->ev[4], st));
+      if (ctx->sink)
+        CK(cudaMemcpyAsync(ctx->sink->row_ptr, row_ptr, (size_t)(N + 1) * 4,
+                           cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       bool again = false;
@@ -950,6 +975,9 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
     CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
                        st));
     CK(cudaEventRecord(ctx->ev[4], st));
+    if (ctx->sink)
+      CK(cudaMemcpyAsync(ctx->sink->row_ptr, row_ptr, (size_t)(N + 1) * 4,
+                         cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (hs->err & ERR_HASH_FULL) return fail(ctx, BNA_INTERNAL, "candidate hash full");
@@ -981,7 +1009,38 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
   a.nnz = nnz;
   int* dense_list;
   ENSURE(S_DENSE, (size_t)nst * sizeof(int), dense_list);
-  CK(launch_csr_fill(a, ctx->sms, dense_list, &ds->dense, st));
+  int fill_launches = 3;
+  bna_ctx::Sink* sink = ctx->sink;
+  if (sink && nnz <= sink->cap && (nnz == 0 || sink->col) && sink->row_ptr[N] == nnz) {
+    // chunked fill, each chunk's entries copied out while the next fills
+    if (!ctx->copy_stream) {
+      CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+      for (auto& e : ctx->chunk_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    CK(launch_csr_fill_dense(a, ctx->sms, dense_list, &ds->dense, st));
+    const int nch = std::min(kFillChunks, a.nb);
+    for (int c = 0; c < nch; ++c) {
+      const int I0 = (int)((long long)c * a.nb / nch), I1 = (int)((long long)(c + 1) * a.nb / nch);
+      CK(launch_csr_fill_rows(a, ctx->sms, I0, I1, st));
+      CK(cudaEventRecord(ctx->chunk_ev[c], st));
+      CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_ev[c], 0));
+      const long long e0 = sink->row_ptr[std::min(I0 * kBlk, N)];
+      const long long e1 = sink->row_ptr[std::min(I1 * kBlk, N)];
+      if (e1 > e0) {
+        CK(cudaMemcpyAsync(sink->col + e0, col + e0, (size_t)(e1 - e0) * 4,
+                           cudaMemcpyDeviceToHost, ctx->copy_stream));
+        if (val && sink->val)
+          CK(cudaMemcpyAsync(sink->val + e0, val + e0, (size_t)(e1 - e0) * 4,
+                             cudaMemcpyDeviceToHost, ctx->copy_stream));
+      }
+    }
+    CK(cudaEventRecord(ctx->chunk_ev[nch], ctx->copy_stream));
+    CK(cudaStreamWaitEvent(st, ctx->chunk_ev[nch], 0));
+    sink->done = true;
+    fill_launches = 2 + nch;
+  } else {
+    CK(launch_csr_fill(a, ctx->sms, dense_list, &ds->dense, st));
+  }
   CK(cudaEventRecord(ctx->ev[5], st));
   CK(cudaMemcpyAsync(hs, ds, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -1005,7 +1064,7 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
     stats->band_1e6 = (int64_t)band_1e6;
     stats->ties_dropped = ties_dropped;
     stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
-    stats->kernel_launches = ctx->klaunch + 2;  // + the fill pass (2 kernels)
+    stats->kernel_launches = ctx->klaunch + fill_launches;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);
@@ -1064,9 +1123,13 @@ int32_t bna_corr_csr_host_into(bna_ctx* ctx, const float* bold_host, int32_t N, 
   CK(cudaMemcpyAsync(bold, bold_host, (size_t)N * T * sizeof(float), cudaMemcpyHostToDevice,
                      nullptr));
   bna_csr d{};
+  bna_ctx::Sink sink{row_ptr_host, col_idx_host, val_host, cap, false};
+  ctx->sink = &sink;
   s = bna_corr_csr(ctx, bold, N, T, opts, &d, stats, nullptr);
+  ctx->sink = nullptr;
   if (s) return s;
   if (nnz_out) *nnz_out = d.nnz;
+  if (sink.done) return BNA_OK;  // copied chunk by chunk behind the fill pass
   CK(cudaMemcpyAsync(row_ptr_host, d.row_ptr, (size_t)(N + 1) * 4, cudaMemcpyDeviceToHost,
                      nullptr));
   if (d.nnz > cap) {

@@ -66,7 +66,9 @@ cudaError_t launch_avg_finalize(float* packed, long long m, int S, int fisher, i
 
 cudaError_t launch_avg_exact(const CorrArgs& a, const void* subj, int S, int fisher, float* out,
                              int sms, cudaStream_t st) {
-  avg_exact_kernel<<<sms * 8, 256, 0, st>>>(a, static_cast<const SubjZ*>(subj), S, fisher, out);
+  // an odd grid: candidate slots come in 256-slot chunks filled from the front
+  avg_exact_kernel<<<sms * 8 - 1, 256, 0, st>>>(a, static_cast<const SubjZ*>(subj), S, fisher,
+                                                 out);
   return cudaGetLastError();
 }
 

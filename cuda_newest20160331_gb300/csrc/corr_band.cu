@@ -277,13 +277,18 @@ __global__ void scan_finish_kernel(const long long* pre, const long long* bsum, 
   }
 }
 
+// Candidate slots come in 256-slot chunks filled from the front; a warp count
+// that is a multiple of 256 would give every warp the same offset in each
+// chunk (and the filled offsets to a few warps): the grid is made odd.
+static int odd_grid(int grid) { return grid > 1 ? (grid | 1) - 2 * ((grid & 1) == 0) : 1; }
+
 cudaError_t launch_recompute(const CorrArgs& a, int grid, cudaStream_t stream) {
-  recompute_kernel<<<grid, 256, 0, stream>>>(a);
+  recompute_kernel<<<odd_grid(grid), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_cand_values(const CorrArgs& a, float* vals, int grid, cudaStream_t stream) {
-  cand_values_kernel<<<grid, 256, 0, stream>>>(a, vals);
+  cand_values_kernel<<<odd_grid(grid), 256, 0, stream>>>(a, vals);
   return cudaGetLastError();
 }
 

@@ -319,11 +319,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     bool wok = true;
     unsigned long long n_def = 0, n_cand = 0;  // this lane's definite edges and candidates
     int cur_s = -1;
+    // the fields the per-value path reads, kept in registers
+    int s_n = 0, s_npad = 0, s_nb = 0;
+    const uint8_t* s_bad = nullptr;
+    uint2* s_elist = nullptr;
+    int32_t* s_seg = nullptr;
+    longlong2* s_etab = nullptr;
     // switch to subject s: arguments, thresholds and chunk state
     auto enter = [&](int s) {
       if (lane == 0) a = MULTI ? p.subj[s].a : p.a;
       __syncwarp();
       cur_s = s;
+      s_n = a.n;
+      s_npad = a.n_pad;
+      s_nb = a.nb;
+      s_bad = a.bad;
+      s_elist = a.elist;
+      s_seg = a.seg;
+      s_etab = a.etab;
       tau = a.th.tau;
       delta = a.th.delta;
       lim = 1.0f - a.th.delta;
@@ -407,7 +420,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int I = tile.x, J = 2 * tile.y + h;
       const int acc = m & 1;
       const uint32_t ar = (uint32_t)(m >> 1);
-      const bool active = (PASS == 2) ? (J < a.nb) : ((J >= I) && (J < a.nb));
+      const bool active = (PASS == 2) ? (J < s_nb) : ((J >= I) && (J < s_nb));
       const bool listing = (PASS == 0);
       const int gi = I * 128 + il;
       long long start = 0;
@@ -439,7 +452,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TC_BN + h * 128);
       const bool diag = (I == J);
       const bool slow = active && (bad_i || bad_j);
-      const bool rowbad = slow && a.bad[gi];
+      const bool rowbad = slow && s_bad[gi];
       int rowcount = 0;
       uint32_t cmk4[4] = {0u, 0u, 0u, 0u};
       if (active) {
@@ -456,8 +469,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             continue;
           }
           const int jb = J * 128 + c * 32;
-          uint32_t valid = (jb + 32 <= a.n) ? 0xffffffffu
-                                            : (jb >= a.n ? 0u : ((1u << (a.n - jb)) - 1u));
+          uint32_t valid = (jb + 32 <= s_n) ? 0xffffffffu
+                                            : (jb >= s_n ? 0u : ((1u << (s_n - jb)) - 1u));
           if (diag) {
             const int lo = il - c * 32 + 1;  // first column index k with jl > il
             valid &= (lo <= 0) ? 0xffffffffu : (lo >= 32 ? 0u : (0xffffffffu << lo));
@@ -466,10 +479,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             uint32_t badm4 = 0;
             if (slow)
               for (int k = 0; k < 32; ++k)
-                if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm4 |= 1u << k;
-            if (gi < a.n) {
+                if (rowbad || (jb + k < s_npad && s_bad[jb + k])) badm4 |= 1u << k;
+            if (gi < s_n) {
               // packed upper-triangle index of (gi, j): gi (2n - gi - 1) / 2 + j - gi - 1
-              const long long rowbase = (long long)gi * (2LL * a.n - gi - 1) / 2 - gi - 1;
+              const long long rowbase = (long long)gi * (2LL * s_n - gi - 1) / 2 - gi - 1;
 #pragma unroll
               for (int k = 0; k < 32; ++k) {
                 if (!((valid >> k) & 1u)) continue;
@@ -490,7 +503,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             uint32_t badm3 = 0;
             if (slow)
               for (int k = 0; k < 32; ++k)
-                if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm3 |= 1u << k;
+                if (rowbad || (jb + k < s_npad && s_bad[jb + k])) badm3 |= 1u << k;
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
               if ((valid >> k) & 1u) {
@@ -521,7 +534,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           uint32_t badm = 0;
           if (slow) {
             for (int k = 0; k < 32; ++k)
-              if (rowbad || (jb + k < a.n_pad && a.bad[jb + k])) badm |= 1u << k;
+              if (rowbad || (jb + k < s_npad && s_bad[jb + k])) badm |= 1u << k;
             it = (it & ~badm) | (zero_int ? badm : 0u);
           }
           it &= valid;
@@ -534,7 +547,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (lane >= o) incl += y;
           }
           const int total = __shfl_sync(0xffffffffu, incl, 31);
-          uint2* dst = a.elist + wcur + (incl - ne);
+          uint2* dst = s_elist + wcur + (incl - ne);
           // classify this lane's few interesting entries; candidates are only
           // flagged here (collected for the exact recompute after the pass)
           uint32_t eb = 0;
@@ -643,7 +656,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         n_cand += nc;
       }
       if (active && lane == 0)
-        a.etab[subtile_index(I, J, a.nb) * 4 + q] =
+        s_etab[subtile_index(I, J, s_nb) * 4 + q] =
             wok ? make_longlong2(start, wcur - start) : make_longlong2(0, 0);
       if (!half_sync(S, h, hphase)) {
         atomicOr(a.err, ERR_TIMEOUT);
@@ -654,10 +667,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t* cm = S.colmask[h][il];
         const int cc = __popc(cm[0]) + __popc(cm[1]) + __popc(cm[2]) + __popc(cm[3]);
         if (diag) {
-          a.seg[(size_t)I * a.n_pad + gi] = rowcount + cc;
+          s_seg[(size_t)I * s_npad + gi] = rowcount + cc;
         } else {
-          a.seg[(size_t)J * a.n_pad + gi] = rowcount;
-          a.seg[(size_t)I * a.n_pad + J * 128 + il] = cc;
+          s_seg[(size_t)J * s_npad + gi] = rowcount;
+          s_seg[(size_t)I * s_npad + J * 128 + il] = cc;
         }
       }
     }

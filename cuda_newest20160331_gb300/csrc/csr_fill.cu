@@ -5,17 +5,20 @@
 // V[e] = r of the pair.  Here the count pass has left, per 128 x 128
 // sub-tile (I, J), I <= J, a compact list of its edges (value) and of its
 // near-threshold candidates (resolved by the recompute pass into a hash).
-// One warp handles one sub-tile:
-//   1. mark every edge in the sub-tile's row and column bitmasks (smem);
+// One warp handles one sub-tile for the 128 rows of one row block: the
+// direct entries of sub-tile (I, J), J >= I, or the transposed entries of
+// sub-tile (J, I), J <= I, for the rows of block I:
+//   1. mark the entries in per-row bitmasks (smem);
 //   2. bases: row i of block I starts its block-J segment at
-//      row_ptr[i] + seg[J][i] (+ the count of its column-direction entries
-//      on a diagonal sub-tile); column j of block J starts at
-//      row_ptr[j] + seg[I][j];
-//   3. each edge goes to base + (number of set bits before it) in its row
-//      mask and in its column mask.
+//      row_ptr[i] + seg[J][i] (+ the count of its transposed entries on a
+//      diagonal sub-tile, whose columns come first);
+//   3. each entry goes to base + (number of set bits before it) in its row.
+// Each sub-tile is read twice (once per direction) so that each CTA writes
+// contiguous stretches of the CSR rows.
 // Sub-tiles with more than kFillDenseE edge-list entries (the dense blocks of
-// networked data) are queued instead and placed by csr_fill_dense_kernel, one
-// block per sub-tile: the entries' values are staged in a 128 x 128 shared-
+// networked data) are listed first (csr_dense_list_kernel, which also checks
+// every sub-tile's ranges) and placed by csr_fill_dense_kernel, one block per
+// sub-tile, before the row-block pass, which skips them: the entries' values are staged in a 128 x 128 shared-
 // memory matrix, and each row run and each column run of the sub-tile is then
 // written by one warp as consecutive CSR positions (coalesced stores instead
 // of one scattered 4-byte store per column-direction entry).
@@ -37,23 +40,47 @@ __device__ __forceinline__ int popc_before4(const uint32_t* m, int pos) {
   return c;
 }
 
-__global__ __launch_bounds__(kFillWarps * 32) void csr_fill_kernel(CorrArgs a, long long nst,
-                                                                   int* dense_list,
-                                                                   unsigned int* dense_count) {
-  __shared__ uint32_t rmask[kFillWarps][128][4];
-  __shared__ uint32_t cmask[kFillWarps][128][4];
-  __shared__ int rbase[kFillWarps][128];
-  __shared__ int cbase[kFillWarps][128];
+// Row-block order: CTA (I, part) handles the rows of 128-row block I and the
+// column blocks of one contiguous range `part`, its warps taking J = j0 + w,
+// j0 + w + 8, ... in turn.  Sub-tile (I, J), J > I, gives the rows of I their
+// entries (direct); sub-tile (J, I), J < I, gives them its column entries
+// (transposed); the diagonal sub-tile both.  Each CSR row is thus written by
+// `parts` CTAs, each filling one contiguous stretch of it segment after
+// segment while it runs, so partial sectors are completed in L2 instead of
+// being read back and written piecemeal.  Per sub-tile, the rows' segment
+// starts are loaded before the entries (no dependence between the two) and a
+// lane keeps its first kFillKeep entries, candidates already resolved, in
+// registers for the placing pass.  Sub-tiles above kFillDenseE entries are
+// queued (once) for csr_fill_dense_kernel.
+constexpr int kFillKeep = 8;
+
+__global__ __launch_bounds__(kFillWarps * 32) void csr_fill_rows_kernel(CorrArgs a, int I0,
+                                                                        int parts) {
+  __shared__ uint32_t rmask[kFillWarps][128][4];  // direct: row il's columns jl
+  __shared__ uint32_t tmask[kFillWarps][128][4];  // transposed: row jl's columns il
+  __shared__ int dbase[kFillWarps][128];
+  __shared__ int tbase[kFillWarps][128];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int Ir = blockIdx.x / parts, part = blockIdx.x - Ir * parts;
+  const int I = I0 + Ir;
+  const int per = (a.nb + parts - 1) / parts;
+  const int j0 = part * per, j1 = min(a.nb, j0 + per);
   uint32_t(*rm)[4] = rmask[w];
-  uint32_t(*cm)[4] = cmask[w];
-  for (long long st = (long long)blockIdx.x * kFillWarps + w; st < nst;
-       st += (long long)gridDim.x * kFillWarps) {
+  uint32_t(*tm)[4] = tmask[w];
+  for (int J = j0 + w; J < j1; J += kFillWarps) {
+    const int lo = min(I, J), hi = max(I, J);
+    const long long st = subtile_index(lo, hi, a.nb);
     long long s0 = 0, c0 = 0;
     if (lane < 4) {
       const longlong2 e = a.etab[st * 4 + lane];
       s0 = e.x;
       c0 = e.y;
+    }
+    int rbeg[4];  // rows lane + 32k: start of their block-J segment
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int gi = I * 128 + lane + 32 * k;
+      rbeg[k] = gi < a.n ? a.row_ptr[gi] + a.seg[(size_t)J * a.n_pad + gi] : 0;
     }
     long long start[4], cnt[4];
 #pragma unroll
@@ -65,72 +92,95 @@ __global__ __launch_bounds__(kFillWarps * 32) void csr_fill_kernel(CorrArgs a, l
 #pragma unroll
     for (int q = 0; q < 4; ++q)
       inside &= cnt[q] >= 0 && start[q] >= 0 && start[q] + cnt[q] <= a.ecap;
-    if (!inside) {
-      if (lane == 0) atomicOr(a.err, ERR_ELIST);
-      continue;
-    }
     const long long E = cnt[0] + cnt[1] + cnt[2] + cnt[3];
-    if (E == 0) continue;
-    if (E > kFillDenseE) {  // dense sub-tile: queued for csr_fill_dense_kernel
-      if (lane == 0) dense_list[atomicAdd(dense_count, 1u)] = (int)st;
-      continue;
-    }
-    int I, J;
-    tile_coords(st, a.nb, I, J);
-    const bool diag = (I == J);
+    if (!inside || E == 0 || E > kFillDenseE) continue;  // flagged / placed by the dense pass
+    const bool diag = I == J, trans = J < I;
     for (int idx = lane; idx < 512; idx += 32) {
-      rm[idx >> 2][idx & 3] = 0u;
-      cm[idx >> 2][idx & 3] = 0u;
+      (&rm[0][0])[idx] = 0u;
+      (&tm[0][0])[idx] = 0u;
     }
     __syncwarp();
     const long long p1 = cnt[0], p2 = p1 + cnt[1], p3 = p2 + cnt[2];
+    // entry e with its candidate bit resolved: bit 15 set = not an edge,
+    // .y = the value to store
     auto entry = [&](long long e) {
       const int q = e < p1 ? 0 : e < p2 ? 1 : e < p3 ? 2 : 3;
       const long long off = e - (q == 0 ? 0 : q == 1 ? p1 : q == 2 ? p2 : p3);
       const long long s = q == 0 ? start[0] : q == 1 ? start[1] : q == 2 ? start[2] : start[3];
-      return a.elist[s + off];
-    };
-    // 1. bitmasks (candidates resolved through the recompute hash)
-    for (long long e = lane; e < E; e += 32) {
-      const uint2 en = entry(e);
-      const int il = en.x & 127, jl = (en.x >> 7) & 127;
-      bool edge = true;
+      uint2 en = a.elist[s + off];
       if ((en.x >> 14) & 1u) {
-        float v;
-        hash_lookup(a, pair_key(I * 128 + il, J * 128 + jl), v, edge);
+        float v = 0.0f;
+        bool edge = false;
+        hash_lookup(a, pair_key(lo * 128 + (en.x & 127), hi * 128 + ((en.x >> 7) & 127)), v, edge);
+        en.y = __float_as_uint(v);
+        if (!edge) en.x |= 1u << 15;
       }
-      if (edge) {
-        atomicOr(&rm[il][jl >> 5], 1u << (jl & 31));
-        atomicOr(&cm[jl][il >> 5], 1u << (il & 31));
-      }
+      return en;
+    };
+    // 1. masks
+    uint2 keep[kFillKeep];
+#pragma unroll
+    for (int k = 0; k < kFillKeep; ++k) {
+      const long long e = lane + 32 * k;
+      keep[k] = make_uint2(1u << 15, 0u);
+      if (e < E) keep[k] = entry(e);
     }
-    __syncwarp();
-    // 2. segment bases of the 128 rows and 128 columns
-    for (int r = lane; r < 128; r += 32) {
-      const int gi = I * 128 + r, gj = J * 128 + r;
-      int b = 0;
-      if (gi < a.n) {
-        b = a.row_ptr[gi] + a.seg[(size_t)J * a.n_pad + gi];
-        if (diag) b += __popc(cm[r][0]) + __popc(cm[r][1]) + __popc(cm[r][2]) + __popc(cm[r][3]);
-      }
-      rbase[w][r] = b;
-      cbase[w][r] = (gj < a.n) ? a.row_ptr[gj] + a.seg[(size_t)I * a.n_pad + gj] : 0;
-    }
-    __syncwarp();
-    // 3. place both directions
-    for (long long e = lane; e < E; e += 32) {
-      const uint2 en = entry(e);
+    auto mark = [&](uint2 en) {
+      if ((en.x >> 15) & 1u) return;
       const int il = en.x & 127, jl = (en.x >> 7) & 127;
-      const int gi = I * 128 + il, gj = J * 128 + jl;
-      float v = __uint_as_float(en.y);
-      bool edge = true;
-      if ((en.x >> 14) & 1u) hash_lookup(a, pair_key(gi, gj), v, edge);
-      if (!edge) continue;
-      put_edge(a, (long long)rbase[w][il] + popc_before4(rm[il], jl), gj, v);
-      put_edge(a, (long long)cbase[w][jl] + popc_before4(cm[jl], il), gi, v);
+      if (!trans) atomicOr(&rm[il][jl >> 5], 1u << (jl & 31));
+      if (trans || diag) atomicOr(&tm[jl][il >> 5], 1u << (il & 31));
+    };
+#pragma unroll
+    for (int k = 0; k < kFillKeep; ++k) mark(keep[k]);
+    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) mark(entry(e));
+    __syncwarp();
+    // 2. segment bases of the block's rows for column block J (on the
+    // diagonal the transposed entries, columns < the row, come first)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int r = lane + 32 * k;
+      const int c = __popc(tm[r][0]) + __popc(tm[r][1]) + __popc(tm[r][2]) + __popc(tm[r][3]);
+      tbase[w][r] = rbeg[k];
+      dbase[w][r] = diag ? rbeg[k] + c : rbeg[k];
     }
+    __syncwarp();
+    // 3. place this block's entries: direct (row il) and transposed (row jl)
+    auto place = [&](uint2 en) {
+      if ((en.x >> 15) & 1u) return;
+      const int il = en.x & 127, jl = (en.x >> 7) & 127;
+      const float v = __uint_as_float(en.y);
+      if (!trans)
+        put_edge(a, (long long)dbase[w][il] + popc_before4(rm[il], jl), hi * 128 + jl, v);
+      if (trans || diag)
+        put_edge(a, (long long)tbase[w][jl] + popc_before4(tm[jl], il), lo * 128 + il, v);
+    };
+#pragma unroll
+    for (int k = 0; k < kFillKeep; ++k) place(keep[k]);
+    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) place(entry(e));
     __syncwarp();
   }
+}
+
+// The dense sub-tiles' list (and the check of every sub-tile's ranges),
+// one thread per sub-tile.
+__global__ __launch_bounds__(256) void csr_dense_list_kernel(CorrArgs a, long long nst,
+                                                             int* dense_list,
+                                                             unsigned int* dense_count) {
+  const long long st = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (st >= nst) return;
+  long long E = 0;
+  bool inside = true;  // ranges written while the pool overflowed are not read
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const longlong2 e = a.etab[st * 4 + q];
+    inside &= e.y >= 0 && e.x >= 0 && e.x + e.y <= a.ecap;
+    E += e.y;
+  }
+  if (!inside)
+    atomicOr(a.err, ERR_ELIST);
+  else if (E > kFillDenseE)
+    dense_list[atomicAdd(dense_count, 1u)] = (int)st;
 }
 
 // Dense sub-tiles, one block (8 warps) per sub-tile.
@@ -163,7 +213,7 @@ __global__ __launch_bounds__(256) void csr_fill_dense_kernel(CorrArgs a, const i
     int I, J;
     tile_coords(st, a.nb, I, J);
     const bool diag = (I == J);
-    // 1. bitmasks and values (ranges were checked by csr_fill_kernel)
+    // 1. bitmasks and values (ranges were checked by csr_dense_list_kernel)
     const long long p1 = S.cnt[0], p2 = p1 + S.cnt[1], p3 = p2 + S.cnt[2], E = p3 + S.cnt[3];
     for (long long e = tid; e < E; e += 256) {
       const int q = e < p1 ? 0 : e < p2 ? 1 : e < p3 ? 2 : 3;
@@ -180,7 +230,7 @@ __global__ __launch_bounds__(256) void csr_fill_dense_kernel(CorrArgs a, const i
       }
     }
     __syncthreads();
-    // 2. segment bases (as in csr_fill_kernel)
+    // 2. segment bases (as in csr_fill_rows_kernel)
     if (tid < 128) {
       const int r = tid, gi = I * 128 + r;
       int b = 0;
@@ -217,20 +267,38 @@ __global__ __launch_bounds__(256) void csr_fill_dense_kernel(CorrArgs a, const i
   }
 }
 
-cudaError_t launch_csr_fill(const CorrArgs& a, int sms, int* dense_list, unsigned int* dense_count,
-                            cudaStream_t stream) {
+cudaError_t launch_csr_fill_dense(const CorrArgs& a, int sms, int* dense_list,
+                                  unsigned int* dense_count, cudaStream_t stream) {
+  if (a.nb <= 0) return cudaSuccess;
   const long long nst = (long long)a.nb * (a.nb + 1) / 2;
-  const long long want = (nst + kFillWarps - 1) / kFillWarps;
-  const int grid = (int)(want < (long long)sms * 4 ? want : (long long)sms * 4);
-  if (grid <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(dense_count, 0, sizeof(unsigned int), stream);
   if (e != cudaSuccess) return e;
-  csr_fill_kernel<<<grid, kFillWarps * 32, 0, stream>>>(a, nst, dense_list, dense_count);
+  csr_dense_list_kernel<<<(unsigned)((nst + 255) / 256), 256, 0, stream>>>(a, nst, dense_list,
+                                                                         dense_count);
   e = cudaFuncSetAttribute(csr_fill_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sizeof(DenseSmem));
   if (e != cudaSuccess) return e;
   csr_fill_dense_kernel<<<sms * 3, 256, sizeof(DenseSmem), stream>>>(a, dense_list, dense_count);
   return cudaGetLastError();
+}
+
+cudaError_t launch_csr_fill_rows(const CorrArgs& a, int sms, int I0, int I1,
+                                 cudaStream_t stream) {
+  if (I1 <= I0) return cudaSuccess;
+  const int rows = I1 - I0;
+  // split the column blocks so that about 8 CTAs per SM take part
+  int parts = (sms * 8 + rows - 1) / rows;
+  if (parts > (a.nb + 7) / 8) parts = (a.nb + 7) / 8;
+  if (parts < 1) parts = 1;
+  csr_fill_rows_kernel<<<rows * parts, kFillWarps * 32, 0, stream>>>(a, I0, parts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csr_fill(const CorrArgs& a, int sms, int* dense_list, unsigned int* dense_count,
+                            cudaStream_t stream) {
+  cudaError_t e = launch_csr_fill_dense(a, sms, dense_list, dense_count, stream);
+  if (e != cudaSuccess) return e;
+  return launch_csr_fill_rows(a, sms, 0, a.nb, stream);
 }
 
 }  // namespace bna

@@ -250,6 +250,30 @@ def test_host_into_caller_buffers_and_capacity(builder):
     assert np.array_equal(ci, d.col_idx) and np.array_equal(va, d.val)
 
 
+@pytest.mark.parametrize("mode,value,weighted", [("r_ge", 0.3, True), ("density", 2.0, True),
+                                                 ("abs_ge", 0.35, False)])
+def test_host_into_chunked_copies_equal_device_path(builder, mode, value, weighted):
+    """The host-buffer form copies the CSR out in row-block chunks behind the
+    fill pass (pinned buffers, several row blocks per chunk): same CSR as the
+    device form."""
+    import torch
+    b = bna.synth_bold(5000, 100, 12, 17)
+    d = builder.corr_csr(dev(b), mode=mode, value=value, weighted=weighted,
+                         precision="bf16x3").numpy()
+    pin = lambda n, dt: torch.empty(n, dtype=dt).pin_memory().numpy()
+    rp = pin(5001, torch.int32)
+    ci = pin(d.nnz + 100, torch.int32)
+    va = pin(d.nnz + 100, torch.float32) if weighted else None
+    bp = torch.from_numpy(b).pin_memory().numpy()
+    nnz, st = builder.corr_csr_host_into(bp, rp, ci, va, mode=mode, value=value,
+                                         precision="bf16x3")
+    assert nnz == d.nnz and np.array_equal(rp, d.row_ptr)
+    assert st["kernel_launches"] > 0
+    assert np.array_equal(ci[:nnz], d.col_idx)
+    if weighted:
+        assert np.array_equal(va[:nnz], d.val)
+
+
 def test_repeat_calls_are_deterministic(builder):
     b = dev(bna.synth_bold(2000, 120, 20, 5))
     r1 = builder.corr_csr(b, mode="r_gt", value=0.3).numpy()
