@@ -238,7 +238,8 @@ def serve_run(n_requests: int, slots: int = 4, rate: float = 4.0, seed: int = 50
                         "mode": r.mode, "value": r.value, "arrival": r.arrival,
                         "status": m.status, "slot": m.slot, "nnz": m.nnz,
                         "sub": m.t_submit, "start": m.t_start, "done": m.t_done,
-                        "solo": a.latency, "iters": m.ec_iters, "stats": m.stats}
+                        "corr": m.t_corr, "solo": a.latency, "solo_corr": a.t_corr - a.t_submit,
+                        "iters": m.ec_iters, "stats": m.stats}
                        for k, (r, m, a) in enumerate(zip(reqs, mixed, alone))], f)
     lat = np.array([r.latency for r in mixed]) * 1000.0
     solo = np.array([r.latency for r in alone]) * 1000.0

@@ -136,8 +136,19 @@ class Builder:
         return names[best.value], {"bf16x3": ms[0], "tf32": ms[1]}
 
     def set_option(self, name: str, value: int):
-        """bna_ctx_set_option: "tiles_per_launch" or "max_nnz" (0 = default)."""
+        """bna_ctx_set_option: "tiles_per_launch", "max_nnz" or "ec_iters_per_launch"
+        (0 = default)."""
         _check(lib().bna_ctx_set_option(self._h, L.OPTIONS[name], int(value)), self._h)
+
+    GATE = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64)
+
+    def set_gate(self, fn=None):
+        """bna_ctx_set_gate: fn(stream_handle, phase, done) is called between the
+        launches of long passes (None removes it)."""
+        self._gate = Builder.GATE(lambda user, stream, phase, done: fn(stream, phase, done)) \
+            if fn else None
+        _check(lib().bna_ctx_set_gate(self._h, C.cast(self._gate, C.c_void_p) if fn else None,
+                                      None), self._h)
 
     @staticmethod
     def _stream(stream):
@@ -380,6 +391,7 @@ class Reply:
     t_submit: float
     t_start: float
     t_done: float
+    t_corr: float
     stats: dict
 
     @property
@@ -450,7 +462,8 @@ class Server:
                      val=va[:nnz] if va is not None else None,
                      ec=ecv, lam=rep.lambda_, ec_iters=rep.ec_iters,
                      ec_converged=bool(rep.ec_converged), t_submit=rep.t_submit,
-                     t_start=rep.t_start, t_done=rep.t_done, stats=rep.stats.as_dict())
+                     t_start=rep.t_start, t_done=rep.t_done, t_corr=rep.t_corr,
+                     stats=rep.stats.as_dict())
 
     @property
     def device_bytes(self) -> int:

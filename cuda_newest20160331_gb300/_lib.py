@@ -16,7 +16,7 @@ BNA_OK = 0
 BNA_NOT_CONVERGED = 4
 BNA_CAPACITY = 13
 BNA_OVER_BUDGET = 14
-OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1}
+OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1, "ec_iters_per_launch": 2}
 THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4}
 PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2, "auto": 3}
 SYNTH_KINDS = {"iid": 0, "blocknet": 1}
@@ -57,7 +57,7 @@ class Reply(C.Structure):
     _fields_ = [("status", C.c_int32), ("slot", C.c_int32), ("tag", C.c_int64),
                 ("nnz", C.c_int64), ("lambda_", C.c_double), ("ec_iters", C.c_int32),
                 ("ec_converged", C.c_int32), ("t_submit", C.c_double), ("t_start", C.c_double),
-                ("t_done", C.c_double), ("stats", CorrStats)]
+                ("t_done", C.c_double), ("t_corr", C.c_double), ("stats", CorrStats)]
 
 
 class SynthParams(C.Structure):
@@ -102,6 +102,7 @@ SIGNATURES = {
     "bna_ec_write": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32]),
     "bna_synth_bold": (C.c_int, [C.POINTER(SynthParams), C.c_void_p, C.c_int]),
     "bna_ctx_set_option": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64]),
+    "bna_ctx_set_gate": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "bna_server_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
     "bna_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "bna_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(Reply)]),

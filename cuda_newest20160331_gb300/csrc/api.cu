@@ -11,6 +11,7 @@
 #include <cstring>
 #include <string>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -42,9 +43,12 @@ int ec_state_err(const void* host_copy);
 int ec_coop_grid(int n, int sms);
 cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
                            const double* vald, long long nnz_used, double* u, float2* uf,
-                           double* parts, void* st, int grid, int max_iter, double eps,
-                           cudaStream_t stream);
+                           double* parts, void* st, int grid, int it_end, int max_iter,
+                           double eps, cudaStream_t stream);
 void tc_tile_list(int nb, std::vector<int2>& out);
+long long tc_tile_count(int nb);
+cudaError_t launch_tile_lists(int nb, int2* tiles, long long n_smp, int s, int2* smp,
+                              cudaStream_t st);
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
@@ -117,6 +121,7 @@ struct DevStatus {
 
 struct EcGraph {
   cudaGraphExec_t exec = nullptr;
+  int iters = 0;  // iterations per replay
   const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int n = -1, grid = 0, max_iter = 0;
   long long nnz_used = -1;
@@ -186,6 +191,9 @@ struct bna_ctx {
   };
   Sink* sink = nullptr;
   cudaStream_t copy_stream = nullptr;
+  int ec_seg = 0;               // BNA_OPT_EC_ITERS_PER_LAUNCH
+  bna_gate_fn gate = nullptr;  // bna_ctx_set_gate
+  void* gate_user = nullptr;
   cudaEvent_t chunk_ev[kFillChunks + 1] = {};
 };
 
@@ -211,6 +219,40 @@ int32_t fail(bna_ctx* c, int32_t st, const char* fmt, ...) {
                   __FILE__, __LINE__);                                                   \
   } while (0)
 
+}  // namespace
+
+namespace bna {
+
+// The library's device memory pool, one per device: freed arena blocks stay
+// cached in it (release threshold: no limit) instead of going back to the
+// driver at every synchronisation, so an arena that grows again (a server
+// slot taking a larger request) reuses memory instead of mapping new memory;
+// bna_ctx_trim hands the cached memory back.
+cudaMemPool_t lib_pool(int device) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(device);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  uint64_t keep = ~0ull;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  pools[device] = pool;
+  return pool;
+}
+
+}  // namespace bna
+
+namespace {
+
 int32_t ensure(bna_ctx* ctx, Slot s, size_t bytes, void** out) {
   if (bytes == 0) bytes = 16;
   if (ctx->cap[s] < bytes) {
@@ -224,10 +266,14 @@ int32_t ensure(bna_ctx* ctx, Slot s, size_t bytes, void** out) {
         return fail(ctx, BNA_CUDA_ERROR, "cudaFreeAsync: %s", cudaGetErrorString(e));
     }
     const size_t want = bytes + bytes / 8;  // headroom so small growth does not reallocate
-    cudaError_t e = cudaMallocAsync(&ctx->ptr[s], want, ctx->cur);
+    cudaMemPool_t pool = lib_pool(ctx->device);
+    if (!pool) return fail(ctx, BNA_CUDA_ERROR, "no device memory pool");
+    cudaError_t e = cudaMallocFromPoolAsync(&ctx->ptr[s], want, pool, ctx->cur);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      e = cudaMallocAsync(&ctx->ptr[s], bytes, ctx->cur);
+      cudaStreamSynchronize(ctx->cur);
+      cudaMemPoolTrimTo(pool, 0);  // cached blocks of other sizes go back first
+      e = cudaMallocFromPoolAsync(&ctx->ptr[s], bytes, pool, ctx->cur);
       if (e != cudaSuccess) {
         cudaGetLastError();
         ctx->ptr[s] = nullptr;
@@ -313,23 +359,19 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
   CK(launch_block_bad(a.bad, a.nb, bb, st));
   ctx->klaunch += 1;
   if (ctx->tiles_nb != a.nb) {
-    std::vector<int2> t;
-    tc_tile_list(a.nb, t);
-    int2* d;
-    ENSURE(S_TILES, t.size() * sizeof(int2), d);
-    CK(cudaMemcpyAsync(d, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
+    // built on the device in stream order: no host wait for the work ahead
+    const long long nt = tc_tile_count(a.nb);
     // every s-th tile: the sample the density histogram may be taken on
-    const int s = std::max<int>(1, (int)t.size() / kSampleTiles);
-    std::vector<int2> smp;
-    for (size_t i = 0; i < t.size(); i += s) smp.push_back(t[i]);
-    int2* ds;
-    ENSURE(S_TILES_SMP, smp.size() * sizeof(int2), ds);
-    CK(cudaMemcpyAsync(ds, smp.data(), smp.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
+    const int s = (int)std::max<long long>(1, nt / kSampleTiles);
+    const long long nsmp = (nt + s - 1) / s;
+    int2 *d, *ds;
+    ENSURE(S_TILES, (size_t)nt * sizeof(int2), d);
+    ENSURE(S_TILES_SMP, (size_t)nsmp * sizeof(int2), ds);
+    CK(launch_tile_lists(a.nb, d, nsmp, s, ds, st));
+    ctx->klaunch += 2;
     ctx->tiles_nb = a.nb;
-    ctx->ntiles = (int)t.size();
-    ctx->ntiles_smp = (int)smp.size();
+    ctx->ntiles = (int)nt;
+    ctx->ntiles_smp = (int)nsmp;
   }
   return BNA_OK;
 }
@@ -379,6 +421,11 @@ void window_from_hist(const unsigned int* hh, long long k_dens, bool sampled, in
 
 // pass 0: count (+ edge lists); pass 3: density histogram (sampled: on the
 // sampled tile list, tensor-core forms)
+// The caller's launch gate (bna_ctx_set_gate), if any.
+inline void gate(bna_ctx* ctx, cudaStream_t st, int phase, long long done) {
+  if (ctx->gate) ctx->gate(ctx->gate_user, st, phase, done);
+}
+
 int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st,
                   bool sampled = false) {
   if (ctx->avg) {  // the averaged matrix is the source
@@ -396,11 +443,13 @@ int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cuda
       const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[sampled ? S_TILES_SMP : S_TILES]);
       const int nt = sampled ? ctx->ntiles_smp : ctx->ntiles;
       const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : nt;
-      for (int t0 = 0; t0 < nt; t0 += per, ++ctx->klaunch)
+      for (int t0 = 0; t0 < nt; t0 += per, ++ctx->klaunch) {
+        if (t0 > 0) gate(ctx, st, BNA_PHASE_CORR, t0);
         CK(launch_corr_tc(a, pass, precision == BNA_PREC_BF16X3 ? 0 : 1, tiles + t0,
                           std::min(per, nt - t0),
                           reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
                           ctx->sms, st));
+      }
       return BNA_OK;
     }
     default:
@@ -499,6 +548,13 @@ int64_t bna_request_bytes(int32_t N, int32_t T, const bna_corr_opts* opts, int64
   return b;
 }
 
+int32_t bna_ctx_set_gate(bna_ctx* ctx, bna_gate_fn fn, void* user) {
+  if (!ctx) return BNA_BAD_ARG;
+  ctx->gate = fn;
+  ctx->gate_user = fn ? user : nullptr;
+  return BNA_OK;
+}
+
 int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value) {
   if (!ctx || value < 0) return fail(ctx, BNA_BAD_ARG, "bna_ctx_set_option: bad arguments");
   switch (option) {
@@ -507,25 +563,52 @@ int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value) {
       ctx->tiles_per_launch = (int)value;
       return BNA_OK;
     case BNA_OPT_MAX_NNZ: ctx->max_nnz = value; return BNA_OK;
+    case BNA_OPT_EC_ITERS_PER_LAUNCH:
+      if (value > 1000000) return fail(ctx, BNA_BAD_ARG, "iterations per launch too large");
+      ctx->ec_seg = (int)value;
+      return BNA_OK;
     default: return fail(ctx, BNA_BAD_ARG, "unknown option %d", option);
   }
 }
+
+}  // extern "C"
+
+// Free the arena on `st` (into the library's pool; with to_driver, the
+// pool's cached memory then goes back to the driver); the caller guarantees
+// that no work using the arena is pending on any other stream.
+static void arena_release(bna_ctx* ctx, cudaStream_t st, bool to_driver) {
+  for (int s = 0; s < S_COUNT; ++s) {
+    if (ctx->ptr[s]) cudaFreeAsync(ctx->ptr[s], st);
+    ctx->ptr[s] = nullptr;
+    ctx->cap[s] = 0;
+  }
+  cudaStreamSynchronize(st);
+  if (to_driver)
+    if (cudaMemPool_t pool = lib_pool(ctx->device)) cudaMemPoolTrimTo(pool, 0);
+  ctx->tiles_nb = -1;  // the tile list lived in the arena
+  ctx->last_ok = false;
+  if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
+  ctx->ecg = EcGraph();
+}
+
+// Trim of a context whose every call has been synchronised (a server slot
+// between requests): no device-wide wait, and the memory stays cached in the
+// library's pool for the request that needs it.
+int32_t bna_ctx_trim_idle(bna_ctx* ctx) {
+  if (!ctx) return BNA_BAD_ARG;
+  cudaSetDevice(ctx->device);
+  arena_release(ctx, ctx->cur, false);
+  return BNA_OK;
+}
+
+extern "C" {
 
 int32_t bna_ctx_trim(bna_ctx* ctx) {
   if (!ctx) return BNA_BAD_ARG;
   cudaSetDevice(ctx->device);
   // the arena is stream-ordered memory: wait for every user, then free it
   cudaDeviceSynchronize();
-  for (int s = 0; s < S_COUNT; ++s) {
-    if (ctx->ptr[s]) cudaFreeAsync(ctx->ptr[s], nullptr);
-    ctx->ptr[s] = nullptr;
-    ctx->cap[s] = 0;
-  }
-  cudaStreamSynchronize(nullptr);
-  ctx->tiles_nb = -1;  // the tile list lived in the arena
-  ctx->last_ok = false;
-  if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
-  ctx->ecg = EcGraph();
+  arena_release(ctx, nullptr, true);
   return BNA_OK;
 }
 
@@ -1037,6 +1120,16 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
     CK(cudaEventRecord(ctx->chunk_ev[nch], ctx->copy_stream));
     CK(cudaStreamWaitEvent(st, ctx->chunk_ev[nch], 0));
     sink->done = true;
+    fill_launches = 2 + nch;
+  } else if (ctx->gate) {
+    // row-block chunks with the gate between them
+    CK(launch_csr_fill_dense(a, ctx->sms, dense_list, &ds->dense, st));
+    const int nch = std::min(kFillChunks, a.nb);
+    for (int c = 0; c < nch; ++c) {
+      if (c > 0) gate(ctx, st, BNA_PHASE_FILL, (long long)c * a.nb / nch);
+      CK(launch_csr_fill_rows(a, ctx->sms, (int)((long long)c * a.nb / nch),
+                              (int)((long long)(c + 1) * a.nb / nch), st));
+    }
     fill_launches = 2 + nch;
   } else {
     CK(launch_csr_fill(a, ctx->sms, dense_list, &ds->dense, st));
@@ -1785,26 +1878,52 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
   // the whole iteration as one cooperative persistent launch
   const int cgrid = ec_coop_grid(n, ctx->sms);
   if (cgrid > 0) {
-    CK(launch_ec_coop(n, rp, ci, val, vald, nnz_used, u, uf, parts, state, cgrid, max_iter, eps,
-                      st));
-    CK(cudaMemcpyAsync(ctx->pinned, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (ec_state_err(ctx->pinned))
-      return fail(ctx, BNA_TIMEOUT, "centrality: a bounded grid barrier expired");
+    // one launch; with a launch gate, segments of about a millisecond of
+    // iterations (each resumes from the state block) with the gate between
+    int seg = std::max(max_iter, 1);
+    if (ctx->ec_seg > 0) {
+      seg = ctx->ec_seg;
+    } else if (ctx->gate) {
+      const double iter_us = std::max(10.0, (8.0 * (double)nnz_used + 16.0 * n) / 2.0e6);
+      seg = (int)std::max(2.0, 1000.0 / iter_us);
+    }
     double lam2 = 0, lam = 0, e1 = 0, e2 = 0;
     int it = 0, done = 0;
-    ec_state_read(ctx->pinned, &lam2, &lam, &e1, &e2, &it, &done);
+    for (long long it_end = std::min(seg, max_iter);; it_end += seg) {
+      if (it > 0) gate(ctx, st, BNA_PHASE_EC, it);
+      CK(launch_ec_coop(n, rp, ci, val, vald, nnz_used, u, uf, parts, state, cgrid,
+                        (int)std::min<long long>(it_end, max_iter), max_iter, eps, st));
+      CK(cudaMemcpyAsync(ctx->pinned, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (ec_state_err(ctx->pinned))
+        return fail(ctx, BNA_TIMEOUT, "centrality: a bounded grid barrier expired");
+      ec_state_read(ctx->pinned, &lam2, &lam, &e1, &e2, &it, &done);
+      if (done || it >= max_iter) break;
+    }
     CK(cudaMemcpyAsync(ec_dev, u + (size_t)(it & 1) * n, (size_t)n * sizeof(double),
                        cudaMemcpyDeviceToDevice, st));
     if (lambda) *lambda = lam;
     if (iters) *iters = it;
     return (e1 <= eps || e2 <= eps) ? BNA_OK : BNA_NOT_CONVERGED;
   }
-  // otherwise: a captured graph of kGraphIters per-iteration launches
+  // otherwise: a captured graph of per-iteration launches, kGraphIters of
+  // them (with a launch gate: about a millisecond of iterations, estimated
+  // from the CSR bytes an iteration streams at ~2 TB/s, so the gate runs
+  // that often)
+  int giters = kGraphIters;
+  if (ctx->ec_seg > 0) {
+    giters = std::min(ctx->ec_seg + (ctx->ec_seg & 1), 1 << 12);
+  } else if (ctx->gate) {
+    const double iter_us = (8.0 * (double)nnz_used + 16.0 * n) / 2.0e6;
+    giters = (int)std::max(1.0, std::min((double)kGraphIters, 1000.0 / std::max(iter_us, 1.0)));
+    // even: iteration it of a replay reads buffer it & 1, so every replay
+    // must end on the buffer the next one starts from
+    giters = std::max(2, giters & ~1);
+  }
   EcGraph& g = ctx->ecg;
   const void* key[6] = {rp, ci, val, vald, u, state};
   bool same = g.exec && g.n == n && g.grid == grid && g.max_iter == max_iter && g.eps == eps &&
-              g.nnz_used == nnz_used;
+              g.nnz_used == nnz_used && g.iters == giters;
   for (int k = 0; k < 6 && same; ++k) same = (g.key[k] == key[k]);
   if (!same) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -1812,7 +1931,7 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
     cudaStream_t cap;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < kGraphIters; ++it) {
+    for (int it = 0; it < giters; ++it) {
       const size_t cur = (size_t)(it & 1) * n, nxt = (size_t)((it + 1) & 1) * n;
       launch_ec_iter(n, rp, ci, val, vald, nnz_used, u + cur, uf + cur, u + nxt, uf + nxt, parts,
                      state, grid, max_iter, eps, cap);
@@ -1830,10 +1949,12 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
     g.max_iter = max_iter;
     g.eps = eps;
     g.nnz_used = nnz_used;
+    g.iters = giters;
   }
   double lam2 = 0, lam = 0, e1 = 0, e2 = 0;
   int it = 0, done = 0;
-  for (int launched = 0; launched < max_iter; launched += kGraphIters) {
+  for (int launched = 0; launched < max_iter; launched += giters) {
+    if (launched > 0) gate(ctx, st, BNA_PHASE_EC, it);
     CK(cudaGraphLaunch(g.exec, st));
     CK(cudaMemcpyAsync(ctx->pinned, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

@@ -749,6 +749,39 @@ void tc_tile_list(int nb, std::vector<int2>& out) {
     for (int jp = I / 2; jp < njp; ++jp) out.push_back(make_int2(I, jp));
 }
 
+// The same list built on the device (no host round trip): row block I holds
+// (I, jp) for jp = I/2 .. njp-1 and starts at I * njp - sum_{I' < I} floor(I'/2),
+// which is m(m-1) for I = 2m and m^2 for I = 2m+1.  One warp per row block.
+__host__ __device__ inline long long tile_row_offset(int I, int njp) {
+  const long long m = I / 2;
+  return (long long)I * njp - ((I & 1) ? m * m : m * (m - 1));
+}
+
+long long tc_tile_count(int nb) { return tile_row_offset(nb, (nb + 1) / 2); }
+
+__global__ void tile_list_kernel(int nb, int2* out) {
+  const int I = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (I >= nb) return;
+  const int njp = (nb + 1) / 2, m = I / 2;
+  const long long off = tile_row_offset(I, njp);
+  for (int jp = m + lane; jp < njp; jp += 32) out[off + jp - m] = make_int2(I, jp);
+}
+
+// Every s-th tile of the list (the density histogram's sample).
+__global__ void tile_sample_kernel(const int2* tiles, long long n_smp, int s, int2* out) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n_smp) out[k] = tiles[k * s];
+}
+
+cudaError_t launch_tile_lists(int nb, int2* tiles, long long n_smp, int s, int2* smp,
+                              cudaStream_t st) {
+  if (nb <= 0) return cudaSuccess;
+  tile_list_kernel<<<(nb + 7) / 8, 256, 0, st>>>(nb, tiles);
+  if (n_smp > 0)
+    tile_sample_kernel<<<(unsigned)((n_smp + 255) / 256), 256, 0, st>>>(tiles, n_smp, s, smp);
+  return cudaGetLastError();
+}
+
 size_t tc_smem_bytes() { return TC_SMEM_BYTES; }
 
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st) {

@@ -315,15 +315,18 @@ template <int VK>
 __global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
     int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
     const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
-    double* u, float2* uf, double* parts, EcState* st, int max_iter, double eps) {
+    double* u, float2* uf, double* parts, EcState* st, int it_end, int max_iter, double eps) {
   __shared__ double ws[kEcThreads / 32][3];
   __shared__ double red[kEcThreads][3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = gridDim.x * (kEcThreads / 32);
-  double lam2 = st->lam2, lam_used = 0.0, e1 = 1.0, e2 = 1.0;
-  int it = 0;
+  // resume from the state block (ec_init_kernel's, or the previous segment's)
+  double lam2 = st->lam2, lam_used = st->lambda_used, e1 = st->e1, e2 = st->e2;
+  int it = st->iter;
+  if (st->done) it_end = it;
+  if (it_end > max_iter) it_end = max_iter;
   __shared__ double lam_s[2];
-  while (it < max_iter) {
+  while (it < it_end) {
     if (threadIdx.x == 0) {
       lam_s[0] = sqrt(lam2);
       lam_s[1] = 1.0 / lam_s[0];
@@ -416,13 +419,15 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
     ++it;
     if (e1 <= eps || e2 <= eps) break;
   }
+  // every block has read the state above before the first grid barrier; with
+  // no iteration run, block 0 writes back what it read
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->lambda_used = lam_used;
     st->lam2 = lam2;
     st->e1 = e1;
     st->e2 = e2;
     st->iter = it;
-    st->done = 1;
+    st->done = (e1 <= eps || e2 <= eps || it >= max_iter) ? 1 : 0;
   }
 }
 
@@ -445,13 +450,15 @@ int ec_coop_grid(int n, int sms) {
   return want < sms ? (want < 1 ? 1 : want) : sms;
 }
 
-// The whole power iteration: parts holds 2 * grid * 3 doubles.
+// The power iteration from the state block's iteration up to it_end (the
+// whole of it with it_end = max_iter): parts holds 2 * grid * 3 doubles.
 cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
                            const double* vald, long long nnz_used, double* u, float2* uf,
-                           double* parts, void* st, int grid, int max_iter, double eps,
-                           cudaStream_t stream) {
+                           double* parts, void* st, int grid, int it_end, int max_iter,
+                           double eps, cudaStream_t stream) {
   EcState* s = (EcState*)st;
-  void* args[] = {&n, &rp, &ci, &val, &vald, &nnz_used, &u, &uf, &parts, &s, &max_iter, &eps};
+  void* args[] = {&n,     &rp, &ci, &val, &vald,   &nnz_used, &u,
+                  &uf,    &parts, &s, &it_end, &max_iter, &eps};
   const void* fn = val    ? (const void*)ec_coop_kernel<1>
                    : vald ? (const void*)ec_coop_kernel<2>
                           : (const void*)ec_coop_kernel<0>;

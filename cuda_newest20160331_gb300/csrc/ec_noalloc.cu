@@ -39,8 +39,8 @@ int ec_state_err(const void* host_copy);
 int ec_coop_grid(int n, int sms);
 cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
                            const double* vald, long long nnz_used, double* u, float2* uf,
-                           double* parts, void* st, int grid, int max_iter, double eps,
-                           cudaStream_t stream);
+                           double* parts, void* st, int grid, int it_end, int max_iter,
+                           double eps, cudaStream_t stream);
 }  // namespace bna
 
 namespace {
@@ -125,7 +125,7 @@ extern "C" int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, doub
   const int cgrid = std::min(ec_coop_grid(n, sms), kNoAllocMaxGrid / 2);
   if (cgrid > 0) {
     e = launch_ec_coop(n, csr_dev->row_ptr, csr_dev->col_idx, csr_dev->val, nullptr, nnz_used, u,
-                       uf, parts, state, cgrid, max_iter, eps, st);
+                       uf, parts, state, cgrid, max_iter, max_iter, eps, st);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(host_state, state, ec_state_bytes(), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -16,6 +16,15 @@
 //     less work use a higher-priority stream, and correlation passes are cut
 //     into launches of a bounded number of tiles, so the block scheduler can
 //     serve a small request between the launches of a large one;
+//   - launch gate (shortest job first): below the top priority level a
+//     request keeps at most two of its launches queued, and while a request
+//     with less correlation work (N^2 T; ties: the one started first) runs on
+//     another slot it drains its stream and waits (at most kGateWaitMs per
+//     gate) before queueing more; so a small request meets at most one
+//     launch of a large one on the device, not its whole queue.  A centrality
+//     that has run kLongEc iterations no longer makes others wait, so a slowly
+//     converging small graph does not hold up larger requests, and such
+//     centralities run one at a time (first started, first served);
 //   - results are independent of the mix: each slot's kernels see only their
 //     own request's buffers, and every reduction has a fixed order.
 #include <algorithm>
@@ -31,6 +40,11 @@
 #include <cuda_runtime.h>
 
 #include "bna.h"
+
+namespace bna {
+cudaMemPool_t lib_pool(int device);
+}
+int32_t bna_ctx_trim_idle(bna_ctx* ctx);
 
 namespace {
 
@@ -48,7 +62,15 @@ struct Job {
 constexpr int kLevels = 6;  // stream priority levels used (fewer if the device has fewer)
 
 struct Slot {
+  bna_server* srv = nullptr;
   int index = 0;
+  int level = 0;                  // priority level of the running request
+  double work = 0;                // its N^2 T (launch gate order)
+  int64_t seq = 0;                // its start order (ties of work)
+  int phase = 0;                  // its pass and progress at its last gate call
+  int64_t progress = 0;
+  cudaEvent_t fence[2] = {};      // launch gate: queue-depth events
+  int nfence = 0;
   bna_ctx* ctx = nullptr;
   cudaStream_t stream[kLevels] = {};  // stream[0]: highest priority
   float* bold = nullptr;
@@ -70,8 +92,15 @@ int level_of(double work, int levels) {
   for (double w = 1.0e10; work >= w && l < levels - 1; w *= 10.0) ++l;
   return l;
 }
-// Tiles per correlation launch (about 1 ms of tensor work at T = 1200).
-constexpr int kTilesPerLaunch = 6144;
+// Tiles per correlation launch: about 0.16 ms of tensor work (1,536 tiles at
+// T = 1200, proportionally more for shorter series).
+int tiles_per_launch(int T) { return std::max(512, (int)(1536LL * 1200 / std::max(T, 1))); }
+// Longest wait of one gate call for higher-priority requests to finish.
+constexpr int kGateWaitMs = 200;
+// A centrality past this many iterations (a graph that converges slowly or
+// never: the reference stops at 10,000) no longer holds up other requests;
+// such centralities run one at a time, in the order their requests started.
+constexpr int64_t kLongEc = 1000;
 
 }  // namespace
 
@@ -84,6 +113,7 @@ struct bna_server {
   std::deque<Job*> queue;
   std::map<int64_t, Job*> jobs;
   int64_t next_id = 1;
+  int64_t next_seq = 0;  // start order of requests on slots
   int levels = 1;
   bool stop = false;
   std::vector<Slot*> slots;
@@ -101,13 +131,15 @@ struct bna_server {
 
 namespace {
 
-// Grow-only slot buffer, stream-ordered (no wait for other slots' work).
-int32_t grow(void** p, size_t* cap, size_t bytes, cudaStream_t st) {
+// Grow-only slot buffer, stream-ordered (no wait for other slots' work), from
+// the library's pool.
+int32_t grow(int device, void** p, size_t* cap, size_t bytes, cudaStream_t st) {
   if (*cap >= bytes) return BNA_OK;
   if (*p) cudaFreeAsync(*p, st);
   *p = nullptr;
   *cap = 0;
-  if (cudaMallocAsync(p, bytes, st) != cudaSuccess) {
+  cudaMemPool_t pool = bna::lib_pool(device);
+  if (!pool || cudaMallocFromPoolAsync(p, bytes, pool, st) != cudaSuccess) {
     cudaGetLastError();
     return BNA_OOM;
   }
@@ -119,14 +151,55 @@ int64_t slot_bytes(const Slot* s) {
   return bna_ctx_arena_bytes(s->ctx) + (int64_t)s->bold_cap + (int64_t)s->ec_cap;
 }
 
+// The slot is idle: every stream it used was synchronised at the end of its
+// last request.
 void release_slot_memory(Slot* s) {
-  bna_ctx_trim(s->ctx);
   if (s->bold) cudaFreeAsync(s->bold, s->stream[0]);
   if (s->ec) cudaFreeAsync(s->ec, s->stream[0]);
   cudaStreamSynchronize(s->stream[0]);
+  bna_ctx_trim_idle(s->ctx);
   s->bold = nullptr;
   s->ec = nullptr;
   s->bold_cap = s->ec_cap = 0;
+}
+
+bool long_ec(const Slot* s) { return s->phase == BNA_PHASE_EC && s->progress >= kLongEc; }
+
+// Launch gate of a slot's context (bna_ctx_set_gate).
+void slot_gate(void* user, void* stream, int32_t phase, int64_t done) {
+  Slot* s = static_cast<Slot*>(user);
+  bna_server* srv = s->srv;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  std::unique_lock<std::mutex> lk(srv->mu);
+  s->phase = phase;
+  s->progress = done;
+  lk.unlock();
+  if (s->level > 0) {
+    // queue depth: the launch before the previous one has finished
+    cudaEventRecord(s->fence[s->nfence & 1], st);
+    if (s->nfence > 0) cudaEventSynchronize(s->fence[(s->nfence + 1) & 1]);
+    ++s->nfence;
+  }
+  lk.lock();
+  const bool mine_long = long_ec(s);
+  auto higher = [&]() {
+    for (const Slot* o : srv->slots) {
+      if (o == s || !o->busy) continue;
+      if (long_ec(o)) {
+        if (mine_long && o->seq < s->seq) return true;
+      } else if (o->work < s->work || (o->work == s->work && o->seq < s->seq)) {
+        return true;
+      }
+    }
+    return false;
+  };
+  if (!higher()) return;
+  lk.unlock();
+  cudaStreamSynchronize(st);  // nothing of this request stays queued
+  lk.lock();
+  const auto until = Clock::now() + std::chrono::milliseconds(kGateWaitMs);
+  while (higher() && srv->cv.wait_until(lk, until) != std::cv_status::timeout) {
+  }
 }
 
 // One request on one slot.
@@ -135,7 +208,7 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
   bna_reply& out = j->reply;
   cudaStream_t st = s->stream[level_of(j->work, srv->levels)];
   const size_t bytes = (size_t)r.N * r.T * sizeof(float);
-  int32_t rc = grow(reinterpret_cast<void**>(&s->bold), &s->bold_cap, bytes, st);
+  int32_t rc = grow(srv->device, reinterpret_cast<void**>(&s->bold), &s->bold_cap, bytes, st);
   if (rc == BNA_OK && cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) !=
                           cudaSuccess)
     rc = BNA_CUDA_ERROR;
@@ -144,7 +217,9 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
     // no CSR larger than the caller's buffers is built (a cap of 0 admits
     // only the empty graph)
     bna_ctx_set_option(s->ctx, BNA_OPT_MAX_NNZ, r.cap > 0 ? r.cap : 1);
+    bna_ctx_set_option(s->ctx, BNA_OPT_TILES_PER_LAUNCH, tiles_per_launch(r.T));
     rc = bna_corr_csr(s->ctx, s->bold, r.N, r.T, &r.opts, &csr, &out.stats, st);
+    out.t_corr = srv->now();
     out.nnz = rc == BNA_OK || rc == BNA_CAPACITY ? out.stats.nnz : 0;
     if (rc == BNA_OK && csr.nnz > r.cap) rc = BNA_CAPACITY;
   }
@@ -161,7 +236,8 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
     if (!ok) rc = BNA_CUDA_ERROR;
   }
   if (rc == BNA_OK && r.ec_max_iter > 0) {
-    rc = grow(reinterpret_cast<void**>(&s->ec), &s->ec_cap, (size_t)r.N * sizeof(double), st);
+    rc = grow(srv->device, reinterpret_cast<void**>(&s->ec), &s->ec_cap, (size_t)r.N * sizeof(double),
+              st);
     if (rc == BNA_OK) {
       double lam = 0;
       int32_t it = 0;
@@ -228,6 +304,12 @@ void worker(bna_server* srv, Slot* s) {
       continue;
     }
     s->busy = true;
+    s->level = level_of(j->work, srv->levels);
+    s->work = j->work;
+    s->seq = srv->next_seq++;
+    s->phase = BNA_PHASE_CORR;
+    s->progress = 0;
+    s->nfence = 0;
     s->held = std::max(s->held, j->est);
     j->reply.t_start = srv->now();
     j->reply.slot = s->index;
@@ -268,19 +350,26 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
   int32_t rc = BNA_OK;
   for (int i = 0; i < slots && rc == BNA_OK; ++i) {
     Slot* s = new Slot();
+    s->srv = srv;
     s->index = i;
     srv->slots.push_back(s);
     rc = bna_ctx_create(device, &s->ctx);
+    for (auto& e : s->fence)
+      if (rc == BNA_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        rc = BNA_CUDA_ERROR;
+    if (rc == BNA_OK) rc = bna_ctx_set_gate(s->ctx, slot_gate, s);
     for (int l = 0; l < srv->levels && rc == BNA_OK; ++l)
       if (cudaStreamCreateWithPriority(&s->stream[l], cudaStreamNonBlocking, greatest + l) !=
           cudaSuccess)
         rc = BNA_CUDA_ERROR;
-    if (rc == BNA_OK) rc = bna_ctx_set_option(s->ctx, BNA_OPT_TILES_PER_LAUNCH, kTilesPerLaunch);
+
   }
   if (rc != BNA_OK) {
     for (Slot* s : srv->slots) {
       for (cudaStream_t& q : s->stream)
         if (q) cudaStreamDestroy(q);
+      for (cudaEvent_t e : s->fence)
+        if (e) cudaEventDestroy(e);
       if (s->ctx) bna_ctx_destroy(s->ctx);
       delete s;
     }
@@ -360,6 +449,8 @@ int32_t bna_server_destroy(bna_server* srv) {
     release_slot_memory(s);
     for (cudaStream_t& q : s->stream)
       if (q) cudaStreamDestroy(q);
+    for (cudaEvent_t e : s->fence)
+      if (e) cudaEventDestroy(e);
     bna_ctx_destroy(s->ctx);
     delete s;
   }

@@ -129,9 +129,31 @@ int64_t bna_ctx_arena_bytes(const bna_ctx* ctx);
  *     between them;
  *   BNA_OPT_MAX_NNZ: bna_corr_csr returns BNA_CAPACITY (stats->nnz = the
  *     required size) instead of building a CSR with more entries (0 = no
- *     limit). */
-typedef enum bna_option { BNA_OPT_TILES_PER_LAUNCH = 0, BNA_OPT_MAX_NNZ = 1 } bna_option;
+ *     limit);
+ *   BNA_OPT_EC_ITERS_PER_LAUNCH: power iterations per centrality launch or
+ *     graph replay, rounded up to even for replays (0 = automatic: the whole
+ *     iteration for small graphs and 32 per replay for larger ones; with a
+ *     launch gate, about a millisecond of iterations). */
+typedef enum bna_option {
+  BNA_OPT_TILES_PER_LAUNCH = 0,
+  BNA_OPT_MAX_NNZ = 1,
+  BNA_OPT_EC_ITERS_PER_LAUNCH = 2
+} bna_option;
 int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value);
+
+/* Launch gate (no reference counterpart).  Long passes call gate(user,
+ * stream, phase, done) on the calling thread between their launches: before
+ * each correlation launch after the first (BNA_PHASE_CORR, done = tiles
+ * launched), before each fill chunk after the first (BNA_PHASE_FILL, done =
+ * row blocks filled) and before each centrality launch or graph replay after
+ * the first (BNA_PHASE_EC, done = iterations completed).  With a gate set,
+ * the fill runs in row-block chunks and a centrality launch or replay holds
+ * about a millisecond of iterations.  The gate may block, e.g. to keep a large
+ * request from queueing work while a smaller one runs (the server's use).
+ * NULL removes it. */
+typedef enum bna_phase { BNA_PHASE_CORR = 0, BNA_PHASE_FILL = 1, BNA_PHASE_EC = 2 } bna_phase;
+typedef void (*bna_gate_fn)(void* user, void* stream, int32_t phase, int64_t done);
+int32_t bna_ctx_set_gate(bna_ctx* ctx, bna_gate_fn gate, void* user);
 
 /* Autotuner (no reference counterpart).  The two tensor-core forms differ in
  * their tile shape along K (64 BF16 values x 3 products vs 32 TF32 values x 1
@@ -336,6 +358,7 @@ typedef struct bna_reply {
   int32_t ec_iters;
   int32_t ec_converged;
   double t_submit, t_start, t_done; /* seconds since the server was created */
+  double t_corr;          /* the CSR was built (seconds since the server was created) */
   bna_corr_stats stats;
 } bna_reply;
 int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_bytes,

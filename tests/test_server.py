@@ -108,3 +108,41 @@ def test_tiles_per_launch_gives_the_same_csr(builder):
         assert np.array_equal(whole.row_ptr, parts.row_ptr)
         assert np.array_equal(whole.col_idx, parts.col_idx)
         assert np.array_equal(whole.val, parts.val)
+
+
+@pytest.mark.parametrize("N", [6000, 17000])
+def test_launch_gate_is_called_and_changes_nothing(builder, N):
+    """A launch gate sees the launches of a chunked correlation pass, of the
+    chunked fill and of the centrality segments (the persistent kernel below
+    16,384 vertices, graph replays above); the CSR and the centrality equal
+    the ungated ones."""
+    import torch
+    b = torch.from_numpy(_bold(N, 240, 20, 508)).cuda()
+    whole = builder.corr_csr(b, mode="r_gt", value=0.4, precision="bf16x3")
+    ec0, lam0, it0, _ = builder.ec(whole)
+    calls = []
+    builder.set_option("tiles_per_launch", 37)
+    builder.set_option("ec_iters_per_launch", 3)
+    builder.set_gate(lambda stream, phase, done: calls.append((phase, done)))
+    try:
+        gated = builder.corr_csr(b, mode="r_gt", value=0.4, precision="bf16x3")
+        n_corr = len(calls)
+        ec1, lam1, it1, _ = builder.ec(gated)
+    finally:
+        builder.set_gate(None)
+        builder.set_option("tiles_per_launch", 0)
+        builder.set_option("ec_iters_per_launch", 0)
+    nb = (N + 127) // 128
+    ntiles = sum((nb + 1) // 2 - I // 2 for I in range(nb))
+    assert n_corr >= (ntiles + 36) // 37 - 1 + min(8, nb) - 1  # correlation + fill chunks
+    per = 3 if N <= 16384 else 4  # replays hold an even number of iterations
+    ec_calls = calls[n_corr:]
+    assert len(ec_calls) >= (it0 - 1) // per
+    assert all(p == 2 for p, _ in ec_calls) and [d for _, d in ec_calls] == sorted(
+        d for _, d in ec_calls)
+    assert {p for p, _ in calls[:n_corr]} == {0, 1}
+    w, g = whole.numpy(), gated.numpy()
+    assert np.array_equal(w.row_ptr, g.row_ptr) and np.array_equal(w.col_idx, g.col_idx)
+    assert np.array_equal(w.val, g.val)
+    assert it1 == it0 and lam1 == lam0
+    assert torch.equal(ec0, ec1)
