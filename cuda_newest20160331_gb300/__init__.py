@@ -322,6 +322,20 @@ class Builder:
                self._h)
         return out
 
+    def modularity(self, csr: CsrResult, lambda_min: float = 0.0, stream=None):
+        """Newman spectral modularity of a device CSR's binary graph ->
+        (labels int32 [n] on the device, modules, Q)."""
+        import torch
+        c = L.Csr(n=csr.n, nnz=csr.nnz, row_ptr=csr.row_ptr.data_ptr(),
+                  col_idx=csr.col_idx.data_ptr() if csr.nnz else None, val=None)
+        labels = torch.empty(csr.n, dtype=torch.int32, device=csr.row_ptr.device)
+        m = C.c_int32()
+        q = C.c_double()
+        _check(lib().bna_modularity(self._h, C.byref(c), float(lambda_min),
+                                    C.c_void_p(labels.data_ptr()), C.byref(m), C.byref(q),
+                                    self._stream(stream)), self._h)
+        return labels, int(m.value), float(q.value)
+
     def ec(self, csr: CsrResult, max_iter: int = 10000, eps: float = 1e-6, stream=None):
         """Eigenvector centrality of a device CSR -> (ec float64 [n], lambda, iters, converged)."""
         import torch

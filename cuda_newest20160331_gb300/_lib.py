@@ -103,6 +103,9 @@ SIGNATURES = {
     "bna_synth_bold": (C.c_int, [C.POINTER(SynthParams), C.c_void_p, C.c_int]),
     "bna_ctx_set_option": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64]),
     "bna_ctx_set_gate": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bna_modularity": (C.c_int32, [C.c_void_p, C.POINTER(Csr), C.c_double, C.c_void_p,
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p]),
+    "bna_modu_write": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32]),
     "bna_server_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
     "bna_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "bna_server_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(Reply)]),

@@ -31,6 +31,29 @@ cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* r
                             long long* pre, long long* bsum, long long* total, int32_t* row_ptr,
                             uint32_t* err, cudaStream_t stream);
 size_t ec_state_bytes();
+size_t mod_state_bytes();
+void mod_state_read(const void* h, long long* numg, long long* kg, int* iter, int* done,
+                    double* lambda, long long* subp, long long* subn, long long* same);
+int mod_grid_blocks(int sms);
+cudaError_t launch_mod_round(int n, const int32_t* label, int round, const int32_t* rp,
+                             uint8_t* g, void* st, int sms, cudaStream_t s);
+cudaError_t launch_mod_sumbg(int n, const int32_t* rp, const int32_t* ci, const uint8_t* g,
+                             long long M, const void* st, double* sumbg, int sms, cudaStream_t s);
+cudaError_t launch_mod_init(int n, const uint8_t* g, const int32_t* rp, double* v, double* parts,
+                            void* st, double beta, int max_iter, double eps, int sms,
+                            cudaStream_t s);
+cudaError_t launch_mod_step(int n, long long M, const int32_t* rp, const int32_t* ci,
+                            const uint8_t* g, const double* sumbg, const double* v0, double* y,
+                            double* v, double* parts, void* st, int sms, cudaStream_t s);
+cudaError_t launch_mod_final(int n, const uint8_t* g, const double* v, const double* v0, void* st,
+                             cudaStream_t s);
+cudaError_t launch_mod_assign(int n, const uint8_t* g, const double* v, int maxres,
+                              long long subp, long long subn, int32_t* label, int sms,
+                              cudaStream_t s);
+cudaError_t launch_mod_q(int n, const int32_t* rp, const int32_t* ci, const int32_t* label,
+                         long long* kmod, void* st, int sms, cudaStream_t s);
+cudaError_t launch_mod_map(int n, const int32_t* label, const int32_t* adj, int32_t* out,
+                           int sms, cudaStream_t s);
 cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
                            int max_iter, cudaStream_t stream);
 cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const float* val,
@@ -106,7 +129,9 @@ enum Slot {
   S_TILES_SMP, S_DSTATE, S_DHIST, S_DCLS, S_DEIDX, S_DEXACT, S_CANDAPX, S_DTIES,
   S_RT_KEEP, S_RT_VALX, S_RT_ROWPTR, S_RT_COL, S_RT_VAL,
   S_AVG_Z, S_AVG_BAD, S_AVG_PACKED, S_AVG_UNC, S_AVG_BADZ, S_AVG_SUBJ,
-  S_BATCH_SUBJ, S_BATCH_TILES, S_COUNT
+  S_BATCH_SUBJ, S_BATCH_TILES,
+  S_MOD_LABEL, S_MOD_G, S_MOD_SUMBG, S_MOD_V, S_MOD_Y, S_MOD_PARTS, S_MOD_STATE, S_MOD_KMOD,
+  S_MOD_ADJ, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -117,6 +142,14 @@ struct DevStatus {
   unsigned long long stats[4];
   long long total;
   unsigned long long epool;  // edge-list entries handed out by the count pass
+};
+
+// Captured power steps of the modularity driver (reused across its rounds).
+struct ModGraph {
+  cudaGraphExec_t exec = nullptr;
+  const void* key[8] = {};
+  int n = 0;
+  long long M = 0;
 };
 
 struct EcGraph {
@@ -150,6 +183,7 @@ struct bna_ctx {
   long long cand_cap = 1 << 20;
   long long elist_cap = 1LL << 23;  // edge-list pool entries (grows on demand)
   EcGraph ecg;
+  ModGraph modg;
   int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
   int ntiles = 0;
   int ntiles_smp = 0;  // sampled tile list (density histogram), same block count
@@ -589,6 +623,8 @@ static void arena_release(bna_ctx* ctx, cudaStream_t st, bool to_driver) {
   ctx->last_ok = false;
   if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
   ctx->ecg = EcGraph();
+  if (ctx->modg.exec) cudaGraphExecDestroy(ctx->modg.exec);
+  ctx->modg = ModGraph();
 }
 
 // Trim of a context whose every call has been synchronised (a server slot
@@ -1973,6 +2009,155 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
   if (iters) *iters = it;
   const bool converged = (e1 <= eps || e2 <= eps);
   return converged ? BNA_OK : BNA_NOT_CONVERGED;
+}
+
+// ---------------------------------------------------------------- modularity
+
+// Power steps replayed per graph launch (an even number: step t reads
+// buffer t & 1 and writes the other).
+constexpr int kModGraphSteps = 32;
+
+int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr, double lambda_min, int32_t* labels_dev,
+                       int32_t* modules, double* q, void* stream) {
+  if (!ctx || !csr || !labels_dev || !modules || !q || csr->n < 1 || !csr->row_ptr ||
+      (csr->nnz > 0 && !csr->col_idx))
+    return fail(ctx, BNA_BAD_ARG, "bna_modularity: bad arguments");
+  int32_t s = set_device(ctx, as_stream(stream));
+  if (s) return s;
+  cudaStream_t st = as_stream(stream);
+  const int n = csr->n;
+  const int32_t* rp = csr->row_ptr;
+  const int32_t* ci = csr->col_idx;
+  const double lam_min = lambda_min > 0 ? lambda_min : 0.001;  // Modularity_CPU.cpp:19
+  // M = (R[N] - R[0]) / 2 (:175)
+  int32_t ends[2];
+  CK(cudaMemcpyAsync(&ends[0], rp, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&ends[1], rp + n, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const long long M = ((long long)ends[1] - ends[0]) / 2;
+  if (M == 0) {  // no edge: one module; the reference's Q is 0 / 0
+    std::vector<int32_t> ones(n, 1);
+    CK(cudaMemcpyAsync(labels_dev, ones.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    *modules = 1;
+    *q = std::nan("");
+    return BNA_OK;
+  }
+  const int sms = ctx->sms;
+  const int grid = mod_grid_blocks(sms);
+  int32_t *label, *adj_dev;
+  uint8_t* g;
+  double *sumbg, *vb, *y, *parts;
+  long long* kmod;
+  void* state;
+  ENSURE(S_MOD_LABEL, (size_t)n * 4, label);
+  ENSURE(S_MOD_G, (size_t)n, g);
+  ENSURE(S_MOD_SUMBG, (size_t)n * 8, sumbg);
+  ENSURE(S_MOD_V, (size_t)2 * n * 8, vb);
+  ENSURE(S_MOD_Y, (size_t)n * 8, y);
+  ENSURE(S_MOD_PARTS, (size_t)grid * 3 * 8, parts);
+  ENSURE(S_MOD_STATE, mod_state_bytes(), state);
+  ENSURE(S_MOD_KMOD, (size_t)(2 * n + 2) * 8, kmod);
+  ENSURE(S_MOD_ADJ, (size_t)(2 * n + 2) * 4, adj_dev);
+  CK(cudaMemsetAsync(label, 0, (size_t)n * 4, st));
+  // the power steps, captured once per graph and buffers
+  ModGraph& mg = ctx->modg;
+  const void* key[8] = {rp, ci, g, sumbg, vb, y, parts, state};
+  bool same = mg.exec && mg.n == n && mg.M == M;
+  for (int k = 0; k < 8 && same; ++k) same = mg.key[k] == key[k];
+  if (!same) {
+    if (mg.exec) cudaGraphExecDestroy(mg.exec);
+    mg = ModGraph();
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (int t = 0; t < kModGraphSteps; ++t)
+      launch_mod_step(n, M, rp, ci, g, sumbg, vb + (size_t)(t & 1) * n, y,
+                      vb + (size_t)((t + 1) & 1) * n, parts, state, sms, cap);
+    cudaGraph_t graph;
+    cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    CK(ce);
+    ce = cudaGraphInstantiate(&mg.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ce);
+    for (int k = 0; k < 8; ++k) mg.key[k] = key[k];
+    mg.n = n;
+    mg.M = M;
+  }
+  // one power iteration (Lead_Vector): -> lambda; the final iterate's buffer
+  long long subp = 0, subn = 0;
+  int vfinal = 0;
+  auto lead_vector = [&](double beta, double* lambda) -> int32_t {
+    CK(launch_mod_init(n, g, rp, vb, parts, state, beta, 10000, 1e-6, sms, st));
+    int it = 0, done = 0;
+    for (;;) {
+      CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      mod_state_read(ctx->pinned, nullptr, nullptr, &it, &done, nullptr, nullptr, nullptr,
+                     nullptr);
+      if (done) break;
+      CK(cudaGraphLaunch(mg.exec, st));
+    }
+    vfinal = it & 1;
+    CK(launch_mod_final(n, g, vb + (size_t)vfinal * n, vb + (size_t)(vfinal ^ 1) * n, state, st));
+    CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    mod_state_read(ctx->pinned, nullptr, nullptr, nullptr, nullptr, lambda, &subp, &subn,
+                   nullptr);
+    return BNA_OK;
+  };
+  // Partition (:186-212): rounds until no label above the current round remains
+  std::vector<int32_t> adj((size_t)2 * n + 2, 0);
+  int round = 0, maxres = 0, index = 1, mods = 1;
+  while (round <= maxres) {
+    CK(launch_mod_round(n, label, round, rp, g, state, sms, st));
+    CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    long long numg = 0;
+    mod_state_read(ctx->pinned, &numg, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                   nullptr);
+    if (numg) {
+      CK(launch_mod_sumbg(n, rp, ci, g, M, state, sumbg, sms, st));
+      double lambda = 0, l2 = 0;
+      s = lead_vector(0.0, &lambda);
+      if (s) return s;
+      if (lambda < 0) {  // the leading eigenvalue of B - lambda I (:271-272)
+        s = lead_vector(-lambda, &l2);
+        if (s) return s;
+        lambda += l2;
+      }
+      const bool issub = lambda > lam_min && subp > 1 && subn > 1;
+      if (issub) {
+        CK(launch_mod_assign(n, g, vb + (size_t)vfinal * n, maxres, subp, subn, label, sms, st));
+        maxres += 2;
+      } else {
+        adj[round] = index++;
+      }
+      mods += issub ? 1 : 0;
+    }
+    ++round;
+  }
+  // Q (:215-224) from integer counts: same-module entries and module degree sums
+  CK(cudaMemsetAsync(state, 0, mod_state_bytes(), st));
+  CK(cudaMemsetAsync(kmod, 0, (size_t)(maxres + 1) * 8, st));
+  CK(launch_mod_q(n, rp, ci, label, kmod, state, sms, st));
+  std::vector<long long> kh((size_t)maxres + 1);
+  CK(cudaMemcpyAsync(kh.data(), kmod, kh.size() * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(adj_dev, adj.data(), (size_t)(maxres + 1) * 4, cudaMemcpyHostToDevice, st));
+  CK(launch_mod_map(n, label, adj_dev, labels_dev, sms, st));
+  CK(cudaStreamSynchronize(st));
+  long long same_cnt = 0;
+  mod_state_read(ctx->pinned, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                 &same_cnt);
+  double qq = (double)same_cnt;
+  for (long long kgv : kh) qq -= (double)kgv * (double)kgv / 2 / (double)M;
+  qq /= 2 * (double)M;
+  *modules = mods;
+  *q = qq;
+  ctx->klaunch = 0;
+  return BNA_OK;
 }
 
 int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr, int32_t max_iter, double eps, double* ec_dev,

@@ -91,3 +91,16 @@ extern "C" int32_t bna_ec_write(const char* path, const double* ec, int32_t N) {
   ok = (std::fclose(f) == 0) && ok;
   return ok ? BNA_OK : BNA_IO_ERROR;
 }
+
+extern "C" int32_t bna_modu_write(const char* path, const int32_t* labels, int32_t N) {
+  if (!path || (!labels && N > 0) || N < 0) return BNA_BAD_ARG;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return BNA_IO_ERROR;
+  bool ok = write_all(f, &N, 4);
+  for (int32_t i = 0; ok && i < N; ++i) {
+    const float v = (float)labels[i];
+    ok = write_all(f, &v, 4);
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? BNA_OK : BNA_IO_ERROR;
+}

@@ -311,6 +311,21 @@ int32_t bna_lead_vector(bna_ctx* ctx, const int32_t* R, const int32_t* C, const 
  * on `stream`, on the current device. */
 int32_t bna_degree(const bna_csr* csr_dev, float* deg_dev, void* stream);
 
+/* Newman spectral modularity of the binary graph of a device CSR (the
+ * reference's modularity tool, U/Newman_Modularity_CPU/Modularity_CPU/
+ * Modularity_CPU.cpp: Partition :173-240, Sub_Partition :250-300,
+ * Lead_Vector :315-377): round by round, the nodes of one module are split
+ * by the sign of the leading eigenvector of their generalised modularity
+ * matrix when its eigenvalue exceeds lambda_min (<= 0: the tool's 0.001) and
+ * both sides hold more than one node.  labels_dev (n int32, device): module
+ * of every vertex, 1-based, numbered in the order the modules stopped
+ * dividing; *modules: their count; *q: the modularity Q (NaN without edges,
+ * where the reference divides by zero).  Column order within rows is free. */
+int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr_dev, double lambda_min,
+                       int32_t* labels_dev, int32_t* modules, double* q, void* stream);
+/* _modu.nm file (Modularity_CPU.cpp:122-131): int32 N; float labels[N]. */
+int32_t bna_modu_write(const char* path, const int32_t* labels_host, int32_t N);
+
 /* .csr file (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:353-360 writer,
  * W/CUEC/weighted-net.cu:275-287 reader): int32 Rlength=N+1; int32 R[N+1];
  * int32 Clength; int32 C[Clength]; then, for a weighted graph, int32 Vlength;

@@ -4,6 +4,7 @@ ctypes access to
   liboracle.so      the C restatement of the reference's CPU arithmetic (oracle.c)
   _ref/libref_w.so  the reference's own CorMat.cpp CPU functions (development host only)
   _ref/libref_u.so  the reference's own multi-threaded CPU correlation tool
+  _ref/libref_m.so  the reference's own unweighted Newman modularity tool
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this package.
@@ -23,6 +24,7 @@ MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3}
 _o = None
 _rw = None
 _ru = None
+_rm = None
 
 
 def lib():
@@ -55,6 +57,9 @@ def lib():
         o.orc_rows_mt_f32_count.restype = C.c_int64
         o.orc_avg_accumulate.argtypes = [P, C.c_int64, C.c_int, P]
         o.orc_avg_finalize.argtypes = [P, C.c_int64, C.c_int, C.c_int]
+        o.orc_modularity.argtypes = [P, P, C.c_int, C.c_double, P, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int)]
+        o.orc_modularity.restype = C.c_int
         _o = o
     return _o
 
@@ -88,6 +93,40 @@ def ref_u():
         r.ref_u_form_csr_graph.argtypes = [P, P, P, C.c_int]
         _ru = r
     return _ru
+
+
+def ref_m():
+    """The reference's unweighted Newman modularity tool, or None when not built here."""
+    global _rm
+    if _rm is None and os.path.exists(_build.REF_M):
+        r = C.CDLL(_build.REF_M)
+        P = C.c_void_p
+        r.ref_m_partition.argtypes = [P, P, C.c_int, P]
+        r.ref_m_partition.restype = C.c_int
+        _rm = r
+    return _rm
+
+
+def modularity(R, Cc, lambda_min: float = 0.001):
+    """-> (labels int32 [N], Q, modules, rounds): the restatement of the
+    reference's spectral bisection (binary graph of R, C)."""
+    R = np.ascontiguousarray(R, np.int32)
+    Cc = np.ascontiguousarray(Cc, np.int32)
+    N = len(R) - 1
+    labels = np.empty(N, np.int32)
+    q, rounds = C.c_double(), C.c_int()
+    m = lib().orc_modularity(_p(R), _p(Cc), N, lambda_min, _p(labels), C.byref(q),
+                             C.byref(rounds))
+    return labels, q.value, m, rounds.value
+
+
+def ref_modularity(R, Cc):
+    """-> (labels int32 [N], modules) from the compiled reference tool."""
+    R = np.ascontiguousarray(R, np.int32)
+    Cc = np.ascontiguousarray(Cc, np.int32)
+    labels = np.empty(len(R) - 1, np.int32)
+    m = ref_m().ref_m_partition(_p(R), _p(Cc), len(R) - 1, _p(labels))
+    return labels, m
 
 
 def _p(a):

@@ -6,6 +6,8 @@
    there, with the Linux shim headers of refshim/:
      libref_w.so  W/CorMat/CUCorMat/CUCorMat/CorMat.cpp   + ref_glue_w.cpp
      libref_u.so  U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp + ref_glue_u.cpp
+     libref_m.so  U/Newman_Modularity_CPU/Modularity_CPU/Modularity_CPU.cpp
+                  + ref_glue_m.cpp
    Both with -ffp-contract=off so they round exactly like the reference's
    scalar code.  main() of each file is renamed and never called.
 """
@@ -21,10 +23,13 @@ W_SRC = os.path.join(REF_ROOT, "BNAPlatform-weighted-win64-cuda7.0-20160331", "s
                      "CorMat", "CUCorMat", "CUCorMat", "CorMat.cpp")
 U_SRC = os.path.join(REF_ROOT, "BNAPlatform-win64-cuda7.0-20160115", "src",
                      "CorMat", "CorMat_CPU", "CorMat", "CorMat_CPU.cpp")
+M_SRC = os.path.join(REF_ROOT, "BNAPlatform-win64-cuda7.0-20160115", "src",
+                     "Newman_Modularity_CPU", "Modularity_CPU", "Modularity_CPU.cpp")
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_W = os.path.join(REF_DIR, "libref_w.so")
 REF_U = os.path.join(REF_DIR, "libref_u.so")
+REF_M = os.path.join(REF_DIR, "libref_m.so")
 
 
 def _run(cmd, verbose):
@@ -55,6 +60,10 @@ def build(verbose: bool = False) -> None:
             _run(common + [W_SRC, gw, "-o", REF_W], verbose)
         if _stale(REF_U, [U_SRC, gu]):
             _run(common + [U_SRC, gu, "-o", REF_U], verbose)
+        gm = os.path.join(HERE, "ref_glue_m.cpp")
+        if os.path.exists(M_SRC) and _stale(REF_M, [M_SRC, gm, __file__]):
+            # -Bsymbolic: the tool's global `verr` must not bind to libc's verr()
+            _run(common + ["-Wl,-Bsymbolic", M_SRC, gm, "-o", REF_M], verbose)
 
 
 if __name__ == "__main__":

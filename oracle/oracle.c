@@ -444,3 +444,122 @@ void orc_avg_finalize(float* acc, long long m, int nsub, int fisher) {
     if (fisher) acc[i] = orc_fisher_r(acc[i]);
   }
 }
+
+/* ---- Newman spectral modularity (unweighted), restating the reference CPU
+ * tool U/Newman_Modularity_CPU/Modularity_CPU/Modularity_CPU.cpp (the
+ * 20160115 tree): Partition (:186-240), Sub_Partition (:252-300),
+ * Lead_Vector (:315-377), VectorNorm (:383-389).  The graph is the binary
+ * CSR (R, C); M = R[N] / 2.  Labels out: 1-based module per node, in the
+ * order the rounds stopped dividing.  Returns the number of modules. */
+static double mod_norm(const double* x, const unsigned char* g, int N) {
+  double s = 0;
+  for (int i = 0; i < N; ++i) s += g[i] ? x[i] * x[i] : 0;
+  return sqrt(s);
+}
+
+static double mod_lead_vector(const int32_t* R, const int32_t* C, int N, long long M,
+                              const double* sumbg, const unsigned char* g, double beta, double* v,
+                              double* v0, double* verr, int* iters) {
+  for (int i = 0; i < N; ++i) v[i] = g[i] ? (double)i : 0;  /* :322-324 */
+  double err1 = 1, err2 = 1, vnorm = 0;
+  int it = 0;
+  while (err1 > 1e-6 && err2 > 1e-6 && it < 10000) {
+    for (int i = 0; i < N; ++i) v0[i] = g[i] ? v[i] : 0;
+    double vk = 0;
+    for (int i = 0; i < N; ++i) vk += g[i] ? v0[i] * (double)(R[i + 1] - R[i]) : 0;
+    for (int i = 0; i < N; ++i) {
+      if (!g[i]) continue;
+      double t = 0;
+      for (int32_t j = R[i]; j < R[i + 1]; ++j) t += g[C[j]] ? v0[C[j]] : 0;
+      t -= vk / 2 / (double)M * (double)(R[i + 1] - R[i]) + (sumbg[i] - beta) * v0[i];
+      v[i] = t;
+    }
+    vnorm = mod_norm(v, g, N);
+    for (int i = 0; i < N; ++i) v[i] = g[i] ? (v[i] / vnorm) : 0;
+    for (int i = 0; i < N; ++i) verr[i] = g[i] ? (v[i] - v0[i]) : 0;
+    err1 = mod_norm(verr, g, N);
+    for (int i = 0; i < N; ++i) verr[i] = v[i] + v0[i];
+    err2 = mod_norm(verr, g, N);
+    ++it;
+  }
+  *iters = it;
+  int mi = 0; /* :370-374 */
+  v[0] = g[0] ? v[0] : 0;
+  for (int i = 0; i < N; ++i)
+    if (g[i] && fabs(v[i]) > fabs(v[mi])) mi = i;
+  return (v[mi] * v0[mi] > 0) ? vnorm : -vnorm;
+}
+
+int orc_modularity(const int32_t* R, const int32_t* C, int N, double lambda_min, int32_t* labels,
+                   double* q_out, int* rounds_out) {
+  const long long M = (R[N] - R[0]) / 2;
+  if (M == 0) { /* no edge: the reference divides by M = 0; one module, Q undefined */
+    for (int i = 0; i < N; ++i) labels[i] = 1;
+    *q_out = NAN;
+    if (rounds_out) *rounds_out = 1;
+    return 1;
+  }
+  int* res = (int*)calloc((size_t)N, sizeof(int));
+  int* adj = (int*)malloc(sizeof(int) * (size_t)(2 * N + 2));
+  unsigned char* g = (unsigned char*)malloc((size_t)N);
+  double* v = (double*)malloc(sizeof(double) * (size_t)N);
+  double* v0 = (double*)malloc(sizeof(double) * (size_t)N);
+  double* verr = (double*)malloc(sizeof(double) * (size_t)N);
+  double* sumbg = (double*)malloc(sizeof(double) * (size_t)N);
+  int round = 0, max_result = 0, index = 1, modules = 1;
+  while (round <= max_result) {
+    int numg = 0;
+    for (int i = 0; i < N; ++i) {
+      g[i] = res[i] == round;
+      numg += g[i];
+    }
+    if (numg) {
+      /* Sub_Partition: sumBG in integer arithmetic (:258-266) */
+      long long kg = 0;
+      for (int j = 0; j < N; ++j) kg += (long long)(R[j + 1] - R[j]) * g[j];
+      for (int i = 0; i < N; ++i) {
+        if (!g[i]) continue;
+        long long in = 0;
+        for (int32_t j = R[i]; j < R[i + 1]; ++j) in += g[C[j]];
+        sumbg[i] = (double)(in - (long long)(R[i + 1] - R[i]) * kg / 2 / M);
+      }
+      int it;
+      double lambda = mod_lead_vector(R, C, N, M, sumbg, g, 0.0, v, v0, verr, &it);
+      if (lambda < 0) lambda += mod_lead_vector(R, C, N, M, sumbg, g, -lambda, v, v0, verr, &it);
+      long long subn = 0, subp = 0;
+      for (int i = 0; i < N; ++i) {
+        subp += g[i] && v[i] > 0;
+        subn += g[i] && v[i] <= 0;
+      }
+      const int issub = lambda > lambda_min && subp > 1 && subn > 1;
+      if (issub) {
+        for (int i = 0; i < N; ++i)
+          if (g[i]) res[i] = max_result + 1 + (v[i] * ((double)(subp - subn) + 0.5) <= 0);
+        max_result += 2;
+      } else {
+        adj[round] = index++;
+      }
+      modules += issub;
+    }
+    ++round;
+  }
+  /* Q (:215-224) */
+  double q = 0;
+  for (int i = 0; i < N; ++i)
+    for (int32_t j = R[i]; j < R[i + 1]; ++j) q += 1.0 * (res[i] == res[C[j]]);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      q -= 1.0 * (res[i] == res[j]) * (R[i + 1] - R[i]) * (R[j + 1] - R[j]) / 2 / M;
+  q /= 2 * M;
+  for (int i = 0; i < N; ++i) labels[i] = adj[res[i]];
+  *q_out = q;
+  if (rounds_out) *rounds_out = round;
+  free(res);
+  free(adj);
+  free(g);
+  free(v);
+  free(v0);
+  free(verr);
+  free(sumbg);
+  return modules;
+}

@@ -334,6 +334,49 @@ def test_ec_matches_oracle(builder):
         assert np.max(np.abs(ec.cpu().numpy() - ec_o)) <= 1e-5 * np.max(np.abs(ec_o))
 
 
+def _random_graph(n, deg, seed):
+    """Symmetric random graph, columns ascending per row, values in (0, 1)."""
+    rng = np.random.default_rng(seed)
+    i = rng.integers(0, n, n * deg // 2)
+    j = rng.integers(0, n, n * deg // 2)
+    keep = i != j
+    i, j = i[keep], j[keep]
+    w = rng.uniform(0.05, 1.0, len(i)).astype(np.float32)
+    rows = np.concatenate([i, j])
+    cols = np.concatenate([j, i])
+    vals = np.concatenate([w, w])
+    key = rows.astype(np.int64) * n + cols
+    key, first = np.unique(key, return_index=True)
+    rows, cols, vals = (key // n).astype(np.int32), (key % n).astype(np.int32), vals[first]
+    R = np.zeros(n + 1, np.int32)
+    np.add.at(R, rows + 1, 1)
+    return np.cumsum(R).astype(np.int32), cols, vals
+
+
+@pytest.mark.parametrize("unsorted", [False, True])
+def test_ec_large_graph_matches_oracle(builder, unsorted):
+    """Graphs above the persistent kernel's size (per-iteration launches
+    replayed from a graph), with columns ascending or not within a row: same
+    iterations and values as the FP64 oracle."""
+    R, C, V = _random_graph(60000, 40, 91)
+    if unsorted:
+        r = 777
+        C[R[r]:R[r + 1]] = C[R[r]:R[r + 1]][::-1].copy()
+        V[R[r]:R[r + 1]] = V[R[r]:R[r + 1]][::-1].copy()
+    ec_o, lam_o, it_o, conv_o = oracle.ec(R, C, V.astype(np.float64))
+    csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), dev(V), {})
+    ec, lam, it, conv = builder.ec(csr)
+    ec = ec.cpu().numpy()
+    assert conv == conv_o and it == it_o, (it, it_o)
+    assert np.max(np.abs(ec - ec_o)) <= 1e-9 * np.max(np.abs(ec_o))
+    assert abs(lam - lam_o) <= 1e-9 * abs(lam_o)
+    ec_o, lam_o, it_o, _ = oracle.ec(R, C)
+    csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), None, {})
+    ec, lam, it, _ = builder.ec(csr)
+    assert it == it_o
+    assert np.max(np.abs(ec.cpu().numpy() - ec_o)) <= 1e-9 * np.max(np.abs(ec_o))
+
+
 def test_lead_vector_known_answer_4node(builder):
     R = np.array([0, 2, 3, 6, 8], np.int32)
     C = np.array([2, 3, 2, 0, 1, 3, 0, 2], np.int32)
@@ -490,3 +533,43 @@ def test_autotune_picks_a_form_and_auto_resolves(builder, tmp_path, monkeypatch)
         assert len([x for x in lines if x.strip()]) == 1
     finally:
         t2.close()
+
+
+MOD_CASES = ["planted60", "planted300", "planted1000", "noisy500", "cliques", "small_c1"]
+
+
+@pytest.mark.parametrize("name", MOD_CASES)
+def test_modularity_matches_reference_golden(builder, name):
+    """Newman spectral modularity on the device: the reference tool's modules
+    (labels from its own compiled code), Q as the oracle computes it."""
+    g = np.load(os.path.join(GOLD, "modularity_ref.npz"))
+    if name == "small_c1":
+        ref = np.load(os.path.join(GOLD, "ref_cases.npz"))
+        R, C = ref["small_c1_R"], ref["small_c1_C"]
+    else:
+        R, C = g[name + "_R"], g[name + "_C"]
+    csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), None, {})
+    labels, m, q = builder.modularity(csr)
+    assert m == int(g[name + "_modules"])
+    assert np.array_equal(labels.cpu().numpy(), g[name + "_labels"])
+    _, q_o, _, _ = oracle.modularity(R, C)
+    assert abs(q - q_o) <= 1e-9 * abs(q_o)
+
+
+def test_modularity_of_a_correlation_network(builder):
+    """The modules of a thresholded correlation CSR (values ignored, as the
+    reference tool reads only R and C) equal the oracle's."""
+    b = bna.synth_bold(6000, 240, 12, 41)
+    res = builder.corr_csr(dev(b), mode="r_gt", value=0.45, precision="bf16x3")
+    h = res.numpy()
+    labels, m, q = builder.modularity(res)
+    lab_o, q_o, m_o, _ = oracle.modularity(h.row_ptr, h.col_idx)
+    assert m == m_o and np.array_equal(labels.cpu().numpy(), lab_o)
+    assert abs(q - q_o) <= 1e-9 * abs(q_o)
+
+
+def test_modularity_without_edges(builder):
+    R = np.zeros(7, np.int32)
+    csr = bna.CsrResult(6, 0, dev(R), dev(np.zeros(1, np.int32)), None, {})
+    labels, m, q = builder.modularity(csr)
+    assert m == 1 and np.all(labels.cpu().numpy() == 1) and np.isnan(q)

@@ -183,3 +183,57 @@ def test_avg_accumulation_matches_reference_post_block(fisher):
         clamp = np.where((P >= -1) & (P <= 1), P, np.float32(0)).astype(np.float32)
         oracle.lib().orc_avg_accumulate(clamp.ctypes.data, m, fisher, acc_orc.ctypes.data)
     assert np.array_equal(acc_ref, acc_orc)
+
+
+MOD_CASES = ["planted60", "planted300", "planted1000", "noisy500", "cliques", "small_c1"]
+
+
+def _mod_graph(name):
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "modularity_ref.npz"))
+    if name == "small_c1":
+        ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_cases.npz"))
+        return ref["small_c1_R"], ref["small_c1_C"], g
+    return g[name + "_R"], g[name + "_C"], g
+
+
+@pytest.mark.parametrize("name", MOD_CASES)
+def test_modularity_oracle_matches_reference_labels(name):
+    """The restated spectral bisection gives the reference tool's modules
+    (labels recorded from its own compiled code)."""
+    R, C, g = _mod_graph(name)
+    labels, q, m, _ = oracle.modularity(R, C)
+    assert m == int(g[name + "_modules"])
+    assert np.array_equal(labels, g[name + "_labels"])
+    assert 0.0 < q < 1.0
+
+
+def test_modularity_known_answer_two_cliques():
+    """Two 5-cliques joined by one edge: split into the cliques, Q = 2 (10/21 - 1/4)."""
+    R, C, _ = _mod_graph("cliques")
+    labels, q, m, _ = oracle.modularity(R, C)
+    assert m == 2 and len(set(labels[:5])) == 1 and len(set(labels[5:])) == 1
+    assert labels[0] != labels[5]
+    assert abs(q - 2 * (10 / 21 - 0.25)) < 1e-12
+
+
+def test_modularity_oracle_against_compiled_reference_random():
+    if oracle.ref_m() is None:
+        pytest.skip("reference tree not present on this host")
+    rng = np.random.default_rng(17)
+    for _ in range(3):
+        n = int(rng.integers(20, 400))
+        p = float(rng.uniform(0.02, 0.2))
+        up = np.triu(rng.random((n, n)) < p, 1)
+        adj = up | up.T
+        R = np.concatenate([[0], np.cumsum(adj.sum(1))]).astype(np.int32)
+        C = np.nonzero(adj)[1].astype(np.int32)
+        if len(C) == 0:
+            continue
+        lab_r, m_r = oracle.ref_modularity(R, C)
+        lab_o, _, m_o, _ = oracle.modularity(R, C)
+        assert m_r == m_o and np.array_equal(lab_r, lab_o)
+
+
+def test_modularity_without_edges_is_one_module():
+    labels, q, m, _ = oracle.modularity(np.zeros(5, np.int32), np.zeros(0, np.int32))
+    assert m == 1 and np.all(labels == 1) and np.isnan(q)
