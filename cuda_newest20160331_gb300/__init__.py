@@ -322,18 +322,29 @@ class Builder:
                self._h)
         return out
 
-    def modularity(self, csr: CsrResult, lambda_min: float = 0.0, stream=None):
+    def modularity(self, csr: CsrResult, lambda_min: float = 0.0, stream=None,
+                   log: list | None = None):
         """Newman spectral modularity of a device CSR's binary graph ->
-        (labels int32 [n] on the device, modules, Q)."""
+        (labels int32 [n] on the device, modules, Q).  With `log` (a list),
+        one dict per round that held nodes is appended: round, nodes, iters
+        (per Lead_Vector call), residual, lambda, divided."""
         import torch
         c = L.Csr(n=csr.n, nnz=csr.nnz, row_ptr=csr.row_ptr.data_ptr(),
                   col_idx=csr.col_idx.data_ptr() if csr.nnz else None, val=None)
         labels = torch.empty(csr.n, dtype=torch.int32, device=csr.row_ptr.device)
         m = C.c_int32()
         q = C.c_double()
+        cap = 0 if log is None else 2 * csr.n + 2
+        recs = (L.ModRound * max(cap, 1))()
+        nrec = C.c_int32()
         _check(lib().bna_modularity(self._h, C.byref(c), float(lambda_min),
                                     C.c_void_p(labels.data_ptr()), C.byref(m), C.byref(q),
-                                    self._stream(stream)), self._h)
+                                    recs, cap, C.byref(nrec), self._stream(stream)), self._h)
+        if log is not None:
+            for r in recs[:min(nrec.value, cap)]:
+                log.append({"round": r.round, "nodes": r.nodes, "iters": list(r.iters),
+                            "residual": list(r.residual), "lambda": r.lambda_,
+                            "divided": bool(r.divided)})
         return labels, int(m.value), float(q.value)
 
     def ec(self, csr: CsrResult, max_iter: int = 10000, eps: float = 1e-6, stream=None):

@@ -27,6 +27,12 @@ class Csr(C.Structure):
                 ("col_idx", C.c_void_p), ("val", C.c_void_p)]
 
 
+class ModRound(C.Structure):
+    _fields_ = [("round", C.c_int32), ("nodes", C.c_int32), ("iters", C.c_int32 * 2),
+                ("residual", C.c_double * 2), ("lambda_", C.c_double), ("divided", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class CorrOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("precision", C.c_int32), ("value", C.c_double),
                 ("weighted", C.c_int32), ("delta", C.c_double), ("reserved", C.c_int32 * 8)]
@@ -104,7 +110,9 @@ SIGNATURES = {
     "bna_ctx_set_option": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64]),
     "bna_ctx_set_gate": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "bna_modularity": (C.c_int32, [C.c_void_p, C.POINTER(Csr), C.c_double, C.c_void_p,
-                                   C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_void_p]),
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                   C.POINTER(ModRound), C.c_int32, C.POINTER(C.c_int32),
+                                   C.c_void_p]),
     "bna_modu_write": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32]),
     "bna_server_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
     "bna_server_submit": (C.c_int32, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),

@@ -31,27 +31,30 @@ cudaError_t launch_csr_scan(int32_t* seg, int nb, int n_pad, int n, long long* r
                             long long* pre, long long* bsum, long long* total, int32_t* row_ptr,
                             uint32_t* err, cudaStream_t stream);
 size_t ec_state_bytes();
-size_t mod_state_bytes();
-void mod_state_read(const void* h, long long* numg, long long* kg, int* iter, int* done,
-                    double* lambda, long long* subp, long long* subn, long long* same);
-int mod_grid_blocks(int sms);
-cudaError_t launch_mod_round(int n, const int32_t* label, int round, const int32_t* rp,
-                             uint8_t* g, void* st, int sms, cudaStream_t s);
-cudaError_t launch_mod_sumbg(int n, const int32_t* rp, const int32_t* ci, const uint8_t* g,
-                             long long M, const void* st, double* sumbg, int sms, cudaStream_t s);
-cudaError_t launch_mod_init(int n, const uint8_t* g, const int32_t* rp, double* v, double* parts,
-                            void* st, double beta, int max_iter, double eps, int sms,
-                            cudaStream_t s);
-cudaError_t launch_mod_step(int n, long long M, const int32_t* rp, const int32_t* ci,
-                            const uint8_t* g, const double* sumbg, const double* v0, double* y,
-                            double* v, double* parts, void* st, int sms, cudaStream_t s);
-cudaError_t launch_mod_final(int n, const uint8_t* g, const double* v, const double* v0, void* st,
-                             cudaStream_t s);
-cudaError_t launch_mod_assign(int n, const uint8_t* g, const double* v, int maxres,
-                              long long subp, long long subn, int32_t* label, int sms,
-                              cudaStream_t s);
+size_t mod_group_bytes();
+size_t mod_assign_bytes();
+int mod_parts_per_block();
+int mod_level_grid(int sms, size_t smem);
+int mod_stage_max();
+int mod_smem_max();
+void mod_group_set(void* rec, int label, int row_off, int rows, int blk0, int nblk, long long kg);
+void mod_group_get(const void* rec, int* err, int iters[2], double resid[2], double* lambda,
+                   long long* subp, long long* subn, int* fbuf);
+void mod_assign_set(void* rec, int row_off, int rows, int fbuf, int base, double w);
+cudaError_t launch_mod_build(int nrows, const int32_t* rows, const int32_t* rp,
+                             const int32_t* ci, const int32_t* label, const int32_t* loc,
+                             int32_t* cnt, int32_t* lrp, int32_t* lci, int sms, cudaStream_t s);
+cudaError_t launch_mod_level(int n, long long M, const int32_t* rp, const int32_t* label,
+                             const int32_t* rows, const int32_t* lrp, const int32_t* lci,
+                             void* groups, const int32_t* blk_grp, double* vd, float2* vf,
+                             float2* rs, double* y, double* parts, int nrows, int stage_max,
+                             int stage_bytes, int ecap, int e16, size_t smem, int grid,
+                             int max_iter, double eps, cudaStream_t s);
+cudaError_t launch_mod_assign(int nrows, const int32_t* rows, const void* as, int nas,
+                              const double* vd, int32_t* label, cudaStream_t s);
 cudaError_t launch_mod_q(int n, const int32_t* rp, const int32_t* ci, const int32_t* label,
-                         long long* kmod, void* st, int sms, cudaStream_t s);
+                         unsigned long long* kmod, unsigned long long* same, int sms,
+                         cudaStream_t s);
 cudaError_t launch_mod_map(int n, const int32_t* label, const int32_t* adj, int32_t* out,
                            int sms, cudaStream_t s);
 cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
@@ -130,7 +133,8 @@ enum Slot {
   S_RT_KEEP, S_RT_VALX, S_RT_ROWPTR, S_RT_COL, S_RT_VAL,
   S_AVG_Z, S_AVG_BAD, S_AVG_PACKED, S_AVG_UNC, S_AVG_BADZ, S_AVG_SUBJ,
   S_BATCH_SUBJ, S_BATCH_TILES,
-  S_MOD_LABEL, S_MOD_G, S_MOD_SUMBG, S_MOD_V, S_MOD_Y, S_MOD_PARTS, S_MOD_STATE, S_MOD_KMOD,
+  S_MOD_LABEL, S_MOD_ROWS, S_MOD_LOC, S_MOD_CNT, S_MOD_LRP, S_MOD_LCI, S_MOD_VD, S_MOD_VF,
+  S_MOD_RS, S_MOD_Y, S_MOD_PARTS, S_MOD_GROUPS, S_MOD_BLKGRP, S_MOD_ASSIGN, S_MOD_KMOD,
   S_MOD_ADJ, S_COUNT
 };
 
@@ -142,14 +146,6 @@ struct DevStatus {
   unsigned long long stats[4];
   long long total;
   unsigned long long epool;  // edge-list entries handed out by the count pass
-};
-
-// Captured power steps of the modularity driver (reused across its rounds).
-struct ModGraph {
-  cudaGraphExec_t exec = nullptr;
-  const void* key[8] = {};
-  int n = 0;
-  long long M = 0;
 };
 
 struct EcGraph {
@@ -183,7 +179,6 @@ struct bna_ctx {
   long long cand_cap = 1 << 20;
   long long elist_cap = 1LL << 23;  // edge-list pool entries (grows on demand)
   EcGraph ecg;
-  ModGraph modg;
   int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
   int ntiles = 0;
   int ntiles_smp = 0;  // sampled tile list (density histogram), same block count
@@ -623,8 +618,6 @@ static void arena_release(bna_ctx* ctx, cudaStream_t st, bool to_driver) {
   ctx->last_ok = false;
   if (ctx->ecg.exec) cudaGraphExecDestroy(ctx->ecg.exec);
   ctx->ecg = EcGraph();
-  if (ctx->modg.exec) cudaGraphExecDestroy(ctx->modg.exec);
-  ctx->modg = ModGraph();
 }
 
 // Trim of a context whose every call has been synchronised (a server slot
@@ -2013,15 +2006,19 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
 
 // ---------------------------------------------------------------- modularity
 
-// Power steps replayed per graph launch (an even number: step t reads
-// buffer t & 1 and writes the other).
-constexpr int kModGraphSteps = 32;
-
+// Partition (Modularity_CPU.cpp:173-240) as a breadth-first walk of the
+// division tree: the rounds of one level are the labels created by the
+// previous level, [lo, maxres]; they run together in one cooperative launch
+// (several when the level holds more groups than fit), then the host takes
+// their decisions in round order — numbering the children as the sequential
+// loop does — and a kernel writes the children's labels.
 int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr, double lambda_min, int32_t* labels_dev,
-                       int32_t* modules, double* q, void* stream) {
+                       int32_t* modules, double* q, bna_mod_round* log, int32_t log_cap,
+                       int32_t* log_n, void* stream) {
   if (!ctx || !csr || !labels_dev || !modules || !q || csr->n < 1 || !csr->row_ptr ||
-      (csr->nnz > 0 && !csr->col_idx))
+      (csr->nnz > 0 && !csr->col_idx) || (log_cap > 0 && !log) || log_cap < 0)
     return fail(ctx, BNA_BAD_ARG, "bna_modularity: bad arguments");
+  if (log_n) *log_n = 0;
   int32_t s = set_device(ctx, as_stream(stream));
   if (s) return s;
   cudaStream_t st = as_stream(stream);
@@ -2029,12 +2026,10 @@ int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr, double lambda_min, int3
   const int32_t* rp = csr->row_ptr;
   const int32_t* ci = csr->col_idx;
   const double lam_min = lambda_min > 0 ? lambda_min : 0.001;  // Modularity_CPU.cpp:19
-  // M = (R[N] - R[0]) / 2 (:175)
-  int32_t ends[2];
-  CK(cudaMemcpyAsync(&ends[0], rp, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(&ends[1], rp + n, 4, cudaMemcpyDeviceToHost, st));
+  std::vector<int32_t> R((size_t)n + 1);
+  CK(cudaMemcpyAsync(R.data(), rp, R.size() * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  const long long M = ((long long)ends[1] - ends[0]) / 2;
+  const long long M = ((long long)R[n] - R[0]) / 2;  // (:175)
   if (M == 0) {  // no edge: one module; the reference's Q is 0 / 0
     std::vector<int32_t> ones(n, 1);
     CK(cudaMemcpyAsync(labels_dev, ones.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
@@ -2044,118 +2039,235 @@ int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr, double lambda_min, int3
     return BNA_OK;
   }
   const int sms = ctx->sms;
-  const int grid = mod_grid_blocks(sms);
-  int32_t *label, *adj_dev;
-  uint8_t* g;
-  double *sumbg, *vb, *y, *parts;
-  long long* kmod;
-  void* state;
+  const int stage_max = mod_stage_max();
+  const int grid0 = mod_level_grid(sms, 0);                          // most blocks
+  const int grid_lo = mod_level_grid(sms, (size_t)stage_max * 8);  // fewest blocks
+  if (grid0 < 1 || grid_lo < 1)
+    return fail(ctx, BNA_CUDA_ERROR, "bna_modularity: no resident block fits");
+  const size_t gbytes = mod_group_bytes(), abytes = mod_assign_bytes();
+  const long long nnz = (long long)R[n] - R[0];
+  int32_t *label, *rows, *loc, *cnt, *lrp, *lci, *blkgrp, *adj_dev;
+  double *vd, *y, *parts;
+  float2 *vf, *rs;
+  void *groups, *assign;
+  unsigned long long* kmod;
   ENSURE(S_MOD_LABEL, (size_t)n * 4, label);
-  ENSURE(S_MOD_G, (size_t)n, g);
-  ENSURE(S_MOD_SUMBG, (size_t)n * 8, sumbg);
-  ENSURE(S_MOD_V, (size_t)2 * n * 8, vb);
+  ENSURE(S_MOD_ROWS, (size_t)n * 4, rows);
+  ENSURE(S_MOD_LOC, (size_t)n * 4, loc);
+  ENSURE(S_MOD_CNT, (size_t)n * 4, cnt);
+  ENSURE(S_MOD_LRP, (size_t)(n + 1) * 4, lrp);
+  ENSURE(S_MOD_LCI, (size_t)std::max(nnz, 1LL) * 4, lci);
+  ENSURE(S_MOD_VD, (size_t)2 * n * 8, vd);
+  ENSURE(S_MOD_VF, (size_t)2 * n * 8, vf);
+  ENSURE(S_MOD_RS, (size_t)n * 8, rs);
   ENSURE(S_MOD_Y, (size_t)n * 8, y);
-  ENSURE(S_MOD_PARTS, (size_t)grid * 3 * 8, parts);
-  ENSURE(S_MOD_STATE, mod_state_bytes(), state);
-  ENSURE(S_MOD_KMOD, (size_t)(2 * n + 2) * 8, kmod);
+  ENSURE(S_MOD_PARTS, (size_t)grid0 * mod_parts_per_block() * 8, parts);
+  ENSURE(S_MOD_BLKGRP, (size_t)grid0 * 4, blkgrp);
+  ENSURE(S_MOD_GROUPS, (size_t)grid0 * gbytes, groups);  // at most one group per block
+  ENSURE(S_MOD_ASSIGN, (size_t)(n / 2 + 1) * abytes, assign);
+  ENSURE(S_MOD_KMOD, (size_t)(2 * n + 2) * 8 + 8, kmod);  // labels run up to 2 (n - 1)
   ENSURE(S_MOD_ADJ, (size_t)(2 * n + 2) * 4, adj_dev);
   CK(cudaMemsetAsync(label, 0, (size_t)n * 4, st));
-  // the power steps, captured once per graph and buffers
-  ModGraph& mg = ctx->modg;
-  const void* key[8] = {rp, ci, g, sumbg, vb, y, parts, state};
-  bool same = mg.exec && mg.n == n && mg.M == M;
-  for (int k = 0; k < 8 && same; ++k) same = mg.key[k] == key[k];
-  if (!same) {
-    if (mg.exec) cudaGraphExecDestroy(mg.exec);
-    mg = ModGraph();
-    cudaStream_t cap;
-    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    for (int t = 0; t < kModGraphSteps; ++t)
-      launch_mod_step(n, M, rp, ci, g, sumbg, vb + (size_t)(t & 1) * n, y,
-                      vb + (size_t)((t + 1) & 1) * n, parts, state, sms, cap);
-    cudaGraph_t graph;
-    cudaError_t ce = cudaStreamEndCapture(cap, &graph);
-    cudaStreamDestroy(cap);
-    CK(ce);
-    ce = cudaGraphInstantiate(&mg.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    CK(ce);
-    for (int k = 0; k < 8; ++k) mg.key[k] = key[k];
-    mg.n = n;
-    mg.M = M;
-  }
-  // one power iteration (Lead_Vector): -> lambda; the final iterate's buffer
-  long long subp = 0, subn = 0;
-  int vfinal = 0;
-  auto lead_vector = [&](double beta, double* lambda) -> int32_t {
-    CK(launch_mod_init(n, g, rp, vb, parts, state, beta, 10000, 1e-6, sms, st));
-    int it = 0, done = 0;
-    for (;;) {
-      CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      mod_state_read(ctx->pinned, nullptr, nullptr, &it, &done, nullptr, nullptr, nullptr,
-                     nullptr);
-      if (done) break;
-      CK(cudaGraphLaunch(mg.exec, st));
-    }
-    vfinal = it & 1;
-    CK(launch_mod_final(n, g, vb + (size_t)vfinal * n, vb + (size_t)(vfinal ^ 1) * n, state, st));
-    CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    mod_state_read(ctx->pinned, nullptr, nullptr, nullptr, nullptr, lambda, &subp, &subn,
-                   nullptr);
-    return BNA_OK;
-  };
-  // Partition (:186-212): rounds until no label above the current round remains
+  std::vector<int32_t> lab_h((size_t)n, 0), rows_h, loc_h((size_t)n, 0), lrp_h, blk_h;
   std::vector<int32_t> adj((size_t)2 * n + 2, 0);
-  int round = 0, maxres = 0, index = 1, mods = 1;
-  while (round <= maxres) {
-    CK(launch_mod_round(n, label, round, rp, g, state, sms, st));
-    CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    long long numg = 0;
-    mod_state_read(ctx->pinned, &numg, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                   nullptr);
-    if (numg) {
-      CK(launch_mod_sumbg(n, rp, ci, g, M, state, sumbg, sms, st));
-      double lambda = 0, l2 = 0;
-      s = lead_vector(0.0, &lambda);
-      if (s) return s;
-      if (lambda < 0) {  // the leading eigenvalue of B - lambda I (:271-272)
-        s = lead_vector(-lambda, &l2);
-        if (s) return s;
-        lambda += l2;
-      }
-      const bool issub = lambda > lam_min && subp > 1 && subn > 1;
-      if (issub) {
-        CK(launch_mod_assign(n, g, vb + (size_t)vfinal * n, maxres, subp, subn, label, sms, st));
-        maxres += 2;
-      } else {
-        adj[round] = index++;
-      }
-      mods += issub ? 1 : 0;
+  std::vector<char> grp_h, asg_h;
+  std::vector<bna_mod_round> recs;
+  std::vector<int> gcount, goff;
+  int lo = 0, maxres = 0, index = 1, mods = 1;
+  int32_t nrec = 0;
+  while (lo <= maxres) {
+    const int hi = maxres, nlab = hi - lo + 1;
+    // the level's groups: nodes by label, ascending (counting sort on the host)
+    gcount.assign((size_t)nlab + 1, 0);
+    for (int i = 0; i < n; ++i)
+      if (lab_h[i] >= lo && lab_h[i] <= hi) ++gcount[lab_h[i] - lo + 1];
+    goff.assign((size_t)nlab + 1, 0);
+    for (int k = 0; k < nlab; ++k) goff[k + 1] = goff[k] + gcount[k + 1];
+    const int nrows = goff[nlab];
+    rows_h.resize((size_t)nrows);
+    {
+      std::vector<int> fill(goff.begin(), goff.end() - 1);
+      for (int i = 0; i < n; ++i)
+        if (lab_h[i] >= lo && lab_h[i] <= hi) {
+          const int k = lab_h[i] - lo;
+          loc_h[i] = fill[k] - goff[k];
+          rows_h[fill[k]++] = i;
+        }
     }
-    ++round;
+    std::vector<int> live;  // non-empty labels of the level, ascending
+    for (int k = 0; k < nlab; ++k)
+      if (goff[k + 1] > goff[k]) live.push_back(k);
+    if (live.empty()) {
+      lo = hi + 1;
+      continue;
+    }
+    // the level's induced subgraph (edges inside a group, group-local columns)
+    CK(cudaMemcpyAsync(rows, rows_h.data(), (size_t)nrows * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(loc, loc_h.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
+    CK(launch_mod_build(nrows, rows, rp, ci, label, loc, cnt, lrp, lci, sms, st));
+    lrp_h.resize((size_t)nrows + 1);
+    CK(cudaMemcpyAsync(lrp_h.data(), lrp, lrp_h.size() * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    recs.assign(live.size(), bna_mod_round{});
+    std::vector<int> fb(live.size());
+    std::vector<long long> sp(live.size()), sn(live.size());
+    // launches of at most grid_lo groups; blocks shared out by each group's
+    // work per step (positions + in-group edges)
+    for (size_t c0 = 0; c0 < live.size(); c0 += (size_t)grid_lo) {
+      const size_t c1 = std::min(live.size(), c0 + (size_t)grid_lo);
+      const int ng = (int)(c1 - c0);
+      int stage_rows = 0;
+      bool e16 = true;
+      for (int k = 0; k < ng; ++k) {
+        const int gk = live[c0 + k], nr = goff[gk + 1] - goff[gk];
+        if (nr <= stage_max) stage_rows = std::max(stage_rows, nr);
+        e16 = e16 && nr <= 65536;
+      }
+      const int stage_bytes = (stage_rows * 8 + 15) / 16 * 16;
+      std::vector<double> work((size_t)ng);
+      double wsum = 0;
+      for (int k = 0; k < ng; ++k) {
+        const int gk = live[c0 + k];
+        work[k] = (double)(goff[gk + 1] - goff[gk]) * 8.0 +
+                  (double)(lrp_h[goff[gk + 1]] - lrp_h[goff[gk]]);
+        wsum += work[k];
+      }
+      // blocks per group for a grid of gm blocks, and the largest column slice
+      // of a block (the kernel's split: equal shares of positions + edges)
+      std::vector<int> nbk((size_t)ng);
+      auto share_out = [&](int gm) -> long long {
+        long long emax = 0;
+        for (int k = 0; k < ng; ++k) {
+          const int gk = live[c0 + k], off = goff[gk], nr = goff[gk + 1] - goff[gk];
+          // a share of the grid by work, but no block with less than ~32 entries
+          // per thread: more blocks than that only lengthen the group's barriers
+          const int nb = std::min(1 + (int)((double)(gm - ng) * work[k] / wsum),
+                                  1 + (int)(work[k] / 32768.0));
+          nbk[k] = nb;
+          const long long e0 = lrp_h[off], W = (long long)nr + (lrp_h[off + nr] - e0);
+          int prev = off;
+          for (int b = 1; b <= nb; ++b) {
+            int p;
+            if (b == nb) {
+              p = off + nr;
+            } else {
+              const long long t = W * b / nb;
+              int l = 0, h = nr;
+              while (l < h) {
+                const int mid = (l + h) >> 1;
+                if ((long long)mid + (lrp_h[off + mid] - e0) >= t) h = mid;
+                else l = mid + 1;
+              }
+              p = off + l;
+            }
+            emax = std::max(emax, (long long)lrp_h[p] - lrp_h[prev]);
+            prev = p;
+          }
+        }
+        return emax;
+      };
+      // the most blocks per SM whose shared memory holds the iterate stage and
+      // every block's column slice; else column slices stay in global memory
+      size_t smem = 0;
+      int ecap = 0, grid_max = 0;
+      const int esz = e16 ? 2 : 4;
+      for (int bps = 4; bps >= 1 && !ecap; --bps) {
+        int dyn = std::min(mod_smem_max(), (228 * 1024) / bps - 17 * 1024) / 1024 * 1024;
+        int gm = 0;
+        for (int tries = 0; tries < 8 && dyn >= stage_bytes; ++tries, dyn -= 1024) {
+          gm = mod_level_grid(sms, (size_t)dyn);
+          if (gm >= bps * sms) break;
+        }
+        if (gm < bps * sms || dyn < stage_bytes) continue;
+        gm = bps * sms;
+        if (gm < ng) continue;
+        const long long emax = share_out(gm);
+        if ((long long)stage_bytes + emax * esz <= dyn) {
+          smem = (size_t)stage_bytes + (size_t)emax * esz;
+          ecap = (int)std::max(emax, 1LL);
+          grid_max = gm;
+        }
+      }
+      if (!ecap) {
+        smem = (size_t)stage_bytes;
+        grid_max = std::max(ng, mod_level_grid(sms, smem));
+        share_out(grid_max);
+      }
+      grp_h.assign((size_t)ng * gbytes, 0);
+      blk_h.clear();
+      for (int k = 0; k < ng; ++k) {
+        const int gk = live[c0 + k];
+        const int nb = nbk[k];
+        long long kg = 0;
+        for (int q2 = goff[gk]; q2 < goff[gk + 1]; ++q2)
+          kg += R[rows_h[q2] + 1] - R[rows_h[q2]];
+        mod_group_set(grp_h.data() + (size_t)k * gbytes, lo + gk, goff[gk],
+                      goff[gk + 1] - goff[gk], (int)blk_h.size(), nb, kg);
+        for (int b = 0; b < nb; ++b) blk_h.push_back(k);
+      }
+      const int grid = (int)blk_h.size();  // <= grid_max: every block resident
+      CK(cudaMemcpyAsync(groups, grp_h.data(), grp_h.size(), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(blkgrp, blk_h.data(), (size_t)grid * 4, cudaMemcpyHostToDevice, st));
+      CK(launch_mod_level(n, M, rp, label, rows, lrp, lci, groups, blkgrp, vd, vf, rs, y, parts,
+                          nrows, stage_rows, stage_bytes, ecap, e16 ? 1 : 0, smem, grid, 10000,
+                          1e-6, st));
+      CK(cudaMemcpyAsync(grp_h.data(), groups, grp_h.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int k = 0; k < ng; ++k) {
+        const int gk = live[c0 + k];
+        bna_mod_round& e = recs[c0 + k];
+        int err = 0;
+        mod_group_get(grp_h.data() + (size_t)k * gbytes, &err, e.iters, e.residual, &e.lambda,
+                      &sp[c0 + k], &sn[c0 + k], &fb[c0 + k]);
+        if (err) return fail(ctx, BNA_TIMEOUT, "bna_modularity: a group barrier wait expired");
+        e.round = lo + gk;
+        e.nodes = goff[gk + 1] - goff[gk];
+      }
+    }
+    // decisions in round order (:204-211, :283-292)
+    int nas = 0;
+    asg_h.resize(live.size() * abytes);
+    for (size_t k = 0; k < live.size(); ++k) {
+      bna_mod_round& e = recs[k];
+      const bool issub = e.lambda > lam_min && sp[k] > 1 && sn[k] > 1;
+      e.divided = issub ? 1 : 0;
+      if (issub) {
+        const int gk = live[k];
+        mod_assign_set(asg_h.data() + (size_t)nas * abytes, goff[gk], goff[gk + 1] - goff[gk],
+                       fb[k], maxres, (double)(sp[k] - sn[k]) + 0.5);
+        ++nas;
+        maxres += 2;
+        ++mods;
+      } else {
+        adj[e.round] = index++;
+      }
+      if (nrec < log_cap) log[nrec] = e;
+      ++nrec;
+    }
+    if (nas) {
+      CK(cudaMemcpyAsync(assign, asg_h.data(), (size_t)nas * abytes, cudaMemcpyHostToDevice, st));
+      CK(launch_mod_assign(nrows, rows, assign, nas, vd, label, st));
+      CK(cudaMemcpyAsync(lab_h.data(), label, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+    }
+    lo = hi + 1;
   }
   // Q (:215-224) from integer counts: same-module entries and module degree sums
-  CK(cudaMemsetAsync(state, 0, mod_state_bytes(), st));
-  CK(cudaMemsetAsync(kmod, 0, (size_t)(maxres + 1) * 8, st));
-  CK(launch_mod_q(n, rp, ci, label, kmod, state, sms, st));
-  std::vector<long long> kh((size_t)maxres + 1);
-  CK(cudaMemcpyAsync(kh.data(), kmod, kh.size() * 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->pinned, state, mod_state_bytes(), cudaMemcpyDeviceToHost, st));
+  unsigned long long* same_dev = kmod + (size_t)2 * n + 2;
+  CK(cudaMemsetAsync(kmod, 0, (size_t)(2 * n + 3) * 8, st));
+  CK(launch_mod_q(n, rp, ci, label, kmod, same_dev, sms, st));
+  std::vector<unsigned long long> kh((size_t)maxres + 2);
+  CK(cudaMemcpyAsync(kh.data(), kmod, (size_t)(maxres + 1) * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&kh[maxres + 1], same_dev, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(adj_dev, adj.data(), (size_t)(maxres + 1) * 4, cudaMemcpyHostToDevice, st));
   CK(launch_mod_map(n, label, adj_dev, labels_dev, sms, st));
   CK(cudaStreamSynchronize(st));
-  long long same_cnt = 0;
-  mod_state_read(ctx->pinned, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                 &same_cnt);
-  double qq = (double)same_cnt;
-  for (long long kgv : kh) qq -= (double)kgv * (double)kgv / 2 / (double)M;
+  double qq = (double)kh[maxres + 1];
+  for (int k = 0; k <= maxres; ++k) qq -= (double)kh[k] * (double)kh[k] / 2 / (double)M;
   qq /= 2 * (double)M;
   *modules = mods;
   *q = qq;
+  if (log_n) *log_n = nrec;
   ctx->klaunch = 0;
   return BNA_OK;
 }

@@ -9,313 +9,648 @@
 // matrix B_G - beta*I by power iteration (v_0[i] = i on G; per step
 // y = A_G v0 - (v0.k / 2 / M) k - (sumBG - beta) v0, v = y / |y|, stop when
 // |v - v0| or |v + v0| <= 1e-6 or after 10,000 steps; eigenvalue = +-|y| by
-// the sign of v*v0 at the largest |v|).  A negative eigenvalue is retried
-// with beta = -lambda; the round divides when lambda > LAMBDA and both signs
-// hold more than one node.  Q (:215-224) is computed at the end.
+// the sign of v*v0 at the first largest |v|).  A negative eigenvalue is
+// retried with beta = -lambda; the round divides when lambda > LAMBDA and
+// both signs hold more than one node.  Q (:215-224) is computed at the end.
 //
-// Here one round's steps are kernels: the mask and K_G, the integer sumBG,
-// then per power step a warp-per-row SpMV (FP64; the correction term with
-// the reference's operation order, no contraction) and an elementwise
-// normalisation with fixed-order reductions of |y|^2, |v -+ v0|^2 and v.k;
-// the steps are replayed from a CUDA graph and stop on a device flag.  The
-// decisions (divide or not, new labels) are the reference's.
+// Rounds are the nodes of a binary division tree visited breadth first, so
+// the groups of one tree level depend on nothing but their own nodes: here
+// every level is one cooperative, persistent launch (mod_level_kernel) in
+// which each group owns a contiguous range of blocks and runs its whole
+// Sub_Partition — sumBG, Lead_Vector, the retry, the sign rule and the sizes
+// of the two sides — with barriers among its own blocks only (bounded waits).
+// The host then takes the decisions in round order, which numbers the
+// children exactly as the sequential loop does.
+//
+// Arithmetic: GB300's FP64 rate is ~1/64 of its FP32 rate, so the SpMV sum
+// over a row runs in float-float ("double-float", Knuth's TwoSum) on the
+// iterate kept as a (hi, lo) float pair beside its double value: about 48
+// significant bits, the same order as the reference's sequential FP64 sum.
+// The correction term, the normalisation, the norms and the stop test stay in
+// FP64, with fixed-order reductions, so a run is deterministic.
+#include <algorithm>
+#include <cmath>
+
 #include "common.cuh"
 
 namespace bna {
 
-struct ModState {
-  double vk;     // sum over G of v0_i k_i for the next step
-  double y2;     // |y|^2 of the current step
-  double vnorm;  // |y| of the last completed step
-  double err1, err2;
-  double beta;
-  double eps;
-  double lambda;  // +-vnorm by the sign rule
-  long long numg, kg;
+// One group (round) of a tree level.  Host-written: label .. kg; device-
+// written: the rest.
+struct ModGroup {
+  int label;     // the round number (Result value) of the group
+  int row_off;   // its nodes: rows[row_off, row_off + rows), ascending
+  int rows;
+  int blk0;      // its blocks: [blk0, blk0 + nblk) of the launch
+  int nblk;
+  int err;       // a bounded barrier wait expired
+  long long kg;  // K_G = sum of the degrees of its nodes
+  int iters[2];
+  double resid[2];
+  double lambda;
   long long subp, subn;
-  long long same;  // directed entries whose ends share a label (Q)
-  int iter, done, max_iter;
-  int maxi;
-  unsigned int counter;
+  int fbuf;      // buffer (0/1) of the final eigenvector iterate
+  unsigned int bar_count, bar_gen;
+  double res[8];  // totals published by the last block to reach a barrier
 };
 
-constexpr int kModThreads = 256;
+constexpr int kModThreads = 1024;
+constexpr int kModWarps = kModThreads / 32;
+// Partial sums per block, each phase in slots of its own: 0 start vector,
+// 1 |y|^2, 2-4 the norms and v.k, 8-11 the eigenvalue sign and side sizes.
+constexpr int kModParts = 12;
+// Groups of at most this many nodes keep their iterate ((hi, lo) floats) in
+// shared memory during the gathers: 96 KB.
+constexpr int kModStageMax = 12288;
+// Dynamic shared memory a block may ask for (iterate stage + column slice).
+constexpr int kModSmemMax = 200 * 1024;
 
-__device__ __forceinline__ bool mod_last_block(ModState* st) {
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = (atomicAdd(&st->counter, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (last) __threadfence();
-  return last;
+// (hi, lo) float pair of a double: hi = RN(x), lo = RN(x - hi).
+__device__ __forceinline__ float2 mod_split(double x) {
+  const float hi = __double2float_rn(x);
+  return make_float2(hi, __double2float_rn(x - (double)hi));
 }
 
-// Fixed-order sum of nparts x W partials by one block (all threads call).
-template <int W>
-__device__ __forceinline__ void mod_reduce(const double* parts, int nparts, double* out) {
-  __shared__ double red[kModThreads][W];
-  double s[W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) s[w] = 0;
-  for (int b = threadIdx.x; b < nparts; b += kModThreads)
-#pragma unroll
-    for (int w = 0; w < W; ++w) s[w] += parts[b * W + w];
-#pragma unroll
-  for (int w = 0; w < W; ++w) red[threadIdx.x][w] = s[w];
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void mod_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Barrier among the nb blocks of one group (all co-resident: cooperative
+// launch).  Bounded: a wait longer than limit_ns raises g->err and returns false.
+__device__ __forceinline__ bool group_barrier(ModGroup* g, int nb, uint64_t limit_ns) {
+  __shared__ int ok_s;
   __syncthreads();
-  for (int h = kModThreads / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h)
-#pragma unroll
-      for (int w = 0; w < W; ++w) red[threadIdx.x][w] += red[threadIdx.x + h][w];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &g->bar_gen;
+    const unsigned int g0 = *gen;  // cannot advance before this block arrives
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(&g->bar_count, 1u) == (unsigned int)nb - 1) {
+      g->bar_count = 0;
+      __threadfence();
+      atomicAdd(&g->bar_gen, 1u);
+    } else {
+      uint64_t t0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == g0) {
+        uint64_t t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > limit_ns) {
+          ok = 0;
+          atomicExch(&g->err, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
   }
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int w = 0; w < W; ++w) out[w] = red[0][w];
   __syncthreads();
+  return ok_s != 0;
 }
 
+// Block sum of W per-thread values into parts[blockIdx.x * kModParts + k0 ..]
+// (warp butterflies, then warps in order: a fixed order).  Only the first
+// `aw` warps can hold non-zero values (FP64 work is scarce on this GPU: the
+// other warps skip it).
 template <int W>
-__device__ __forceinline__ void mod_block_partials(double (&a)[W], double* parts) {
-  __shared__ double ws[kModThreads / 32][W];
+__device__ __forceinline__ void block_partials(double (&a)[W], double* parts, int k0, int aw) {
+  __shared__ double ws[kModWarps][W];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < aw) {
 #pragma unroll
-  for (int w = 0; w < W; ++w)
+    for (int w = 0; w < W; ++w)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a[w] += __shfl_xor_sync(0xffffffffu, a[w], o);
-  if (lane == 0)
+      for (int o = 16; o > 0; o >>= 1) a[w] += __shfl_xor_sync(0xffffffffu, a[w], o);
+    if (lane == 0)
 #pragma unroll
-    for (int w = 0; w < W; ++w) ws[warp][w] = a[w];
+      for (int w = 0; w < W; ++w) ws[warp][w] = a[w];
+  }
   __syncthreads();
   if (threadIdx.x == 0)
 #pragma unroll
     for (int w = 0; w < W; ++w) {
       double t = 0;
-      for (int k = 0; k < kModThreads / 32; ++k) t += ws[k][w];
-      parts[blockIdx.x * W + w] = t;
+      for (int k = 0; k < aw; ++k) t += ws[k][w];
+      parts[(size_t)blockIdx.x * kModParts + k0 + w] = t;
     }
+  __syncthreads();
 }
 
-// Round setup: G = (label == round), |G| and K_G = sum of degrees over G
-// (integer atomics: exact in any order).  st->numg / kg zeroed by the host.
-__global__ void mod_round_kernel(int n, const int32_t* __restrict__ label, int round,
-                                 const int32_t* __restrict__ rp, uint8_t* __restrict__ g,
-                                 ModState* st) {
-  long long cnt = 0, deg = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const bool in = label[i] == round;
-    g[i] = in ? 1 : 0;
-    if (in) {
-      ++cnt;
-      deg += rp[i + 1] - rp[i];
-    }
-  }
+// Warps holding thread-per-position work for `cnt` positions.
+__device__ __forceinline__ int active_warps(int cnt) {
+  const int w = (cnt + 31) >> 5;
+  return w < kModWarps ? w : kModWarps;
+}
+
+// Sum over the group's blocks [b0, b0 + nb) of partial k0 .. k0 + W - 1 in a
+// fixed order (thread-strided sums, warp butterflies, warps in order), so
+// the result does not depend on timing.  Every thread gets the totals.
+template <int W>
+__device__ __forceinline__ void group_reduce(const double* parts, int b0, int nb, int k0,
+                                             double (&out)[W]) {
+  __shared__ double ws[kModWarps][W];
+  __shared__ double tot[W];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double s[W];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    deg += __shfl_xor_sync(0xffffffffu, deg, o);
+  for (int w = 0; w < W; ++w) s[w] = 0;
+  for (int b = threadIdx.x; b < nb; b += kModThreads)
+#pragma unroll
+    for (int w = 0; w < W; ++w) s[w] += __ldcg(parts + (size_t)(b0 + b) * kModParts + k0 + w);
+  const int aw = active_warps(nb);
+  if (warp < aw) {
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s[w] += __shfl_xor_sync(0xffffffffu, s[w], o);
+    if (lane == 0)
+#pragma unroll
+      for (int w = 0; w < W; ++w) ws[warp][w] = s[w];
   }
-  if ((threadIdx.x & 31) == 0 && cnt) {
-    atomicAdd((unsigned long long*)&st->numg, (unsigned long long)cnt);
-    atomicAdd((unsigned long long*)&st->kg, (unsigned long long)deg);
-  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      double t = 0;
+      for (int k = 0; k < aw; ++k) t += ws[k][w];
+      tot[w] = t;
+    }
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < W; ++w) out[w] = tot[w];
+  __syncthreads();
 }
 
-// sumBG[i] = |adj(i) ∩ G| - k_i * K_G / 2 / M in integer arithmetic
-// (Modularity_CPU.cpp:258-266), warp per row of G.
-__global__ void mod_sumbg_kernel(int n, const int32_t* __restrict__ rp,
-                                 const int32_t* __restrict__ ci, const uint8_t* __restrict__ g,
-                                 long long M, const ModState* st, double* __restrict__ sumbg) {
+// Induced subgraph of a tree level, built before its launch: positions p of
+// the level's node list (groups contiguous, nodes ascending within a group);
+// lrp / lci = the CSR of the edges whose ends share a group, columns as
+// group-local indices (position - the group's first position), in the
+// original column order.
+
+// Edges of each position's node that stay inside its group (warp per position).
+__global__ void mod_count_kernel(int nrows, const int32_t* __restrict__ rows,
+                                 const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                 const int32_t* __restrict__ label, int32_t* __restrict__ cnt) {
   const int lane = threadIdx.x & 31;
-  const long long kg = st->kg;
-  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n;
-       i += gridDim.x * (blockDim.x >> 5)) {
-    if (!g[i]) continue;
-    const int b = rp[i], e = rp[i + 1];
+  for (int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < nrows;
+       p += gridDim.x * (blockDim.x >> 5)) {
+    const int i = rows[p], r = label[i];
+    const int kb = rp[i], ke = rp[i + 1];
     int in = 0;
-    for (int k = b + lane; k < e; k += 32) in += g[ci[k]];
+    for (int k = kb + lane; k < ke; k += 32) in += __ldg(label + __ldg(ci + k)) == r;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) in += __shfl_xor_sync(0xffffffffu, in, o);
-    if (lane == 0) sumbg[i] = (double)((long long)in - (long long)(e - b) * kg / 2 / M);
+    if (lane == 0) cnt[p] = in;
   }
 }
 
-// Start of a power iteration: v = (G ? i : 0), v.k, counters.
-__global__ __launch_bounds__(kModThreads) void mod_init_kernel(
-    int n, const uint8_t* __restrict__ g, const int32_t* __restrict__ rp, double* __restrict__ v,
-    double* parts, ModState* st, double beta, int max_iter, double eps) {
-  double a[1] = {0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double x = g[i] ? (double)i : 0.0;
-    v[i] = x;
-    if (g[i]) a[0] += x * (double)(rp[i + 1] - rp[i]);
-  }
-  mod_block_partials<1>(a, parts);
-  if (mod_last_block(st)) {
-    __shared__ double tot[1];
-    mod_reduce<1>(parts, gridDim.x, tot);
-    if (threadIdx.x == 0) {
-      st->vk = tot[0];
-      st->beta = beta;
-      st->eps = eps;
-      st->max_iter = max_iter;
-      st->iter = 0;
-      st->err1 = st->err2 = 1.0;
-      st->vnorm = 0.0;
-      st->done = max_iter <= 0 ? 1 : 0;
-      st->counter = 0;
-    }
-  }
-}
-
-// One power step, part 1: y = A_G v0 - (vk / 2 / M * k + (sumBG - beta) * v0)
-// on G (v0 is zero off G, so the gather needs no mask), |y|^2.
-__global__ __launch_bounds__(kModThreads) void mod_spmv_kernel(
-    int n, long long M, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-    const uint8_t* __restrict__ g, const double* __restrict__ sumbg,
-    const double* __restrict__ v0, double* __restrict__ y, double* parts, ModState* st) {
-  if (st->done) return;
-  const double vk = st->vk, beta = st->beta;
-  const double c = __ddiv_rn(__ddiv_rn(vk, 2.0), (double)M);  // vk / 2 / M
-  const int lane = threadIdx.x & 31;
-  double a[1] = {0};
-  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n;
-       i += gridDim.x * (blockDim.x >> 5)) {
-    if (!g[i]) continue;
-    const int b = rp[i], e = rp[i + 1];
-    double t = 0;
-    for (int k0 = b; k0 < e; k0 += 128) {
-      double x[4];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int k = k0 + lane + 32 * m;
-        x[m] = k < e ? v0[__ldg(ci + k)] : 0.0;
-      }
-#pragma unroll
-      for (int m = 0; m < 4; ++m) t = __dadd_rn(t, x[m]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t = __dadd_rn(t, __shfl_xor_sync(0xffffffffu, t, o));
-    if (lane == 0) {
-      const double corr = __dadd_rn(__dmul_rn(c, (double)(e - b)),
-                                    __dmul_rn(__dsub_rn(sumbg[i], beta), v0[i]));
-      t = __dsub_rn(t, corr);
-      y[i] = t;
-      a[0] = __dadd_rn(a[0], __dmul_rn(t, t));
-    }
-  }
-  mod_block_partials<1>(a, parts);
-  if (mod_last_block(st)) {
-    __shared__ double tot[1];
-    mod_reduce<1>(parts, gridDim.x, tot);
-    if (threadIdx.x == 0) {
-      st->y2 = tot[0];
-      st->counter = 0;
-    }
-  }
-}
-
-// One power step, part 2: v = y / |y| on G, |v - v0|, |v + v0|, v.k, stop test.
-__global__ __launch_bounds__(kModThreads) void mod_norm_kernel(
-    int n, const int32_t* __restrict__ rp, const uint8_t* __restrict__ g,
-    const double* __restrict__ y, const double* __restrict__ v0, double* __restrict__ v,
-    double* parts, ModState* st) {
-  if (st->done) return;
-  __shared__ double nrm;
-  if (threadIdx.x == 0) nrm = sqrt(st->y2);
+// Exclusive scan of cnt[0, m) into out[0, m] by one block of 1024 threads
+// (int64 running sums; the totals fit int32 since they are CSR entries).
+__global__ __launch_bounds__(1024) void mod_scan_kernel(int m, const int32_t* __restrict__ cnt,
+                                                        int32_t* __restrict__ out) {
+  __shared__ long long tot[1024];
+  const int per = (m + 1023) / 1024;
+  const int b = threadIdx.x * per, e = min(m, b + per);
+  long long s = 0;
+  for (int k = b; k < e; ++k) s += cnt[k];
+  tot[threadIdx.x] = s;
   __syncthreads();
-  const double vn = nrm;
-  double a[3] = {0, 0, 0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double old = v0[i];
-    const double x = g[i] ? __ddiv_rn(y[i], vn) : 0.0;
-    v[i] = x;
-    const double d = __dsub_rn(x, old), s = __dadd_rn(x, old);
-    a[0] = __dadd_rn(a[0], __dmul_rn(d, d));
-    a[1] = __dadd_rn(a[1], __dmul_rn(s, s));
-    if (g[i]) a[2] = __dadd_rn(a[2], __dmul_rn(x, (double)(rp[i + 1] - rp[i])));
-  }
-  mod_block_partials<3>(a, parts);
-  if (mod_last_block(st)) {
-    __shared__ double tot[3];
-    mod_reduce<3>(parts, gridDim.x, tot);
-    if (threadIdx.x == 0) {
-      st->vnorm = vn;
-      st->err1 = sqrt(tot[0]);
-      st->err2 = sqrt(tot[1]);
-      st->vk = tot[2];
-      st->iter += 1;
-      if (!(st->err1 > st->eps && st->err2 > st->eps && st->iter < st->max_iter)) st->done = 1;
-      st->counter = 0;
-    }
-  }
-}
-
-// After a power iteration (one block): the first node of G with the largest
-// |v| (node 0 when that is 0), the sign rule for lambda, and the sizes of the
-// two signs.
-__global__ __launch_bounds__(1024) void mod_final_kernel(int n, const uint8_t* __restrict__ g,
-                                                         const double* __restrict__ v,
-                                                         const double* __restrict__ v0,
-                                                         ModState* st) {
-  __shared__ double bv[1024];
-  __shared__ int bi[1024];
-  __shared__ long long bp[1024], bn[1024];
-  double best = 0.0;
-  int idx = 0;
-  long long p = 0, q = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    if (!g[i]) continue;
-    const double a = fabs(v[i]);
-    if (a > best) {  // ascending i per thread: the first maximum is kept
-      best = a;
-      idx = i;
-    }
-    p += v[i] > 0;
-    q += v[i] <= 0;
-  }
-  bv[threadIdx.x] = best;
-  bi[threadIdx.x] = idx;
-  bp[threadIdx.x] = p;
-  bn[threadIdx.x] = q;
-  __syncthreads();
-  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h) {
-      const double ov = bv[threadIdx.x + h];
-      const int oi = bi[threadIdx.x + h];
-      if (ov > bv[threadIdx.x] || (ov == bv[threadIdx.x] && ov > 0 && oi < bi[threadIdx.x])) {
-        bv[threadIdx.x] = ov;
-        bi[threadIdx.x] = oi;
-      }
-      bp[threadIdx.x] += bp[threadIdx.x + h];
-      bn[threadIdx.x] += bn[threadIdx.x + h];
-    }
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan of the thread sums
+    const long long v = threadIdx.x >= (unsigned)o ? tot[threadIdx.x - o] : 0;
+    __syncthreads();
+    tot[threadIdx.x] += v;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    const int mi = bv[0] > 0 ? bi[0] : 0;
-    st->maxi = mi;
-    st->lambda = (v[mi] * v0[mi] > 0) ? st->vnorm : -st->vnorm;
-    st->subp = bp[0];
-    st->subn = bn[0];
+  long long run = threadIdx.x ? tot[threadIdx.x - 1] : 0;
+  for (int k = b; k < e; ++k) {
+    out[k] = (int32_t)run;
+    run += cnt[k];
+  }
+  if (threadIdx.x == 1023) out[m] = (int32_t)tot[1023];
+}
+
+// Group-local columns of the in-group edges, original order (warp per
+// position; ballot + prefix popcount place each lane's entry).
+__global__ void mod_fill_kernel(int nrows, const int32_t* __restrict__ rows,
+                                const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                const int32_t* __restrict__ label, const int32_t* __restrict__ loc,
+                                const int32_t* __restrict__ lrp, int32_t* __restrict__ lci) {
+  const int lane = threadIdx.x & 31;
+  for (int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < nrows;
+       p += gridDim.x * (blockDim.x >> 5)) {
+    const int i = rows[p], r = label[i];
+    const int kb = rp[i], ke = rp[i + 1];
+    int pos = lrp[p];
+    const int end = lrp[p + 1];
+    for (int k0 = kb; k0 < ke; k0 += 32) {
+      const int k = k0 + lane;
+      const int j = k < ke ? __ldg(ci + k) : -1;
+      const bool in = j >= 0 && __ldg(label + j) == r;
+      const unsigned bal = __ballot_sync(0xffffffffu, in);
+      const int at = pos + __popc(bal & ((1u << lane) - 1u));
+      if (in && at < end) lci[at] = loc[j];
+      pos += __popc(bal);
+    }
   }
 }
 
-// A successful division: G's nodes go to maxres + 1 or maxres + 2 by sign.
-__global__ void mod_assign_kernel(int n, const uint8_t* __restrict__ g,
-                                  const double* __restrict__ v, int maxres, long long subp,
-                                  long long subn, int32_t* __restrict__ label) {
-  const double w = (double)(subp - subn) + 0.5;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    if (g[i]) label[i] = maxres + 1 + (v[i] * w <= 0 ? 1 : 0);
+// Barrier among the group's blocks that also sums partial k0 .. k0 + W - 1
+// of every block: the last block to arrive reduces them in a fixed order
+// (as group_reduce), publishes the totals in g->res and releases the others,
+// so each value is read from the partials once, not once per block.
+template <int W>
+__device__ __forceinline__ bool group_sync_reduce(ModGroup* g, int nb, int b0,
+                                                  const double* parts, int k0,
+                                                  uint64_t limit_ns, double (&out)[W]) {
+  __shared__ int last_s, ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &g->bar_gen;
+    const unsigned int g0 = *gen;  // cannot advance before this block arrives
+    __threadfence();
+    const bool last = atomicAdd(&g->bar_count, 1u) == (unsigned int)nb - 1;
+    last_s = last ? 1 : 0;
+    ok_s = 1;
+    if (!last) {
+      uint64_t t0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == g0) {
+        uint64_t t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > limit_ns) {
+          ok_s = 0;
+          atomicExch(&g->err, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  if (last_s) {
+    double t[W];
+    group_reduce<W>(parts, b0, nb, k0, t);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int w = 0; w < W; ++w) g->res[k0 + w] = t[w];
+      g->bar_count = 0;
+      __threadfence();
+      atomicAdd(&g->bar_gen, 1u);
+    }
+#pragma unroll
+    for (int w = 0; w < W; ++w) out[w] = t[w];
+    __syncthreads();
+    return true;
+  }
+  if (!ok_s) return false;
+#pragma unroll
+  for (int w = 0; w < W; ++w) out[w] = __ldcg(&g->res[k0 + w]);
+  return true;
+}
+
+struct ModArgs {
+  int n;
+  long long M;
+  const int32_t* rp;       // the graph's row pointers (degrees)
+  const int32_t* label;
+  const int32_t* rows;     // level positions -> nodes
+  const int32_t* lrp;      // induced CSR of the level (positions)
+  const int32_t* lci;      // group-local columns
+  ModGroup* groups;
+  const int32_t* blk_grp;  // group index of every block
+  double* vd;              // [2][nrows] iterate (double), by position
+  float2* vf;              // [2][nrows] iterate (hi, lo), by position
+  float2* rs;              // [nrows] float-float row sums of a step
+  double* y;               // [nrows]
+  double* parts;           // [grid][kModParts]
+  int nrows;
+  int stage_max;           // groups of at most this many nodes gather from shared memory
+  int stage_bytes;         // offset of the column slice in dynamic shared memory
+  int ecap;                // column-slice capacity (entries) in shared memory, 0: none
+  int e16;                 // slice entries are 16-bit (every group below 65,536 nodes)
+  int max_iter;
+  double eps;
+  uint64_t limit_ns;
+};
+
+// One Lead_Vector call (Modularity_CPU.cpp:315-377) of group g with the
+// given beta, run by the group's blocks; block lb owns positions [p0, p1).
+// Returns false when a barrier wait expired.  On return: *lambda,
+// iterations, residual, final buffer, the sizes of the two signs.
+// Column (group-local index) of in-group edge e: from the block's slice in
+// shared memory (s16 / s32, first edge eb0) when it was loaded there.
+__device__ __forceinline__ int edge_col(const ModArgs& a, const uint16_t* s16, const int32_t* s32,
+                                        int eb0, int e) {
+  return s16 ? (int)s16[e - eb0] : s32 ? s32[e - eb0] : __ldg(a.lci + e);
+}
+
+__device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb, int p0, int p1,
+                            long long kg, double beta, float2* stage, const uint16_t* s16,
+                            const int32_t* s32, double* lambda, int* iters, double* resid,
+                            int* fbuf, long long* subp, long long* subn) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int off = g->row_off, nr = g->rows;
+  const double Md = (double)a.M;
+  const bool staged = stage != nullptr;
+  const int eb0 = __ldg(a.lrp + p0);
+  // v = (G ? i : 0) (:322-324); v.k for the first step
+  double p1s[1] = {0};
+  for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
+    const int i = a.rows[p];
+    const double x = (double)i;
+    a.vd[p] = x;
+    a.vf[p] = mod_split(x);
+    p1s[0] += x * (double)(a.rp[i + 1] - a.rp[i]);
+  }
+  const int aw = active_warps(p1 - p0);
+  __shared__ double scal[4];  // per-step scalars, computed by one thread
+  block_partials<1>(p1s, a.parts, 0, aw);
+  double t1[1];
+  if (!group_sync_reduce<1>(g, nb, b0, a.parts, 0, a.limit_ns, t1)) return false;
+  double vk = t1[0];
+  double err1 = 1, err2 = 1, vn = 0;
+  int it = 0;
+  while (err1 > a.eps && err2 > a.eps && it < a.max_iter) {
+    const size_t cur = (size_t)(it & 1) * a.nrows, nxt = (size_t)((it + 1) & 1) * a.nrows;
+    const float2* vfc = a.vf + cur + off;  // the group's iterate, group-local index
+    if (staged) {
+      for (int q = threadIdx.x; q < nr; q += kModThreads) stage[q] = __ldcg(vfc + q);
+      __syncthreads();
+    }
+    // A_G v0 over the in-group edges (:342-343), float-float: warp per position
+    for (int p = p0 + warp; p < p1; p += kModWarps) {
+      const int eb = __ldg(a.lrp + p), ee = __ldg(a.lrp + p + 1);
+      float sh = 0.0f, sl = 0.0f;
+      for (int e0 = eb; e0 < ee; e0 += 128) {
+        float2 x[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const int e = e0 + lane + 32 * m;
+          const int q = e < ee ? edge_col(a, s16, s32, eb0, e) : -1;
+          x[m] = q < 0 ? make_float2(0.0f, 0.0f) : (staged ? stage[q] : __ldcg(vfc + q));
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          float s, e;
+          mod_two_sum(sh, x[m].x, s, e);
+          sh = s;
+          sl = __fadd_rn(sl, __fadd_rn(e, x[m].y));
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+        float s, e;
+        mod_two_sum(sh, oh, s, e);
+        sh = s;
+        sl = __fadd_rn(sl, __fadd_rn(ol, e));
+      }
+      if (lane == 0) a.rs[p] = make_float2(sh, sl);
+    }
+    __syncthreads();
+    // y = A_G v0 - (v_k / 2 / M k + (sumBG - beta) v0) (:344), thread per position;
+    // sumBG = |adj(i) ∩ G| - k K_G / 2 / M in integers (:258-266)
+    if (threadIdx.x == 0) scal[0] = __ddiv_rn(__ddiv_rn(vk, 2.0), Md);  // v_k / 2 / M
+    __syncthreads();
+    const double c = scal[0];
+    double py[1] = {0};
+    for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
+      const int i = a.rows[p];
+      const long long k = a.rp[i + 1] - a.rp[i];
+      const double sbg = (double)((long long)(a.lrp[p + 1] - a.lrp[p]) - k * kg / 2 / a.M);
+      const float2 rsum = a.rs[p];
+      const double v0 = a.vd[cur + p];
+      const double corr = __dadd_rn(__dmul_rn(c, (double)k), __dmul_rn(__dsub_rn(sbg, beta), v0));
+      const double t = __dsub_rn(__dadd_rn((double)rsum.x, (double)rsum.y), corr);
+      a.y[p] = t;
+      py[0] = __dadd_rn(py[0], __dmul_rn(t, t));
+    }
+    block_partials<1>(py, a.parts, 1, aw);
+    double ty[1];
+    if (!group_sync_reduce<1>(g, nb, b0, a.parts, 1, a.limit_ns, ty)) return false;
+    if (threadIdx.x == 0) {
+      scal[1] = sqrt(ty[0]);  // VectorNorm (:383-389)
+      scal[2] = 1.0 / scal[1];
+    }
+    __syncthreads();
+    vn = scal[1];
+    const double inv = scal[2];
+    // v = y / |y|, |v - v0|^2, |v + v0|^2, v.k (:349-357, :333-335); the
+    // block's own positions, so no cross-block read
+    double pe[3] = {0, 0, 0};
+    for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
+      const int i = a.rows[p];
+      const double x = __dmul_rn(a.y[p], inv);  // y / |y| through the reciprocal
+      const double old = a.vd[cur + p];
+      a.vd[nxt + p] = x;
+      a.vf[nxt + p] = mod_split(x);
+      const double d = __dsub_rn(x, old), s = __dadd_rn(x, old);
+      pe[0] = __dadd_rn(pe[0], __dmul_rn(d, d));
+      pe[1] = __dadd_rn(pe[1], __dmul_rn(s, s));
+      pe[2] = __dadd_rn(pe[2], __dmul_rn(x, (double)(a.rp[i + 1] - a.rp[i])));
+    }
+    block_partials<3>(pe, a.parts, 2, aw);
+    double te[3];
+    if (!group_sync_reduce<3>(g, nb, b0, a.parts, 2, a.limit_ns, te)) return false;
+    if (threadIdx.x == 0) {
+      scal[0] = sqrt(te[0]);
+      scal[3] = sqrt(te[1]);
+    }
+    __syncthreads();
+    err1 = scal[0];
+    err2 = scal[3];
+    vk = te[2];
+    __syncthreads();  // scal[0] is rewritten at the next step's start
+    ++it;
+  }
+  // eigenvalue sign (:369-375): the first node of G with the largest |v|
+  // (node 0 when none exceeds |v[0]|, v[0] taken as 0 off G); side sizes (:276-281)
+  const size_t fin = (size_t)(it & 1) * a.nrows, prv = (size_t)((it + 1) & 1) * a.nrows;
+  double best = 0.0;
+  int bq = 0x7fffffff;  // position of the maximum (positions ascend with node index)
+  long long sp = 0, sn = 0;
+  for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
+    const double v = a.vd[fin + p];
+    const double av = fabs(v);
+    if (av > best) {  // ascending positions per thread: the first maximum is kept
+      best = av;
+      bq = p;
+    }
+    sp += v > 0;
+    sn += v <= 0;
+  }
+  // warp butterflies (largest |v|, then the smaller position), warps in order
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oq = __shfl_xor_sync(0xffffffffu, bq, o);
+    if (ob > best || (ob == best && oq < bq)) {
+      best = ob;
+      bq = oq;
+    }
+    sp += __shfl_xor_sync(0xffffffffu, sp, o);
+    sn += __shfl_xor_sync(0xffffffffu, sn, o);
+  }
+  __shared__ double sb[kModWarps];
+  __shared__ int si[kModWarps];
+  __shared__ long long sps[kModWarps], sns[kModWarps];
+  if (lane == 0) {
+    sb[warp] = best;
+    si[warp] = bq;
+    sps[warp] = sp;
+    sns[warp] = sn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kModWarps; ++w) {
+      if (sb[w] > sb[0] || (sb[w] == sb[0] && si[w] < si[0])) {
+        sb[0] = sb[w];
+        si[0] = si[w];
+      }
+      sps[0] += sps[w];
+      sns[0] += sns[w];
+    }
+    double* pp = a.parts + (size_t)blockIdx.x * kModParts;
+    pp[8] = sb[0];
+    pp[9] = (double)si[0];
+    pp[10] = (double)sps[0];  // counts < 2^53: exact in a double
+    pp[11] = (double)sns[0];
+  }
+  if (!group_barrier(g, nb, a.limit_ns)) return false;
+  double gb = 0.0;
+  int gq = 0x7fffffff;
+  long long gp = 0, gn = 0;
+  for (int b = 0; b < nb; ++b) {  // fixed order, every block alike
+    const double* pp = a.parts + (size_t)(b0 + b) * kModParts;
+    const double ob = __ldcg(pp + 8);
+    const int oi = (int)__ldcg(pp + 9);
+    if (ob > gb || (ob == gb && oi < gq)) {
+      gb = ob;
+      gq = oi;
+    }
+    gp += (long long)__ldcg(pp + 10);
+    gn += (long long)__ldcg(pp + 11);
+  }
+  double prod = 0.0;
+  if (gb > 0.0) {
+    prod = __ldcg(a.vd + fin + gq) * __ldcg(a.vd + prv + gq);
+  } else if (__ldg(a.label) == r) {  // max_index stays 0, node 0 in G: its position is off
+    prod = __ldcg(a.vd + fin + off) * __ldcg(a.vd + prv + off);
+  }
+  *lambda = prod > 0 ? vn : -vn;
+  *iters = it;
+  *resid = err1 < err2 ? err1 : err2;
+  *fbuf = it & 1;
+  *subp = gp;
+  *subn = gn;
+  // the next call rewrites the iterate: wait until every block has read it
+  return group_barrier(g, nb, a.limit_ns);
+}
+
+// One tree level: every group's Sub_Partition (Modularity_CPU.cpp:250-285)
+// up to the division test, which the host takes in round order.
+__global__ __launch_bounds__(kModThreads, 1) void mod_level_kernel(ModArgs a) {
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  const int gidx = a.blk_grp[blockIdx.x];
+  ModGroup* g = a.groups + gidx;
+  const int r = g->label, b0 = g->blk0, nb = g->nblk, lb = blockIdx.x - b0;
+  const int off = g->row_off, nr = g->rows;
+  const long long kg = g->kg;
+  // this block's positions: an equal share of (positions + in-group edges)
+  __shared__ int range_s[2];
+  if (threadIdx.x < 2) {
+    const long long e0 = a.lrp[off];
+    const long long W = (long long)nr + (a.lrp[off + nr] - e0);
+    const long long t = W * (lb + (int)threadIdx.x) / nb;
+    int lo = 0, hi = nr;  // first q with q + lrp[off + q] - e0 >= t
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if ((long long)mid + (a.lrp[off + mid] - e0) >= t) hi = mid;
+      else lo = mid + 1;
+    }
+    range_s[threadIdx.x] = off + lo;
+  }
+  __syncthreads();
+  const int p0 = range_s[0], p1 = lb == nb - 1 ? off + nr : range_s[1];
+  float2* stage = (nr <= a.stage_max) ? reinterpret_cast<float2*>(dyn_smem) : nullptr;
+  // the block's in-group columns, kept in shared memory for the whole launch
+  // when they fit (every power step reads them)
+  const int eb0 = a.lrp[p0], ne = a.lrp[p1] - eb0;
+  uint16_t* s16 = nullptr;
+  int32_t* s32 = nullptr;
+  if (ne <= a.ecap) {
+    if (a.e16) {
+      s16 = reinterpret_cast<uint16_t*>(dyn_smem + a.stage_bytes);
+      for (int e = threadIdx.x; e < ne; e += kModThreads) s16[e] = (uint16_t)__ldg(a.lci + eb0 + e);
+    } else {
+      s32 = reinterpret_cast<int32_t*>(dyn_smem + a.stage_bytes);
+      for (int e = threadIdx.x; e < ne; e += kModThreads) s32[e] = __ldg(a.lci + eb0 + e);
+    }
+  }
+  __syncthreads();
+  double lambda = 0, l2 = 0, res = 0;
+  int its = 0, fb = 0;
+  long long sp = 0, sn = 0;
+  if (!lead_vector(a, g, r, b0, nb, p0, p1, kg, 0.0, stage, s16, s32, &lambda, &its, &res, &fb,
+                   &sp, &sn))
+    return;
+  if (lb == 0 && threadIdx.x == 0) {
+    g->iters[0] = its;
+    g->resid[0] = res;
+    g->iters[1] = 0;
+    g->resid[1] = 0;
+  }
+  if (lambda < 0) {  // the leading eigenvalue of B - lambda I (:271-272)
+    if (!lead_vector(a, g, r, b0, nb, p0, p1, kg, -lambda, stage, s16, s32, &l2, &its, &res, &fb,
+                     &sp, &sn))
+      return;
+    lambda += l2;
+    if (lb == 0 && threadIdx.x == 0) {
+      g->iters[1] = its;
+      g->resid[1] = res;
+    }
+  }
+  if (lb == 0 && threadIdx.x == 0) {
+    g->lambda = lambda;
+    g->subp = sp;
+    g->subn = sn;
+    g->fbuf = fb;
+  }
+}
+
+// A division (:285-287): the group's nodes go to base + 1 or base + 2 by the
+// sign of v * (subP - subN + 0.5).
+struct ModAssign {
+  int row_off, rows, fbuf, base;
+  double w;
+};
+
+__global__ void mod_assign_kernel(int nrows, const int32_t* __restrict__ rows,
+                                  const ModAssign* __restrict__ as, int nas,
+                                  const double* __restrict__ vd, int32_t* __restrict__ label) {
+  for (int k = blockIdx.y; k < nas; k += gridDim.y) {
+    const ModAssign s = as[k];
+    const double* v = vd + (size_t)s.fbuf * nrows;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < s.rows; q += gridDim.x * blockDim.x) {
+      const int p = s.row_off + q;
+      label[rows[p]] = s.base + 1 + (v[p] * s.w <= 0 ? 1 : 0);
+    }
+  }
 }
 
 // Q's counts: directed entries inside a module (warp per row) and the degree
 // sum of every module (labels < nlab), both integer.
 __global__ void mod_q_kernel(int n, const int32_t* __restrict__ rp,
                              const int32_t* __restrict__ ci, const int32_t* __restrict__ label,
-                             long long* __restrict__ kmod, ModState* st) {
+                             unsigned long long* __restrict__ kmod,
+                             unsigned long long* __restrict__ same_out) {
   const int lane = threadIdx.x & 31;
   long long same = 0;
   for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n;
@@ -323,11 +658,11 @@ __global__ void mod_q_kernel(int n, const int32_t* __restrict__ rp,
     const int b = rp[i], e = rp[i + 1];
     const int li = label[i];
     for (int k = b + lane; k < e; k += 32) same += label[ci[k]] == li;
-    if (lane == 0) atomicAdd((unsigned long long*)&kmod[li], (unsigned long long)(e - b));
+    if (lane == 0) atomicAdd(&kmod[li], (unsigned long long)(e - b));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) same += __shfl_xor_sync(0xffffffffu, same, o);
-  if (lane == 0 && same) atomicAdd((unsigned long long*)&st->same, (unsigned long long)same);
+  if (lane == 0 && same) atomicAdd(same_out, (unsigned long long)same);
 }
 
 // Final labels: the consecutive module numbers of the rounds that stopped.
@@ -337,21 +672,96 @@ __global__ void mod_map_kernel(int n, const int32_t* __restrict__ label,
     out[i] = adj[label[i]];
 }
 
-// ---- launchers ------------------------------------------------------------------
+// ---- host side -----------------------------------------------------------------
 
-size_t mod_state_bytes() { return sizeof(ModState); }
+size_t mod_group_bytes() { return sizeof(ModGroup); }
+size_t mod_assign_bytes() { return sizeof(ModAssign); }
+int mod_parts_per_block() { return kModParts; }
 
-void mod_state_read(const void* h, long long* numg, long long* kg, int* iter, int* done,
-                    double* lambda, long long* subp, long long* subn, long long* same) {
-  const ModState* s = (const ModState*)h;
-  if (numg) *numg = s->numg;
-  if (kg) *kg = s->kg;
-  if (iter) *iter = s->iter;
-  if (done) *done = s->done;
-  if (lambda) *lambda = s->lambda;
-  if (subp) *subp = s->subp;
-  if (subn) *subn = s->subn;
-  if (same) *same = s->same;
+// Blocks of mod_level_kernel that fit on the device at once (cooperative
+// launch) with `smem` bytes of staged iterate per block.
+int mod_level_grid(int sms, size_t smem) {
+  if (cudaFuncSetAttribute(mod_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kModSmemMax) != cudaSuccess) {  // per device: set every call
+    cudaGetLastError();
+    return 0;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mod_level_kernel, kModThreads,
+                                                    smem) != cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per_sm * sms;
+}
+
+int mod_stage_max() { return kModStageMax; }
+int mod_smem_max() { return kModSmemMax; }
+
+// Host view of a group record: host-written fields in, results out.
+void mod_group_set(void* rec, int label, int row_off, int rows, int blk0, int nblk, long long kg) {
+  ModGroup g{};
+  g.label = label;
+  g.row_off = row_off;
+  g.rows = rows;
+  g.blk0 = blk0;
+  g.nblk = nblk;
+  g.kg = kg;
+  *(ModGroup*)rec = g;
+}
+
+void mod_group_get(const void* rec, int* err, int iters[2], double resid[2], double* lambda,
+                   long long* subp, long long* subn, int* fbuf) {
+  const ModGroup* g = (const ModGroup*)rec;
+  *err = g->err;
+  iters[0] = g->iters[0];
+  iters[1] = g->iters[1];
+  resid[0] = g->resid[0];
+  resid[1] = g->resid[1];
+  *lambda = g->lambda;
+  *subp = g->subp;
+  *subn = g->subn;
+  *fbuf = g->fbuf;
+}
+
+void mod_assign_set(void* rec, int row_off, int rows, int fbuf, int base, double w) {
+  ModAssign s{row_off, rows, fbuf, base, w};
+  *(ModAssign*)rec = s;
+}
+
+cudaError_t launch_mod_build(int nrows, const int32_t* rows, const int32_t* rp,
+                             const int32_t* ci, const int32_t* label, const int32_t* loc,
+                             int32_t* cnt, int32_t* lrp, int32_t* lci, int sms, cudaStream_t s) {
+  const int grid = (int)std::min<long long>(((long long)nrows + 7) / 8, (long long)sms * 16);
+  mod_count_kernel<<<grid, 256, 0, s>>>(nrows, rows, rp, ci, label, cnt);
+  mod_scan_kernel<<<1, 1024, 0, s>>>(nrows, cnt, lrp);
+  mod_fill_kernel<<<grid, 256, 0, s>>>(nrows, rows, rp, ci, label, loc, lrp, lci);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mod_level(int n, long long M, const int32_t* rp, const int32_t* label,
+                             const int32_t* rows, const int32_t* lrp, const int32_t* lci,
+                             void* groups, const int32_t* blk_grp, double* vd, float2* vf,
+                             float2* rs, double* y, double* parts, int nrows, int stage_max,
+                             int stage_bytes, int ecap, int e16, size_t smem, int grid,
+                             int max_iter, double eps, cudaStream_t s) {
+  ModArgs a{n,        M,           rp,   label, rows,  lrp,      lci,
+            (ModGroup*)groups, blk_grp, vd, vf, rs,    y,        parts,
+            nrows,    stage_max,   stage_bytes, ecap, e16, max_iter, eps,
+            2000000000ull};
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((const void*)mod_level_kernel, dim3(grid), dim3(kModThreads),
+                                     args, smem, s);
+}
+
+cudaError_t launch_mod_assign(int nrows, const int32_t* rows, const void* as, int nas,
+                              const double* vd, int32_t* label, cudaStream_t s) {
+  if (nas <= 0) return cudaSuccess;
+  const int gy = nas < 65535 ? nas : 65535;
+  mod_assign_kernel<<<dim3(8, gy), 256, 0, s>>>(nrows, rows, (const ModAssign*)as, nas, vd,
+                                                label);
+  return cudaGetLastError();
 }
 
 static int mod_grid(int n, int per_block, int sms) {
@@ -360,57 +770,10 @@ static int mod_grid(int n, int per_block, int sms) {
   return (int)(want < 1 ? 1 : want < cap ? want : cap);
 }
 
-cudaError_t launch_mod_round(int n, const int32_t* label, int round, const int32_t* rp,
-                             uint8_t* g, void* st, int sms, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(st, 0, sizeof(ModState), s);
-  if (e != cudaSuccess) return e;
-  mod_round_kernel<<<mod_grid(n, 256, sms), 256, 0, s>>>(n, label, round, rp, g, (ModState*)st);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_mod_sumbg(int n, const int32_t* rp, const int32_t* ci, const uint8_t* g,
-                             long long M, const void* st, double* sumbg, int sms, cudaStream_t s) {
-  mod_sumbg_kernel<<<mod_grid(n, 8, sms), 256, 0, s>>>(n, rp, ci, g, M, (const ModState*)st,
-                                                       sumbg);
-  return cudaGetLastError();
-}
-
-int mod_grid_blocks(int sms) { return sms * 4; }
-
-cudaError_t launch_mod_init(int n, const uint8_t* g, const int32_t* rp, double* v, double* parts,
-                            void* st, double beta, int max_iter, double eps, int sms,
-                            cudaStream_t s) {
-  mod_init_kernel<<<mod_grid_blocks(sms), kModThreads, 0, s>>>(n, g, rp, v, parts, (ModState*)st,
-                                                               beta, max_iter, eps);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_mod_step(int n, long long M, const int32_t* rp, const int32_t* ci,
-                            const uint8_t* g, const double* sumbg, const double* v0, double* y,
-                            double* v, double* parts, void* st, int sms, cudaStream_t s) {
-  const int grid = mod_grid_blocks(sms);
-  mod_spmv_kernel<<<grid, kModThreads, 0, s>>>(n, M, rp, ci, g, sumbg, v0, y, parts,
-                                               (ModState*)st);
-  mod_norm_kernel<<<grid, kModThreads, 0, s>>>(n, rp, g, y, v0, v, parts, (ModState*)st);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_mod_final(int n, const uint8_t* g, const double* v, const double* v0, void* st,
-                             cudaStream_t s) {
-  mod_final_kernel<<<1, 1024, 0, s>>>(n, g, v, v0, (ModState*)st);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_mod_assign(int n, const uint8_t* g, const double* v, int maxres,
-                              long long subp, long long subn, int32_t* label, int sms,
-                              cudaStream_t s) {
-  mod_assign_kernel<<<mod_grid(n, 256, sms), 256, 0, s>>>(n, g, v, maxres, subp, subn, label);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_mod_q(int n, const int32_t* rp, const int32_t* ci, const int32_t* label,
-                         long long* kmod, void* st, int sms, cudaStream_t s) {
-  mod_q_kernel<<<mod_grid(n, 8, sms), 256, 0, s>>>(n, rp, ci, label, kmod, (ModState*)st);
+                         unsigned long long* kmod, unsigned long long* same, int sms,
+                         cudaStream_t s) {
+  mod_q_kernel<<<mod_grid(n, 8, sms), 256, 0, s>>>(n, rp, ci, label, kmod, same);
   return cudaGetLastError();
 }
 

@@ -320,9 +320,24 @@ int32_t bna_degree(const bna_csr* csr_dev, float* deg_dev, void* stream);
  * both sides hold more than one node.  labels_dev (n int32, device): module
  * of every vertex, 1-based, numbered in the order the modules stopped
  * dividing; *modules: their count; *q: the modularity Q (NaN without edges,
- * where the reference divides by zero).  Column order within rows is free. */
+ * where the reference divides by zero).  Column order within rows is free.
+ * log (optional, host, log_cap entries): one record per round that held
+ * nodes, in the reference's round order — what its _modu.txt log prints
+ * (Modularity_CPU.cpp:196-203, 268-283, 362-363); *log_n (optional): the
+ * number of such rounds, also when it exceeds log_cap. */
+typedef struct bna_mod_round {
+  int32_t round;       /* the label being divided (Partition's Round) */
+  int32_t nodes;       /* its node count (NumG) */
+  int32_t iters[2];    /* power steps of Lead_Vector: first call, retry with
+                          beta = -lambda (0 when lambda >= 0) */
+  double residual[2];  /* min(err1, err2) when each call stopped */
+  double lambda;       /* the eigenvalue the division test uses */
+  int32_t divided;     /* 1: split in two (lambda > lambda_min, both sides > 1 node) */
+  int32_t reserved;
+} bna_mod_round;
 int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr_dev, double lambda_min,
-                       int32_t* labels_dev, int32_t* modules, double* q, void* stream);
+                       int32_t* labels_dev, int32_t* modules, double* q, bna_mod_round* log,
+                       int32_t log_cap, int32_t* log_n, void* stream);
 /* _modu.nm file (Modularity_CPU.cpp:122-131): int32 N; float labels[N]. */
 int32_t bna_modu_write(const char* path, const int32_t* labels_host, int32_t N);
 

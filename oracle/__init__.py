@@ -58,7 +58,7 @@ def lib():
         o.orc_avg_accumulate.argtypes = [P, C.c_int64, C.c_int, P]
         o.orc_avg_finalize.argtypes = [P, C.c_int64, C.c_int, C.c_int]
         o.orc_modularity.argtypes = [P, P, C.c_int, C.c_double, P, C.POINTER(C.c_double),
-                                     C.POINTER(C.c_int)]
+                                     C.POINTER(C.c_int), P, C.POINTER(C.c_int)]
         o.orc_modularity.restype = C.c_int
         _o = o
     return _o
@@ -107,16 +107,23 @@ def ref_m():
     return _rm
 
 
-def modularity(R, Cc, lambda_min: float = 0.001):
+def modularity(R, Cc, lambda_min: float = 0.001, log: list | None = None):
     """-> (labels int32 [N], Q, modules, rounds): the restatement of the
-    reference's spectral bisection (binary graph of R, C)."""
+    reference's spectral bisection (binary graph of R, C).  With `log` (a
+    list), one dict per round that held nodes is appended: round, nodes,
+    iters (per Lead_Vector call), lambda, divided."""
     R = np.ascontiguousarray(R, np.int32)
     Cc = np.ascontiguousarray(Cc, np.int32)
     N = len(R) - 1
     labels = np.empty(N, np.int32)
-    q, rounds = C.c_double(), C.c_int()
+    q, rounds, nlog = C.c_double(), C.c_int(), C.c_int()
+    buf = np.zeros((2 * N + 2, 6)) if log is not None else None
     m = lib().orc_modularity(_p(R), _p(Cc), N, lambda_min, _p(labels), C.byref(q),
-                             C.byref(rounds))
+                             C.byref(rounds), _p(buf), C.byref(nlog))
+    if log is not None:
+        for e in buf[:nlog.value]:
+            log.append({"round": int(e[0]), "nodes": int(e[1]), "iters": [int(e[2]), int(e[3])],
+                        "lambda": float(e[4]), "divided": bool(e[5])})
     return labels, q.value, m, rounds.value
 
 

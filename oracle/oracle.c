@@ -490,9 +490,13 @@ static double mod_lead_vector(const int32_t* R, const int32_t* C, int N, long lo
   return (v[mi] * v0[mi] > 0) ? vnorm : -vnorm;
 }
 
+/* log (optional, 6 doubles per round that held nodes, at most 2N + 2 rounds):
+ * round, nodes, iterations of the first and of the retried Lead_Vector call
+ * (0: none), lambda, divided. */
 int orc_modularity(const int32_t* R, const int32_t* C, int N, double lambda_min, int32_t* labels,
-                   double* q_out, int* rounds_out) {
+                   double* q_out, int* rounds_out, double* log, int* log_n) {
   const long long M = (R[N] - R[0]) / 2;
+  if (log_n) *log_n = 0;
   if (M == 0) { /* no edge: the reference divides by M = 0; one module, Q undefined */
     for (int i = 0; i < N; ++i) labels[i] = 1;
     *q_out = NAN;
@@ -523,15 +527,24 @@ int orc_modularity(const int32_t* R, const int32_t* C, int N, double lambda_min,
         for (int32_t j = R[i]; j < R[i + 1]; ++j) in += g[C[j]];
         sumbg[i] = (double)(in - (long long)(R[i + 1] - R[i]) * kg / 2 / M);
       }
-      int it;
+      int it = 0, it2 = 0;
       double lambda = mod_lead_vector(R, C, N, M, sumbg, g, 0.0, v, v0, verr, &it);
-      if (lambda < 0) lambda += mod_lead_vector(R, C, N, M, sumbg, g, -lambda, v, v0, verr, &it);
+      if (lambda < 0) lambda += mod_lead_vector(R, C, N, M, sumbg, g, -lambda, v, v0, verr, &it2);
       long long subn = 0, subp = 0;
       for (int i = 0; i < N; ++i) {
         subp += g[i] && v[i] > 0;
         subn += g[i] && v[i] <= 0;
       }
       const int issub = lambda > lambda_min && subp > 1 && subn > 1;
+      if (log && log_n) {
+        double* e = log + 6 * (size_t)(*log_n)++;
+        e[0] = round;
+        e[1] = numg;
+        e[2] = it;
+        e[3] = it2;
+        e[4] = lambda;
+        e[5] = issub;
+      }
       if (issub) {
         for (int i = 0; i < N; ++i)
           if (g[i]) res[i] = max_result + 1 + (v[i] * ((double)(subp - subn) + 0.5) <= 0);

@@ -114,3 +114,28 @@ def test_degree_tool_and_api(tmp_path, builder):
     assert np.array_equal(builder.degree(binres).cpu().numpy(),
                           np.diff(g.row_ptr).astype(np.float32))
 
+
+
+def test_modularity_tool(tmp_path):
+    """Modularity tool (U/Newman_Modularity_CPU/Modularity_CPU/Modularity_CPU.cpp
+    main :35-162): <name>_modu.nm holds the reference's own labels as floats;
+    <name>_modu.txt logs every round and, per network (the real one, then each
+    random rewiring), the module count and Q."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "modularity_ref.npz"))
+    R, C = g["planted300_R"], g["planted300_C"]
+    bna.csr_write(str(tmp_path / "p.csr"), R, C, None)
+    out = _run("bna_modularity", tmp_path, 2)
+    raw = np.fromfile(tmp_path / "p_modu.nm", np.int32, count=1)
+    lab = np.fromfile(tmp_path / "p_modu.nm", np.float32, offset=4)
+    assert raw[0] == len(R) - 1
+    assert np.array_equal(lab, g["planted300_labels"].astype(np.float32))
+    log = (tmp_path / "p_modu.txt").read_text()
+    _, q_o, m_o, _ = oracle.modularity(R, C)
+    heads = re.findall(r"Number of Modules: (\d+),\tQ=([-\d.e+]+)", log)
+    assert len(heads) == 3, log
+    assert int(heads[0][0]) == m_o and abs(float(heads[0][1]) - q_o) <= 1e-5 * abs(q_o)
+    # the random networks are less modular than the planted one
+    assert all(float(q) < q_o for _, q in heads[1:])
+    rounds = re.findall(r"Round:\t(\d+)\tnumber of nodes:\t(\d+)\t", log)
+    assert rounds[0] == ("0", str(len(R) - 1)) and "Divide?: 1" in log
+    assert "Save partition results as" in out

@@ -549,11 +549,25 @@ def test_modularity_matches_reference_golden(builder, name):
     else:
         R, C = g[name + "_R"], g[name + "_C"]
     csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), None, {})
-    labels, m, q = builder.modularity(csr)
+    log = []
+    labels, m, q = builder.modularity(csr, log=log)
     assert m == int(g[name + "_modules"])
     assert np.array_equal(labels.cpu().numpy(), g[name + "_labels"])
-    _, q_o, _, _ = oracle.modularity(R, C)
+    log_o = []
+    _, q_o, _, _ = oracle.modularity(R, C, log=log_o)
     assert abs(q - q_o) <= 1e-9 * abs(q_o)
+    _same_rounds(log, log_o)
+
+
+def _same_rounds(log, log_o):
+    """Round records of the device run against the oracle's: the same rounds,
+    node counts and decisions; power-step counts within one step of the
+    oracle's (the FP64 sums run in another order) and eigenvalues within 1e-6."""
+    assert len(log) == len(log_o)
+    for a, b in zip(log, log_o):
+        assert (a["round"], a["nodes"], a["divided"]) == (b["round"], b["nodes"], b["divided"])
+        assert all(abs(x - y) <= 1 for x, y in zip(a["iters"], b["iters"])), (a, b)
+        assert abs(a["lambda"] - b["lambda"]) <= 1e-6 * max(1.0, abs(b["lambda"])), (a, b)
 
 
 def test_modularity_of_a_correlation_network(builder):
@@ -562,10 +576,12 @@ def test_modularity_of_a_correlation_network(builder):
     b = bna.synth_bold(6000, 240, 12, 41)
     res = builder.corr_csr(dev(b), mode="r_gt", value=0.45, precision="bf16x3")
     h = res.numpy()
-    labels, m, q = builder.modularity(res)
-    lab_o, q_o, m_o, _ = oracle.modularity(h.row_ptr, h.col_idx)
+    log, log_o = [], []
+    labels, m, q = builder.modularity(res, log=log)
+    lab_o, q_o, m_o, _ = oracle.modularity(h.row_ptr, h.col_idx, log=log_o)
     assert m == m_o and np.array_equal(labels.cpu().numpy(), lab_o)
     assert abs(q - q_o) <= 1e-9 * abs(q_o)
+    _same_rounds(log, log_o)
 
 
 def test_modularity_without_edges(builder):
