@@ -313,6 +313,68 @@ def batch_run(n_subjects: int, precision: str = "auto", plain: bool = True) -> d
     return out
 
 
+def mod_levels(log):
+    """Critical path of a modularity run: rounds are the nodes of a binary
+    tree visited breadth first (a division of round r numbers its children
+    maxres + 1, maxres + 2); the rounds of one tree level run side by side, so
+    the level's longest round (power steps of both Lead_Vector calls) bounds it."""
+    level = {0: 0}
+    maxres = 0
+    per_level = {}
+    for e in log:
+        lv = level.get(e["round"], 0)
+        per_level[lv] = max(per_level.get(lv, 0), sum(e["iters"]))
+        if e["divided"]:
+            level[maxres + 1] = level[maxres + 2] = lv + 1
+            maxres += 2
+    return sum(per_level.values()), len(per_level)
+
+
+def modularity_run(b, csr, stream, reps: int = 2) -> dict:
+    """Newman modularity of a device CSR's binary graph, CUDA-event timed."""
+    import torch
+    times = []
+    for _ in range(reps):
+        log = []
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        labels, m, q = b.modularity(csr, log=log)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    crit, levels = mod_levels(log)
+    ms = statistics.median(times)
+    return {"ms": ms, "modules": m, "Q": q, "rounds": len(log),
+            "power_steps": sum(sum(e["iters"]) for e in log), "tree_levels": levels,
+            "critical_path_steps": crit, "us_per_critical_step": ms * 1e3 / max(crit, 1),
+            "labels": labels}
+
+
+def modularity_small_pair(b, stream) -> dict:
+    """The small workload's binary CSR (N=4,096, r >= 0.5): the device
+    modularity against the reference tool's CPU arithmetic (the C restatement,
+    one thread) on the same graph, whole runs on both sides."""
+    import numpy as np
+    import torch
+    import oracle
+    from cuda_newest20160331_gb300 import workloads
+    ws = workloads.get("small")
+    bs = torch.from_numpy(ws.bold()).cuda()
+    csr = b.corr_csr(bs, mode=ws.mode, value=ws.value, precision="bf16x3", weighted=False,
+                     copy=True)
+    g = modularity_run(b, csr, stream, reps=1)
+    h = csr.numpy()
+    t0 = time.perf_counter()
+    lab_o, q_o, m_o, _ = oracle.modularity(h.row_ptr, h.col_idx)
+    cpu_s = time.perf_counter() - t0
+    same = bool(np.array_equal(g.pop("labels").cpu().numpy(), lab_o))
+    return {"workload": f"small: N={ws.N} T={ws.T} r>=0.5 binary, nnz={csr.nnz}",
+            "gpu_ms": g["ms"], "cpu_ms": cpu_s * 1e3, "cpu_cores": 1, "cpu_kind": "port",
+            "modules": g["modules"], "labels_equal": same,
+            "critical_path_steps": g["critical_path_steps"], "power_steps": g["power_steps"]}
+
+
 def load_traffic(kernel: str, workload: str):
     """DRAM bytes per launch of `kernel` on `workload` from one ncu capture
     (profiles/traffic.txt: `kernel:workload bytes` lines), or None."""
@@ -453,6 +515,11 @@ def main():
                "converged": conv,
                "hbm_gbs_per_iteration": (8.0 * csr_dev.nnz + 4.0 * (N + 1) + 16.0 * N) * iters
                / (statistics.median(ec_ms) / 1000.0) / 1e9 if iters else None}
+    # Newman modularity of the same CSR's binary graph (values ignored, as the
+    # reference tool reads only R and C)
+    mod_info = modularity_run(b, csr_dev, stream)
+    mod_info.pop("labels")
+    mod_info["workload"] = f"{w.name} CSR, binary view (nnz={csr_dev.nnz})"
     del csr_dev
 
     # the other forms on the same input, same edge set (3 timed steps each):
@@ -542,6 +609,7 @@ def main():
         "plain_fp32": plain,
         ("tf32" if precision == "bf16x3" else "bf16x3"): other_tc,
         "ec": ec_info,
+        "modularity": mod_info,
         "e2e": {"value": world * he_nnz / (e2e / 1000.0), "unit": "edges/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms": e2e},
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
@@ -553,6 +621,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_sample(w, bold_h, args.cpu_seconds, host_cores())
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["modularity"]["small_vs_cpu"] = modularity_small_pair(b, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     b.close()

@@ -83,6 +83,7 @@ __device__ __forceinline__ void mod_two_sum(float a, float b, float& s, float& e
 __device__ __forceinline__ bool group_barrier(ModGroup* g, int nb, uint64_t limit_ns) {
   __shared__ int ok_s;
   __syncthreads();
+  if (nb == 1) return true;  // a group of one block: its own barrier suffices
   if (threadIdx.x == 0) {
     volatile unsigned int* gen = &g->bar_gen;
     const unsigned int g0 = *gen;  // cannot advance before this block arrives
@@ -118,8 +119,10 @@ __device__ __forceinline__ bool group_barrier(ModGroup* g, int nb, uint64_t limi
 // `aw` warps can hold non-zero values (FP64 work is scarce on this GPU: the
 // other warps skip it).
 template <int W>
-__device__ __forceinline__ void block_partials(double (&a)[W], double* parts, int k0, int aw) {
+__device__ __forceinline__ void block_partials(double (&a)[W], double* parts, int k0, int aw,
+                                               double (&tot)[W]) {
   __shared__ double ws[kModWarps][W];
+  __shared__ double bt[W];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp < aw) {
 #pragma unroll
@@ -137,8 +140,11 @@ __device__ __forceinline__ void block_partials(double (&a)[W], double* parts, in
       double t = 0;
       for (int k = 0; k < aw; ++k) t += ws[k][w];
       parts[(size_t)blockIdx.x * kModParts + k0 + w] = t;
+      bt[w] = t;
     }
   __syncthreads();
+#pragma unroll
+  for (int w = 0; w < W; ++w) tot[w] = bt[w];
 }
 
 // Warps holding thread-per-position work for `cnt` positions.
@@ -361,25 +367,29 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   const int eb0 = __ldg(a.lrp + p0);
   // v = (G ? i : 0) (:322-324); v.k for the first step
   double p1s[1] = {0};
+  // a single-block group keeps its staged iterate current itself (no reload per step)
+  const bool self_stage = staged && nb == 1;
   for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
     const int i = a.rows[p];
     const double x = (double)i;
     a.vd[p] = x;
     a.vf[p] = mod_split(x);
+    if (self_stage) stage[p - off] = mod_split(x);
     p1s[0] += x * (double)(a.rp[i + 1] - a.rp[i]);
   }
   const int aw = active_warps(p1 - p0);
   __shared__ double scal[4];  // per-step scalars, computed by one thread
-  block_partials<1>(p1s, a.parts, 0, aw);
+  // a group of one block takes its own totals: no global barrier, no L2 round trip
   double t1[1];
-  if (!group_sync_reduce<1>(g, nb, b0, a.parts, 0, a.limit_ns, t1)) return false;
+  block_partials<1>(p1s, a.parts, 0, aw, t1);
+  if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 0, a.limit_ns, t1)) return false;
   double vk = t1[0];
   double err1 = 1, err2 = 1, vn = 0;
   int it = 0;
   while (err1 > a.eps && err2 > a.eps && it < a.max_iter) {
     const size_t cur = (size_t)(it & 1) * a.nrows, nxt = (size_t)((it + 1) & 1) * a.nrows;
     const float2* vfc = a.vf + cur + off;  // the group's iterate, group-local index
-    if (staged) {
+    if (staged && !self_stage) {
       for (int q = threadIdx.x; q < nr; q += kModThreads) stage[q] = __ldcg(vfc + q);
       __syncthreads();
     }
@@ -432,9 +442,9 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       a.y[p] = t;
       py[0] = __dadd_rn(py[0], __dmul_rn(t, t));
     }
-    block_partials<1>(py, a.parts, 1, aw);
     double ty[1];
-    if (!group_sync_reduce<1>(g, nb, b0, a.parts, 1, a.limit_ns, ty)) return false;
+    block_partials<1>(py, a.parts, 1, aw, ty);
+    if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 1, a.limit_ns, ty)) return false;
     if (threadIdx.x == 0) {
       scal[1] = sqrt(ty[0]);  // VectorNorm (:383-389)
       scal[2] = 1.0 / scal[1];
@@ -450,15 +460,17 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       const double x = __dmul_rn(a.y[p], inv);  // y / |y| through the reciprocal
       const double old = a.vd[cur + p];
       a.vd[nxt + p] = x;
-      a.vf[nxt + p] = mod_split(x);
+      const float2 xf = mod_split(x);
+      a.vf[nxt + p] = xf;
+      if (self_stage) stage[p - off] = xf;  // phase A of this step is over
       const double d = __dsub_rn(x, old), s = __dadd_rn(x, old);
       pe[0] = __dadd_rn(pe[0], __dmul_rn(d, d));
       pe[1] = __dadd_rn(pe[1], __dmul_rn(s, s));
       pe[2] = __dadd_rn(pe[2], __dmul_rn(x, (double)(a.rp[i + 1] - a.rp[i])));
     }
-    block_partials<3>(pe, a.parts, 2, aw);
     double te[3];
-    if (!group_sync_reduce<3>(g, nb, b0, a.parts, 2, a.limit_ns, te)) return false;
+    block_partials<3>(pe, a.parts, 2, aw, te);
+    if (nb > 1 && !group_sync_reduce<3>(g, nb, b0, a.parts, 2, a.limit_ns, te)) return false;
     if (threadIdx.x == 0) {
       scal[0] = sqrt(te[0]);
       scal[3] = sqrt(te[1]);
