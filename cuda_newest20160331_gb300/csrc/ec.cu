@@ -43,6 +43,8 @@ struct EcState {
   unsigned int counter;
   int err;                // bounded grid barrier expired (persistent kernel)
   unsigned int bar_count, bar_gen;  // grid barrier of the persistent kernel
+  double tot[5];          // persistent kernel: lam2, e1, e2, lambda, 1/lambda published by
+                          // the last block to reach the barrier
 };
 
 constexpr int kEcThreads = 256;
@@ -195,6 +197,102 @@ __device__ __forceinline__ void ec_row_accum(const int32_t* __restrict__ ci,
   }
 }
 
+// Rounds per batch: round k of a block covers rows blockIdx.x * 8 + k * (all
+// warps) .. + 7, one per warp (the interleaving spreads dense row ranges over
+// every block); the batch's float-float row sums wait in shared memory for the
+// thread-per-row FP64 epilogue, one thread per row.
+constexpr int kEcRounds = kEcThreads / (kEcThreads / 32);
+
+// One iteration's work of this block: warp per row for the float-float sums,
+// then one thread per row for the FP64 epilogue (y = sum / lambda, the
+// iterate copies, the partial sums of y^2, (y - u)^2, (y + u)^2).  The FP64
+// pipe of this GPU is narrow and a warp instruction costs it the same with
+// one lane as with 32, so the FP64 work runs on full warps instead of on
+// lane 0 of every row's warp.
+template <int VK>
+__device__ __forceinline__ void ec_block_rows(int n, const int32_t* __restrict__ rp,
+                                              const int32_t* __restrict__ ci,
+                                              const float* __restrict__ val,
+                                              const double* __restrict__ vald, long long nnz_used,
+                                              const double* uc, const float2* ufc, double* un,
+                                              float2* unf, double inv, bool l2_only, double& a0,
+                                              double& a1, double& a2) {
+  constexpr int kW = kEcThreads / 32;
+  __shared__ float2 rs[kEcThreads];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = gridDim.x * kW;
+  for (long long base = (long long)blockIdx.x * kW; base < n; base += (long long)kEcRounds * nw) {
+    for (int k = 0; k < kEcRounds; ++k) {
+      const long long row = base + (long long)k * nw + warp;
+      if (row >= n) break;  // later rounds of this warp are past n too
+      long long b = __ldg(rp + row), e = __ldg(rp + row + 1);
+      if (e > nnz_used) e = nnz_used;
+      float sh = 0.0f, sl = 0.0f;
+      ec_row_accum<VK>(ci, val, vald, ufc, b, e, lane, sh, sl, l2_only);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+        float s2, e2;
+        two_sum(sh, oh, s2, e2);
+        sh = s2;
+        sl = __fadd_rn(sl, __fadd_rn(ol, e2));
+      }
+      if (lane == 0) rs[k * kW + warp] = make_float2(sh, sl);
+    }
+    __syncthreads();
+    {
+      const int k = threadIdx.x / kW, w = threadIdx.x % kW;
+      const long long row = base + (long long)k * nw + w;
+      if (row < n) {
+        const float2 sm = rs[threadIdx.x];
+        const double y = ((double)sm.x + (double)sm.y) * inv;
+        const double old = l2_only ? __ldcg(uc + row) : uc[row];
+        un[row] = y;
+        unf[row] = split_df(y);
+        a0 += y * y;
+        const double d = y - old, p = y + old;
+        a1 += d * d;
+        a2 += p * p;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Block sums of the three partials (warp butterflies over the first aw warps,
+// then warps in order by thread 0) into parts[blockIdx.x * 3 ..].
+__device__ __forceinline__ void ec_block_partials(double a0, double a1, double a2, int aw,
+                                                  double* parts) {
+  __shared__ double ws[kEcThreads / 32][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < aw) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0) {
+      ws[warp][0] = a0;
+      ws[warp][1] = a1;
+      ws[warp][2] = a2;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int w = 0; w < aw; ++w) {
+      t0 += ws[w][0];
+      t1 += ws[w][1];
+      t2 += ws[w][2];
+    }
+    parts[blockIdx.x * 3 + 0] = t0;
+    parts[blockIdx.x * 3 + 1] = t1;
+    parts[blockIdx.x * 3 + 2] = t2;
+  }
+}
+
 // VK: 0 binary (val NULL), 1 float values, 2 double values (split into a float pair).
 template <int VK>
 __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
@@ -213,53 +311,9 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
   __syncthreads();
   const double lam = lam_s[0];
   const double inv = lam_s[1];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = gridDim.x * (kEcThreads / 32);
   double a0 = 0, a1 = 0, a2 = 0;
-  for (int row = blockIdx.x * (kEcThreads / 32) + warp; row < n; row += nwarps) {
-    long long b = rp[row], e = rp[row + 1];
-    if (e > nnz_used) e = nnz_used;
-    float sh = 0.0f, sl = 0.0f;
-    ec_row_accum<VK>(ci, val, vald, uf, b, e, lane, sh, sl, false);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
-      const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
-      float s2, e2;
-      two_sum(sh, oh, s2, e2);
-      sh = s2;
-      sl = __fadd_rn(sl, __fadd_rn(ol, e2));
-    }
-    if (lane == 0) {
-      const double s = (double)sh + (double)sl;
-      const double y = s * inv;
-      const double old = u[row];
-      un[row] = y;
-      unf[row] = split_df(y);
-      a0 += y * y;
-      const double d = y - old, p = y + old;
-      a1 += d * d;
-      a2 += p * p;
-    }
-  }
-  __shared__ double ws[kEcThreads / 32][3];
-  if (lane == 0) {
-    ws[warp][0] = a0;
-    ws[warp][1] = a1;
-    ws[warp][2] = a2;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0, t2 = 0;
-    for (int w = 0; w < kEcThreads / 32; ++w) {
-      t0 += ws[w][0];
-      t1 += ws[w][1];
-      t2 += ws[w][2];
-    }
-    parts[blockIdx.x * 3 + 0] = t0;
-    parts[blockIdx.x * 3 + 1] = t1;
-    parts[blockIdx.x * 3 + 2] = t2;
-  }
+  ec_block_rows<VK>(n, rp, ci, val, vald, nnz_used, u, uf, un, unf, inv, false, a0, a1, a2);
+  ec_block_partials(a0, a1, a2, kEcThreads / 32, parts);
   if (last_block_arrives(st)) {
     __shared__ double tot[3];
     reduce_partials(parts, gridDim.x, tot);
@@ -311,82 +365,41 @@ __device__ __forceinline__ bool grid_barrier(EcState* st, uint64_t limit_ns) {
   return ok_s != 0;
 }
 
-template <int VK>
-__global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
-    int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-    const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
-    double* u, float2* uf, double* parts, EcState* st, int it_end, int max_iter, double eps) {
-  __shared__ double ws[kEcThreads / 32][3];
-  __shared__ double red[kEcThreads][3];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = gridDim.x * (kEcThreads / 32);
-  // resume from the state block (ec_init_kernel's, or the previous segment's)
-  double lam2 = st->lam2, lam_used = st->lambda_used, e1 = st->e1, e2 = st->e2;
-  int it = st->iter;
-  if (st->done) it_end = it;
-  if (it_end > max_iter) it_end = max_iter;
-  __shared__ double lam_s[2];
-  while (it < it_end) {
-    if (threadIdx.x == 0) {
-      lam_s[0] = sqrt(lam2);
-      lam_s[1] = 1.0 / lam_s[0];
-    }
-    __syncthreads();
-    const double lam = lam_s[0];
-    const double inv = lam_s[1];
-    const size_t cur = (size_t)(it & 1) * n, nxt = (size_t)((it + 1) & 1) * n;
-    // the iterate was written by other blocks: read it from L2 (__ldcg), not L1
-    const double* uc = u + cur;
-    const float2* ufc = uf + cur;
-    double a0 = 0, a1 = 0, a2 = 0;
-    for (int row = blockIdx.x * (kEcThreads / 32) + warp; row < n; row += nwarps) {
-      long long b = __ldg(rp + row), e = __ldg(rp + row + 1);
-      if (e > nnz_used) e = nnz_used;
-      float sh = 0.0f, sl = 0.0f;
-      ec_row_accum<VK>(ci, val, vald, ufc, b, e, lane, sh, sl, true);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
-        const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
-        float s2, e2_;
-        two_sum(sh, oh, s2, e2_);
-        sh = s2;
-        sl = __fadd_rn(sl, __fadd_rn(ol, e2_));
-      }
-      if (lane == 0) {
-        const double y = ((double)sh + (double)sl) * inv;
-        const double old = __ldcg(uc + row);
-        u[nxt + row] = y;
-        uf[nxt + row] = split_df(y);
-        a0 += y * y;
-        const double d = y - old, p = y + old;
-        a1 += d * d;
-        a2 += p * p;
+// Grid barrier of the persistent kernel that also reduces the iteration's
+// block partials pp (grid x 3): the last block to arrive sums them in a fixed
+// order (thread-strided sums, then a shared-memory tree: the order of the
+// per-iteration kernel's reduce_partials), publishes lam2, e1, e2 and the next
+// iteration's lambda and 1/lambda in st->tot, and releases the others — each
+// partial is read once, not once per block.  Bounded like grid_barrier.
+__device__ __forceinline__ bool grid_sync_reduce(EcState* st, const double* pp,
+                                                 uint64_t limit_ns) {
+  __shared__ int last_s, ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &st->bar_gen;
+    const unsigned int g = *gen;  // the generation cannot advance before this block arrives
+    __threadfence();
+    const bool last = atomicAdd(&st->bar_count, 1u) == gridDim.x - 1;
+    last_s = last ? 1 : 0;
+    ok_s = 1;
+    if (!last) {
+      uint64_t t0;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+      while (*gen == g) {
+        uint64_t t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > limit_ns) {
+          ok_s = 0;
+          break;
+        }
+        __nanosleep(32);
       }
     }
-    if (lane == 0) {
-      ws[warp][0] = a0;
-      ws[warp][1] = a1;
-      ws[warp][2] = a2;
-    }
-    __syncthreads();
-    double* pp = parts + (size_t)(it & 1) * gridDim.x * 3;
-    if (threadIdx.x == 0) {
-      double t0 = 0, t1 = 0, t2 = 0;
-      for (int w = 0; w < kEcThreads / 32; ++w) {
-        t0 += ws[w][0];
-        t1 += ws[w][1];
-        t2 += ws[w][2];
-      }
-      pp[blockIdx.x * 3 + 0] = t0;
-      pp[blockIdx.x * 3 + 1] = t1;
-      pp[blockIdx.x * 3 + 2] = t2;
-    }
-    if (!grid_barrier(st, 2000000000ull)) {
-      if (threadIdx.x == 0) atomicOr(&st->err, 1);
-      return;
-    }
-    // every block reduces the partials in the same fixed order
+    __threadfence();
+  }
+  __syncthreads();
+  if (last_s) {
+    __shared__ double red[kEcThreads][3];
     double s0 = 0, s1 = 0, s2 = 0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
       s0 += __ldcg(pp + b * 3 + 0);
@@ -405,17 +418,58 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
       }
       __syncthreads();
     }
-    __shared__ double e_s[2];
     if (threadIdx.x == 0) {
-      e_s[0] = sqrt(red[0][1]);
-      e_s[1] = sqrt(red[0][2]);
+      st->tot[0] = red[0][0];
+      st->tot[1] = sqrt(red[0][1]);
+      st->tot[2] = sqrt(red[0][2]);
+      st->tot[3] = sqrt(red[0][0]);
+      st->tot[4] = 1.0 / st->tot[3];
+      st->bar_count = 0;
+      __threadfence();
+      atomicAdd(&st->bar_gen, 1u);
     }
     __syncthreads();
+    return true;
+  }
+  if (!ok_s && threadIdx.x == 0) atomicOr(&st->err, 1);
+  return ok_s != 0;
+}
+
+template <int VK>
+__global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
+    int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+    const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
+    double* u, float2* uf, double* parts, EcState* st, int it_end, int max_iter, double eps) {
+  // resume from the state block (ec_init_kernel's, or the previous segment's)
+  double lam2 = st->lam2, lam_used = st->lambda_used, e1 = st->e1, e2 = st->e2;
+  int it = st->iter;
+  if (st->done) it_end = it;
+  if (it_end > max_iter) it_end = max_iter;
+  // lambda and its reciprocal for the first iteration (FP64 sqrt and division
+  // are long instruction sequences on this GPU: one thread computes them)
+  __shared__ double lam_s[2];
+  if (threadIdx.x == 0) {
+    lam_s[0] = sqrt(lam2);
+    lam_s[1] = 1.0 / lam_s[0];
+  }
+  __syncthreads();
+  double lam = lam_s[0], inv = lam_s[1];
+  while (it < it_end) {
+    const size_t cur = (size_t)(it & 1) * n, nxt = (size_t)((it + 1) & 1) * n;
+    // the iterate was written by other blocks: read it from L2 (__ldcg), not L1
+    double a0 = 0, a1 = 0, a2 = 0;
+    ec_block_rows<VK>(n, rp, ci, val, vald, nnz_used, u + cur, uf + cur, u + nxt, uf + nxt, inv,
+                      true, a0, a1, a2);
+    double* pp = parts + (size_t)(it & 1) * gridDim.x * 3;
+    ec_block_partials(a0, a1, a2, kEcThreads / 32, pp);
+    if (!grid_sync_reduce(st, pp, 2000000000ull)) return;
+    // the totals: published by the last block (L2 reads; the same bits everywhere)
     lam_used = lam;
-    lam2 = red[0][0];
-    e1 = e_s[0];
-    e2 = e_s[1];
-    __syncthreads();  // red, lam_s and e_s are rewritten in the next iteration
+    lam2 = __ldcg(&st->tot[0]);
+    e1 = __ldcg(&st->tot[1]);
+    e2 = __ldcg(&st->tot[2]);
+    lam = __ldcg(&st->tot[3]);
+    inv = __ldcg(&st->tot[4]);
     ++it;
     if (e1 <= eps || e2 <= eps) break;
   }
