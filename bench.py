@@ -453,6 +453,12 @@ def main():
                               "value": sv["p99_ms"], "unit": "ms", "higher_is_better": False,
                               "n_gpus": 1, "serve": sv}), flush=True)
         return
+    # serving first, in a fresh device state: its requests then meet only one
+    # another (a builder context and its arena from the measurements below
+    # would share the device with them)
+    serve = None
+    if rank == 0 and args.serve_requests > 0:
+        serve = serve_run(args.serve_requests, slots=args.serve_slots, dump=args.serve_dump)
     w = workloads.get(args.workload)
     precision = args.precision
     bold_h = w.bold()
@@ -615,9 +621,8 @@ def main():
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "clocks": clk.summary(),
     }
-    if rank == 0 and args.serve_requests > 0:
-        line["serve"] = serve_run(args.serve_requests, slots=args.serve_slots,
-                                  dump=args.serve_dump)
+    if serve is not None:
+        line["serve"] = serve
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_sample(w, bold_h, args.cpu_seconds, host_cores())
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
