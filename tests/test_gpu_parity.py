@@ -95,6 +95,17 @@ def test_zscore_bit_exact_scanner_like_series(builder, kind):
     assert np.array_equal(z[:, :T], ref, equal_nan=True)
 
 
+def test_zscore_bit_exact_long_series(builder):
+    """24 M elements of long (T = 1,200), offset series: z equals the
+    reference's bit for bit."""
+    N, T = 20000, 1200
+    rng = np.random.default_rng(31)
+    b = bna.synth_bold(N, T, 30, 31)
+    b = (b * rng.uniform(1.0, 40.0, N) + rng.uniform(100.0, 5000.0, N)).astype(np.float32)
+    z = builder.zscore(dev(b)).cpu().numpy()
+    assert np.array_equal(z[:, :T], oracle.zscore(b), equal_nan=True)
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("N,T,mode,tau", [
     (2, 10, "r_gt", -1.0), (127, 33, "r_gt", 0.3), (128, 240, "r_ge", 0.2),
