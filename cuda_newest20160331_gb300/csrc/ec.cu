@@ -261,7 +261,7 @@ __device__ __forceinline__ void ec_block_rows(int n, const int32_t* __restrict__
 }
 
 // Block sums of the three partials (warp butterflies over the first aw warps,
-// then warps in order by thread 0) into parts[blockIdx.x * 3 ..].
+// then a butterfly over the warps' sums in warp 0) into parts[blockIdx.x * 3 ..].
 __device__ __forceinline__ void ec_block_partials(double a0, double a1, double a2, int aw,
                                                   double* parts) {
   __shared__ double ws[kEcThreads / 32][3];
@@ -280,16 +280,21 @@ __device__ __forceinline__ void ec_block_partials(double a0, double a1, double a
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0, t2 = 0;
-    for (int w = 0; w < aw; ++w) {
-      t0 += ws[w][0];
-      t1 += ws[w][1];
-      t2 += ws[w][2];
+  if (warp == 0) {  // the warps' sums by a butterfly (a dependent FP64 add costs ~0.3 us here)
+    double t0 = lane < aw ? ws[lane][0] : 0.0;
+    double t1 = lane < aw ? ws[lane][1] : 0.0;
+    double t2 = lane < aw ? ws[lane][2] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+      t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+      t2 += __shfl_xor_sync(0xffffffffu, t2, o);
     }
-    parts[blockIdx.x * 3 + 0] = t0;
-    parts[blockIdx.x * 3 + 1] = t1;
-    parts[blockIdx.x * 3 + 2] = t2;
+    if (lane == 0) {
+      parts[blockIdx.x * 3 + 0] = t0;
+      parts[blockIdx.x * 3 + 1] = t1;
+      parts[blockIdx.x * 3 + 2] = t2;
+    }
   }
 }
 
@@ -304,9 +309,10 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
   // lambda and its reciprocal once per block (FP64 sqrt and division are
   // long instruction sequences on this GPU), shared through shared memory
   __shared__ double lam_s[2];
-  if (threadIdx.x == 0) {
-    lam_s[0] = sqrt(st->lam2);
-    lam_s[1] = 1.0 / lam_s[0];
+  if (threadIdx.x == 0) {  // 1 / lambda and lambda from one reciprocal square root
+    const double l2 = st->lam2;
+    lam_s[1] = rsqrt(l2);
+    lam_s[0] = l2 == 0.0 ? 0.0 : l2 * lam_s[1];  // sqrt(0) = 0, 1 / 0 = inf
   }
   __syncthreads();
   const double lam = lam_s[0];
@@ -419,11 +425,12 @@ __device__ __forceinline__ bool grid_sync_reduce(EcState* st, const double* pp,
       __syncthreads();
     }
     if (threadIdx.x == 0) {
-      st->tot[0] = red[0][0];
+      const double r0 = red[0][0], inv = rsqrt(r0);
+      st->tot[0] = r0;
       st->tot[1] = sqrt(red[0][1]);
       st->tot[2] = sqrt(red[0][2]);
-      st->tot[3] = sqrt(red[0][0]);
-      st->tot[4] = 1.0 / st->tot[3];
+      st->tot[3] = r0 == 0.0 ? 0.0 : r0 * inv;
+      st->tot[4] = inv;
       st->bar_count = 0;
       __threadfence();
       atomicAdd(&st->bar_gen, 1u);
@@ -449,8 +456,8 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_coop_kernel(
   // are long instruction sequences on this GPU: one thread computes them)
   __shared__ double lam_s[2];
   if (threadIdx.x == 0) {
-    lam_s[0] = sqrt(lam2);
-    lam_s[1] = 1.0 / lam_s[0];
+    lam_s[1] = rsqrt(lam2);
+    lam_s[0] = lam2 == 0.0 ? 0.0 : lam2 * lam_s[1];
   }
   __syncthreads();
   double lam = lam_s[0], inv = lam_s[1];

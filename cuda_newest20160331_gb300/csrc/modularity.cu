@@ -115,9 +115,10 @@ __device__ __forceinline__ bool group_barrier(ModGroup* g, int nb, uint64_t limi
 }
 
 // Block sum of W per-thread values into parts[blockIdx.x * kModParts + k0 ..]
-// (warp butterflies, then warps in order: a fixed order).  Only the first
-// `aw` warps can hold non-zero values (FP64 work is scarce on this GPU: the
-// other warps skip it).
+// (warp butterflies, then a butterfly over the warps' sums: a fixed order).
+// Only the first `aw` warps can hold non-zero values (FP64 work is scarce on
+// this GPU: the other warps skip it).  A dependent FP64 add costs ~0.3 us
+// here, so the warps' sums are not added one after the other.
 template <int W>
 __device__ __forceinline__ void block_partials(double (&a)[W], double* parts, int k0, int aw,
                                                double (&tot)[W]) {
@@ -134,14 +135,18 @@ __device__ __forceinline__ void block_partials(double (&a)[W], double* parts, in
       for (int w = 0; w < W; ++w) ws[warp][w] = a[w];
   }
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (warp == 0) {  // the warps' sums by a second butterfly (5 dependent adds, not aw)
 #pragma unroll
     for (int w = 0; w < W; ++w) {
-      double t = 0;
-      for (int k = 0; k < aw; ++k) t += ws[k][w];
-      parts[(size_t)blockIdx.x * kModParts + k0 + w] = t;
-      bt[w] = t;
+      double t = lane < aw ? ws[lane][w] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) {
+        parts[(size_t)blockIdx.x * kModParts + k0 + w] = t;
+        bt[w] = t;
+      }
     }
+  }
   __syncthreads();
 #pragma unroll
   for (int w = 0; w < W; ++w) tot[w] = bt[w];
@@ -154,8 +159,9 @@ __device__ __forceinline__ int active_warps(int cnt) {
 }
 
 // Sum over the group's blocks [b0, b0 + nb) of partial k0 .. k0 + W - 1 in a
-// fixed order (thread-strided sums, warp butterflies, warps in order), so
-// the result does not depend on timing.  Every thread gets the totals.
+// fixed order (thread-strided sums, warp butterflies, a butterfly over the
+// warps' sums), so the result does not depend on timing.  Every thread gets
+// the totals.
 template <int W>
 __device__ __forceinline__ void group_reduce(const double* parts, int b0, int nb, int k0,
                                              double (&out)[W]) {
@@ -179,12 +185,13 @@ __device__ __forceinline__ void group_reduce(const double* parts, int b0, int nb
       for (int w = 0; w < W; ++w) ws[warp][w] = s[w];
   }
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (warp == 0)
 #pragma unroll
     for (int w = 0; w < W; ++w) {
-      double t = 0;
-      for (int k = 0; k < aw; ++k) t += ws[k][w];
-      tot[w] = t;
+      double t = lane < aw ? ws[lane][w] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) tot[w] = t;
     }
   __syncthreads();
 #pragma unroll
@@ -379,14 +386,18 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   }
   const int aw = active_warps(p1 - p0);
   __shared__ double scal[4];  // per-step scalars, computed by one thread
+  // v_k / 2 / M as v_k * RN(0.5 / M); the stop test on squared norms (no
+  // square root per step): a dependent FP64 operation costs ~0.3 us here
+  const double half_inv_m = 0.5 / Md;
+  const double eps2 = a.eps * a.eps;
   // a group of one block takes its own totals: no global barrier, no L2 round trip
   double t1[1];
   block_partials<1>(p1s, a.parts, 0, aw, t1);
   if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 0, a.limit_ns, t1)) return false;
   double vk = t1[0];
-  double err1 = 1, err2 = 1, vn = 0;
+  double err1 = 1, err2 = 1, vn = 0;  // squared norms |v -+ v0|^2 during the loop
   int it = 0;
-  while (err1 > a.eps && err2 > a.eps && it < a.max_iter) {
+  while (err1 > eps2 && err2 > eps2 && it < a.max_iter) {
     const size_t cur = (size_t)(it & 1) * a.nrows, nxt = (size_t)((it + 1) & 1) * a.nrows;
     const float2* vfc = a.vf + cur + off;  // the group's iterate, group-local index
     if (staged && !self_stage) {
@@ -427,7 +438,7 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
     __syncthreads();
     // y = A_G v0 - (v_k / 2 / M k + (sumBG - beta) v0) (:344), thread per position;
     // sumBG = |adj(i) ∩ G| - k K_G / 2 / M in integers (:258-266)
-    if (threadIdx.x == 0) scal[0] = __ddiv_rn(__ddiv_rn(vk, 2.0), Md);  // v_k / 2 / M
+    if (threadIdx.x == 0) scal[0] = __dmul_rn(vk, half_inv_m);  // v_k / 2 / M
     __syncthreads();
     const double c = scal[0];
     double py[1] = {0};
@@ -445,9 +456,9 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
     double ty[1];
     block_partials<1>(py, a.parts, 1, aw, ty);
     if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 1, a.limit_ns, ty)) return false;
-    if (threadIdx.x == 0) {
-      scal[1] = sqrt(ty[0]);  // VectorNorm (:383-389)
-      scal[2] = 1.0 / scal[1];
+    if (threadIdx.x == 0) {  // VectorNorm (:383-389) and its reciprocal, one sequence
+      scal[2] = rsqrt(ty[0]);
+      scal[1] = ty[0] == 0.0 ? 0.0 : __dmul_rn(ty[0], scal[2]);  // sqrt(0) = 0
     }
     __syncthreads();
     vn = scal[1];
@@ -471,15 +482,9 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
     double te[3];
     block_partials<3>(pe, a.parts, 2, aw, te);
     if (nb > 1 && !group_sync_reduce<3>(g, nb, b0, a.parts, 2, a.limit_ns, te)) return false;
-    if (threadIdx.x == 0) {
-      scal[0] = sqrt(te[0]);
-      scal[3] = sqrt(te[1]);
-    }
-    __syncthreads();
-    err1 = scal[0];
-    err2 = scal[3];
+    err1 = te[0];
+    err2 = te[1];
     vk = te[2];
-    __syncthreads();  // scal[0] is rewritten at the next step's start
     ++it;
   }
   // eigenvalue sign (:369-375): the first node of G with the largest |v|
@@ -558,7 +563,7 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   }
   *lambda = prod > 0 ? vn : -vn;
   *iters = it;
-  *resid = err1 < err2 ? err1 : err2;
+  *resid = sqrt(err1 < err2 ? err1 : err2);
   *fbuf = it & 1;
   *subp = gp;
   *subn = gn;
