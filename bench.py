@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--impl", default="gb300")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--modularity", default="auto", choices=["auto", "on", "off"],
+                   help="Newman modularity of the step's CSR (auto: N <= 100,000)")
     p.add_argument("--serve-requests", type=int, default=120)
     p.add_argument("--serve-slots", type=int, default=4)
     p.add_argument("--serve-dump", default="", help="write per-request records (JSON) here")
@@ -523,9 +525,12 @@ def main():
                / (statistics.median(ec_ms) / 1000.0) / 1e9 if iters else None}
     # Newman modularity of the same CSR's binary graph (values ignored, as the
     # reference tool reads only R and C)
-    mod_info = modularity_run(b, csr_dev, stream)
-    mod_info.pop("labels")
-    mod_info["workload"] = f"{w.name} CSR, binary view (nnz={csr_dev.nnz})"
+    if args.modularity == "on" or (args.modularity == "auto" and N <= 100000):
+        mod_info = modularity_run(b, csr_dev, stream)
+        mod_info.pop("labels")
+        mod_info["workload"] = f"{w.name} CSR, binary view (nnz={csr_dev.nnz})"
+    else:
+        mod_info = {"skipped": f"N={N} above the automatic limit (--modularity on runs it)"}
     del csr_dev
 
     # the other forms on the same input, same edge set (3 timed steps each):
@@ -626,7 +631,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_sample(w, bold_h, args.cpu_seconds, host_cores())
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        line["modularity"]["small_vs_cpu"] = modularity_small_pair(b, stream)
+        if "skipped" not in line["modularity"]:
+            line["modularity"]["small_vs_cpu"] = modularity_small_pair(b, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     b.close()
