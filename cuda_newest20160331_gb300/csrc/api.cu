@@ -82,6 +82,7 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* ti
 cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t st);
 size_t tc_subj_bytes();
 bool tc_subj_fill(void* host, int s, const CorrArgs& a, const uint8_t* blockbad, int form);
+cudaError_t prepare_corr_tc_multi(int form, bool dens, bool absm);
 cudaError_t launch_corr_tc_multi(const CorrArgs& batch, const void* subj_dev, const int4* tiles4,
                                  int ntiles, int form, bool dens, bool absm, int grid,
                                  cudaStream_t st);
@@ -1745,10 +1746,40 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
   batch.err = &bst->err;
   const int4* tiles4 = reinterpret_cast<const int4*>(ctx->ptr[S_BATCH_TILES]);
   const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : ctx->batch_ntiles;
+  const int form = prec == BNA_PREC_BF16X3 ? 0 : 1;
   int launches = 0;
-  for (int t0 = 0; t0 < ctx->batch_ntiles; t0 += per, ++launches)
-    CK(launch_corr_tc_multi(batch, table_dev, tiles4 + t0, std::min(per, ctx->batch_ntiles - t0),
-                            prec == BNA_PREC_BF16X3 ? 0 : 1, dev_sel, absm, ctx->sms, st));
+  // the persistent count pass over every subject's tiles, replayed from a
+  // captured CUDA graph (one launch, or the chunks a launch gate asks for)
+  CK(prepare_corr_tc_multi(form, dev_sel, absm));  // its attributes: outside the capture
+  struct ExecGuard {  // released once its launch is over, on every return path
+    cudaGraphExec_t e = nullptr;
+    cudaStream_t s = nullptr;
+    ~ExecGuard() {
+      if (e) {
+        cudaStreamSynchronize(s);
+        cudaGraphExecDestroy(e);
+      }
+    }
+  } guard;
+  guard.s = st;
+  cudaGraphExec_t& count_exec = guard.e;
+  {
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    for (int t0 = 0; ce == cudaSuccess && t0 < ctx->batch_ntiles; t0 += per, ++launches)
+      ce = launch_corr_tc_multi(batch, table_dev, tiles4 + t0,
+                                std::min(per, ctx->batch_ntiles - t0), form, dev_sel, absm,
+                                ctx->sms, cap);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(cap, &graph);
+    if (ce == cudaSuccess) ce = ee;
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&count_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cap);
+    CK(ce);
+  }
+  CK(cudaGraphLaunch(count_exec, st));
   CK(cudaEventRecord(ctx->ev[2], st));
   // ---- candidates, selection / recompute, scans (one synchronisation)
   for (int k = 0; k < nsub; ++k) {
@@ -1756,7 +1787,10 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
     if (s) return fail(ctx, s, "subject %d: %s", k, ctx->kids[k]->last_error.c_str());
   }
   CK(cudaMemcpyAsync(ctx->pinned, bst, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+  const cudaError_t se = cudaStreamSynchronize(st);
+  cudaGraphExecDestroy(count_exec);  // its launch has completed
+  count_exec = nullptr;
+  CK(se);
   if (reinterpret_cast<DevStatus*>(ctx->pinned)->err & ERR_TIMEOUT)
     return fail(ctx, BNA_TIMEOUT, "batch count pass: a bounded wait expired");
   for (int k = 0; k < nsub; ++k) {

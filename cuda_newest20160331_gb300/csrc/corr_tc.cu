@@ -816,6 +816,24 @@ bool tc_subj_fill(void* host, int s, const CorrArgs& a, const uint8_t* blockbad,
 // Count pass over the tiles of several subjects in one persistent launch:
 // tiles4 = (I, J-pair, subject); subj_dev = the device copy of the table;
 // batch.err receives timeouts of the producer and MMA warps.
+// The multi-subject kernel of a form, with its shared-memory limit set (a
+// call outside any stream capture; the launcher sets it too).
+static void (*tc_multi_kernel(int form, bool dens, bool absm))(CUtensorMap, CUtensorMap, TcArgs) {
+  if (form == FORM_BF16X3)
+    return dens ? corr_tc_kernel<0, false, FORM_BF16X3, true, true>
+           : absm ? corr_tc_kernel<0, true, FORM_BF16X3, false, true>
+                  : corr_tc_kernel<0, false, FORM_BF16X3, false, true>;
+  return dens ? corr_tc_kernel<0, false, FORM_TF32, true, true>
+         : absm ? corr_tc_kernel<0, true, FORM_TF32, false, true>
+                : corr_tc_kernel<0, false, FORM_TF32, false, true>;
+}
+
+cudaError_t prepare_corr_tc_multi(int form, bool dens, bool absm) {
+  if (dens && absm) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(tc_multi_kernel(form, dens, absm),
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_BYTES);
+}
+
 cudaError_t launch_corr_tc_multi(const CorrArgs& batch, const void* subj_dev, const int4* tiles4,
                                  int ntiles, int form, bool dens, bool absm, int grid,
                                  cudaStream_t st) {
@@ -828,18 +846,7 @@ cudaError_t launch_corr_tc_multi(const CorrArgs& batch, const void* subj_dev, co
   p.nksteps = 0;
   const int g = grid < ntiles ? grid : ntiles;
   if (g <= 0) return cudaSuccess;
-  void (*kern)(CUtensorMap, CUtensorMap, TcArgs);
-  if (form == FORM_BF16X3)
-    kern = dens ? corr_tc_kernel<0, false, FORM_BF16X3, true, true>
-           : absm ? corr_tc_kernel<0, true, FORM_BF16X3, false, true>
-                  : corr_tc_kernel<0, false, FORM_BF16X3, false, true>;
-  else
-    kern = dens ? corr_tc_kernel<0, false, FORM_TF32, true, true>
-           : absm ? corr_tc_kernel<0, true, FORM_TF32, false, true>
-                  : corr_tc_kernel<0, false, FORM_TF32, false, true>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)TC_SMEM_BYTES);
-  if (e != cudaSuccess) return e;
+  void (*kern)(CUtensorMap, CUtensorMap, TcArgs) = tc_multi_kernel(form, dens, absm);
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   kern<<<g, TC_THREADS, TC_SMEM_BYTES, st>>>(dummy, dummy, p);
