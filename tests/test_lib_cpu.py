@@ -115,6 +115,17 @@ def test_ec_file_format(tmp_path):
     assert np.array_equal(np.frombuffer(raw[4:], np.float32), np.array([1.5, 2.25, -3.0], np.float32))
 
 
+def test_modu_file_format(tmp_path):
+    """_modu.nm (Modularity_CPU.cpp:122-131): int32 N, then the labels as floats."""
+    p = str(tmp_path / "x_modu.nm")
+    labels = np.array([1, 2, 2, 3, 1], np.int32)
+    assert bna.lib().bna_modu_write(p.encode(), labels.ctypes.data, len(labels)) == 0
+    raw = open(p, "rb").read()
+    assert np.frombuffer(raw[:4], np.int32)[0] == 5
+    assert np.array_equal(np.frombuffer(raw[4:], np.float32), labels.astype(np.float32))
+    assert bna.lib().bna_modu_write(p.encode(), None, 3) == 1  # BNA_BAD_ARG
+
+
 def test_bad_arguments_fail_loudly():
     with pytest.raises(ValueError):
         bna._opts("nope", 0.5, "fp32", True, None)
@@ -212,3 +223,6 @@ def test_cli_usage_and_argument_errors(tmp_path):
     assert r.returncode == 1 and "threshold type error" in r.stdout
     r = subprocess.run([os.path.join(b, "bna_cuec")], capture_output=True, text=True)
     assert r.returncode == 1
+    r = subprocess.run([os.path.join(b, "bna_modularity"), str(tmp_path)], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "Input format" in r.stderr
