@@ -246,7 +246,13 @@ def serve_run(n_requests: int, slots: int = 4, rate: float = 4.0, seed: int = 50
     lat = np.array([r.latency for r in mixed]) * 1000.0
     solo = np.array([r.latency for r in alone]) * 1000.0
     slow = lat / solo
-    same = all(a.nnz == m.nnz and a.lam == m.lam for a, m in zip(alone, mixed))
+    diff = [{"k": k, "N": subjects[reqs[k].subject][0], "T": subjects[reqs[k].subject][1],
+             "mode": reqs[k].mode, "value": reqs[k].value, "nnz": [a.nnz, m.nnz],
+             "lambda": [a.lam, m.lam], "iters": [a.ec_iters, m.ec_iters],
+             "status": [a.status, m.status]}
+            for k, (a, m) in enumerate(zip(alone, mixed))
+            if a.nnz != m.nnz or not (a.lam == m.lam or (a.lam != a.lam and m.lam != m.lam))]
+    same = not diff
     edges = sum(r.nnz for r in mixed)
     return {
         "requests": len(reqs), "rate_per_s": rate, "slots": slots,
@@ -258,6 +264,7 @@ def serve_run(n_requests: int, slots: int = 4, rate: float = 4.0, seed: int = 50
         "p99_over_median_solo": float(np.percentile(lat, 99) / np.percentile(solo, 50)),
         "throughput_req_s": len(reqs) / span, "edges_per_s": edges / span,
         "same_results_alone_and_mixed": same,
+        "differences": diff[:20],
         "sample": f"{len(reqs)} requests from {len(subjects)} seeded subjects "
                   f"(N {min(s[0] for s in subjects)}..{n_max}, T in {{240,600,1200}}), "
                   "tau U[0.3,0.6] or density U[0.1,2]%, split-BF16, CSR kept on device, "

@@ -219,6 +219,7 @@ __device__ __forceinline__ void ec_block_rows(int n, const int32_t* __restrict__
                                               double& a1, double& a2) {
   constexpr int kW = kEcThreads / 32;
   __shared__ float2 rs[kEcThreads];
+  __shared__ bool rempty[kEcThreads];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = gridDim.x * kW;
   for (long long base = (long long)blockIdx.x * kW; base < n; base += (long long)kEcRounds * nw) {
@@ -238,15 +239,21 @@ __device__ __forceinline__ void ec_block_rows(int n, const int32_t* __restrict__
         sh = s2;
         sl = __fadd_rn(sl, __fadd_rn(ol, e2));
       }
-      if (lane == 0) rs[k * kW + warp] = make_float2(sh, sl);
+      if (lane == 0) {
+        rs[k * kW + warp] = make_float2(sh, sl);
+        rempty[k * kW + warp] = e <= b;
+      }
     }
     __syncthreads();
     {
       const int k = threadIdx.x / kW, w = threadIdx.x % kW;
       const long long row = base + (long long)k * nw + w;
       if (row < n) {
+        // y = A (u / lambda) as the reference orders it (weighted-net.cu:160-167):
+        // a row without entries gives 0 even when 1 / lambda is infinite (an
+        // all-zero iterate), where sum * (1 / lambda) would give 0 * inf = NaN
         const float2 sm = rs[threadIdx.x];
-        const double y = ((double)sm.x + (double)sm.y) * inv;
+        const double y = rempty[threadIdx.x] ? 0.0 : ((double)sm.x + (double)sm.y) * inv;
         const double old = l2_only ? __ldcg(uc + row) : uc[row];
         un[row] = y;
         unf[row] = split_df(y);

@@ -43,6 +43,7 @@
 
 namespace bna {
 cudaMemPool_t lib_pool(int device);
+cudaError_t copy_from_host(const void* src, void* dst, size_t bytes, int sms, cudaStream_t stream);
 }
 int32_t bna_ctx_trim_idle(bna_ctx* ctx);
 
@@ -106,6 +107,7 @@ constexpr int64_t kLongEc = 1000;
 
 struct bna_server {
   int device = 0;
+  int sms = 1;
   int64_t budget = 0;
   Clock::time_point t0;
   std::mutex mu;
@@ -209,8 +211,11 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
   cudaStream_t st = s->stream[level_of(j->work, srv->levels)];
   const size_t bytes = (size_t)r.N * r.T * sizeof(float);
   int32_t rc = grow(srv->device, reinterpret_cast<void**>(&s->bold), &s->bold_cap, bytes, st);
-  if (rc == BNA_OK && cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) !=
-                          cudaSuccess)
+  // the series by an SM-driven copy from the caller's page-locked buffer
+  // (copy-engine uploads slowed to a few GB/s while other requests shared
+  // the device); a pageable buffer takes the copy engine
+  if (rc == BNA_OK && bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st) != cudaSuccess &&
+      cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = BNA_CUDA_ERROR;
   bna_csr csr{};
   if (rc == BNA_OK) {
@@ -343,6 +348,9 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
   if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return BNA_CUDA_ERROR;
   bna_server* srv = new bna_server();
   srv->device = device;
+  if (cudaDeviceGetAttribute(&srv->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      srv->sms < 1)
+    srv->sms = 1;
   srv->budget = hbm_budget_bytes;
   srv->t0 = Clock::now();
   // numerically lower = higher priority; greatest <= least

@@ -388,6 +388,19 @@ def test_ec_large_graph_matches_oracle(builder, unsorted):
     assert np.max(np.abs(ec.cpu().numpy() - ec_o)) <= 1e-9 * np.max(np.abs(ec_o))
 
 
+@pytest.mark.parametrize("n", [7, 20000])
+def test_ec_of_a_graph_without_edges_matches_reference_order(builder, n):
+    """No edges: the reference normalises before its SpMV, so the second
+    iterate is exactly 0 (an empty row adds nothing, even of an infinite
+    1 / lambda) and it stops there with lambda 0 (weighted-net.cu:154-189)."""
+    R = np.zeros(n + 1, np.int32)
+    ec_o, lam_o, it_o, _ = oracle.ec(R, np.zeros(0, np.int32))
+    assert it_o == 2 and lam_o == 0.0 and not ec_o.any()
+    csr = bna.CsrResult(n, 0, dev(R), dev(np.zeros(1, np.int32)), None, {})
+    ec, lam, it, conv = builder.ec(csr)
+    assert conv and it == 2 and lam == 0.0 and not ec.cpu().numpy().any()
+
+
 def test_lead_vector_known_answer_4node(builder):
     R = np.array([0, 2, 3, 6, 8], np.int32)
     C = np.array([2, 3, 2, 0, 1, 3, 0, 2], np.int32)
