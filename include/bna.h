@@ -365,7 +365,10 @@ int32_t bna_ec_write(const char* path, const double* ec_host, int32_t N);
  * for a large one to finish.  Results do not depend on what else runs. */
 typedef struct bna_server bna_server;
 typedef struct bna_request {
-  const float* bold_host; /* time-major [T][N]; must stay valid until the reply */
+  const float* bold_host; /* time-major [T][N]; must stay valid until the reply.  A
+                             page-locked buffer (cudaHostAlloc / cudaMallocHost) is read
+                             by the SMs at full link speed whatever else runs; a pageable
+                             one goes through the copy engine */
   int32_t N, T;
   bna_corr_opts opts;
   int32_t ec_max_iter;    /* 0: no centrality */
