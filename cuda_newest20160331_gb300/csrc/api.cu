@@ -456,6 +456,14 @@ inline void gate(bna_ctx* ctx, cudaStream_t st, int phase, long long done) {
   if (ctx->gate) ctx->gate(ctx->gate_user, st, phase, done);
 }
 
+// Blocks of the exact-value passes (warp per candidate, grid-stride): eight
+// per SM fill every SM; a context that interleaves its launches with other
+// work (BNA_OPT_TILES_PER_LAUNCH set: a server slot) takes half, so a
+// smaller request's kernels find room beside a long exact-value pass.
+inline int band_grid(const bna_ctx* ctx) {
+  return ctx->tiles_per_launch > 0 ? ctx->sms * 4 : ctx->sms * 8;
+}
+
 int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cudaStream_t st,
                   bool sampled = false) {
   if (ctx->avg) {  // the averaged matrix is the source
@@ -965,7 +973,7 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
           CK(launch_avg_exact(a, ctx->avg->subj, ctx->avg->S, ctx->avg->fisher, cvals, ctx->sms,
                               st));
         else
-          CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
+          CK(launch_cand_values(a, cvals, band_grid(ctx), st));
         ctx->klaunch += 1;
       } else {
         if (ctx->avg) {  // exact averaged values, then the decisions on them
@@ -974,7 +982,7 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
           a.cand_val = cvals;
           ctx->klaunch += 1;
         }
-        CK(launch_recompute(a, ctx->sms * 8, st));
+        CK(launch_recompute(a, band_grid(ctx), st));
         ctx->klaunch += 1 + 4;  // recompute, scan
         CK(cudaEventRecord(ctx->ev[3], st));
         CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr,
@@ -1023,7 +1031,7 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
       } else {
         // ties beyond the device sort (or an inconsistency): the host selection
         dev_sel = false;
-        CK(launch_cand_values(a, cvals, ctx->sms * 8, st));
+        CK(launch_cand_values(a, cvals, band_grid(ctx), st));
         ctx->klaunch += 1;
       }
     }
@@ -1082,7 +1090,7 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
     a.th.mode = BNA_THR_DENSITY;
     a.th.tau = tau_star;
     a.cand_val = cvals;
-    CK(launch_recompute(a, ctx->sms * 8, st));
+    CK(launch_recompute(a, band_grid(ctx), st));
     ctx->klaunch += 1 + 4;  // decide, scan
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(launch_csr_scan(a.seg, a.nb, a.n_pad, N, rowlen, pre, bsum, &ds->total, row_ptr, a.err,
@@ -1609,7 +1617,7 @@ int32_t batch_after(bna_ctx* ctx, BatchSubj& b, bool dev_sel, cudaStream_t st) {
     CK(cudaMemcpyAsync(static_cast<char*>(ctx->pinned) + 2048, b.dstate, dens_state_bytes(),
                        cudaMemcpyDeviceToHost, st));
   } else {
-    CK(launch_recompute(a, ctx->sms * 8, st));
+    CK(launch_recompute(a, band_grid(ctx), st));
   }
   CK(launch_csr_scan(a.seg, a.nb, a.n_pad, b.N, b.rowlen, b.pre, b.bsum, &b.ds->total, b.row_ptr,
                      a.err, st));

@@ -126,7 +126,8 @@ int64_t bna_ctx_arena_bytes(const bna_ctx* ctx);
  *   BNA_OPT_TILES_PER_LAUNCH: split each tensor-core correlation pass into
  *     launches of at most this many 128 x 256 tiles (0 = one launch), so that
  *     work of other streams - other requests of a server - can be scheduled
- *     between them;
+ *     between them; with it set, the exact-value passes also leave half of
+ *     every SM to other work;
  *   BNA_OPT_MAX_NNZ: bna_corr_csr returns BNA_CAPACITY (stats->nnz = the
  *     required size) instead of building a CSR with more entries (0 = no
  *     limit);
