@@ -83,6 +83,20 @@ def test_server_matches_single_context_and_oracle(builder):
     assert abs(r.lam - lam) <= 1e-5 * lam
 
 
+def test_page_locked_input_gives_the_same_result():
+    """A page-locked series is uploaded by the SMs (csrc/hostcopy.cu), a pageable
+    one by the copy engine: same CSR and centrality, bit for bit (N * T * 4 not a
+    multiple of 16 exercises the tail bytes)."""
+    import torch
+    N, T, K, seed, mode, value = (3001, 151, 12, 507, "r_ge", 0.35)
+    b = _bold(N, T, K, seed)
+    pinned = torch.from_numpy(b.copy()).pin_memory().numpy()
+    with bna.Server(0, slots=1) as s:
+        r_pageable = s.wait(s.submit(b, mode=mode, value=value, precision="bf16x3"))
+        r_pinned = s.wait(s.submit(pinned, mode=mode, value=value, precision="bf16x3"))
+    _same(r_pageable, r_pinned)
+
+
 def test_capacity_and_budget_refusals():
     N, T, K, seed, mode, value = SUBJECTS[0]
     b = _bold(N, T, K, seed)
