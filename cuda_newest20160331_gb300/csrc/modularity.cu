@@ -78,6 +78,87 @@ __device__ __forceinline__ void mod_two_sum(float a, float b, float& s, float& e
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// Float-float ("double-float") arithmetic for the per-node work of a power
+// step: (hi, lo) pairs with |lo| <= ulp(hi) / 2, about 2^-44 relative per
+// operation (Dekker 1971; TwoProduct by FMA).  The FP64 latency of this GPU
+// (~0.3 us per dependent operation) made the FP64 form of these chains the
+// largest part of a step.
+__device__ __forceinline__ float2 ff_norm(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  float s, e;
+  mod_two_sum(a.x, b.x, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  return ff_norm(s, e);
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ float2 ff_mulf(float2 a, float f) {  // f exact in float
+  const float p = __fmul_rn(a.x, f);
+  float e = __fmaf_rn(a.x, f, -p);
+  e = __fmaf_rn(a.y, f, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ double ff_to_d(float2 a) { return (double)a.x + (double)a.y; }
+// An integer of at most 2^48 in magnitude, exactly.
+__device__ __forceinline__ float2 ff_from_ll(long long x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (long long)h));
+}
+
+// Block sum of W float-float values per thread (warp butterflies, then a
+// butterfly over the warps' sums: a fixed order) into parts[...k0 + w] as
+// doubles (hi + lo is exact in a double) and into tot for every thread.
+template <int W>
+__device__ __forceinline__ void block_partials_ff(float2 (&a)[W], double* parts, int k0, int aw,
+                                                  double (&tot)[W]) {
+  __shared__ float2 wsf[kModWarps][W];
+  __shared__ double btf[W];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < aw) {
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float2 b = make_float2(__shfl_xor_sync(0xffffffffu, a[w].x, o),
+                                     __shfl_xor_sync(0xffffffffu, a[w].y, o));
+        a[w] = ff_add(a[w], b);
+      }
+    if (lane == 0)
+#pragma unroll
+      for (int w = 0; w < W; ++w) wsf[warp][w] = a[w];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      float2 t = lane < aw ? wsf[lane][w] : make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float2 b = make_float2(__shfl_xor_sync(0xffffffffu, t.x, o),
+                                     __shfl_xor_sync(0xffffffffu, t.y, o));
+        t = ff_add(t, b);
+      }
+      if (lane == 0) {
+        const double d = ff_to_d(t);
+        parts[(size_t)blockIdx.x * kModParts + k0 + w] = d;
+        btf[w] = d;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < W; ++w) tot[w] = btf[w];
+}
+
 // Barrier among the nb blocks of one group (all co-resident: cooperative
 // launch).  Bounded: a wait longer than limit_ns raises g->err and returns false.
 __device__ __forceinline__ bool group_barrier(ModGroup* g, int nb, uint64_t limit_ns) {
@@ -386,6 +467,8 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   }
   const int aw = active_warps(p1 - p0);
   __shared__ double scal[4];  // per-step scalars, computed by one thread
+  __shared__ float2 scal_ff[2];
+  const float2 nbeta = mod_split(-beta);
   // v_k / 2 / M as v_k * RN(0.5 / M); the stop test on squared norms (no
   // square root per step): a dependent FP64 operation costs ~0.3 us here
   const double half_inv_m = 0.5 / Md;
@@ -436,51 +519,51 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       if (lane == 0) a.rs[p] = make_float2(sh, sl);
     }
     __syncthreads();
-    // y = A_G v0 - (v_k / 2 / M k + (sumBG - beta) v0) (:344), thread per position;
-    // sumBG = |adj(i) ∩ G| - k K_G / 2 / M in integers (:258-266)
-    if (threadIdx.x == 0) scal[0] = __dmul_rn(vk, half_inv_m);  // v_k / 2 / M
+    // y = A_G v0 - (v_k / 2 / M k + (sumBG - beta) v0) (:344), thread per position
+    // in float-float; sumBG = |adj(i) ∩ G| - k K_G / 2 / M in integers (:258-266)
+    if (threadIdx.x == 0) scal_ff[0] = mod_split(__dmul_rn(vk, half_inv_m));  // v_k / 2 / M
     __syncthreads();
-    const double c = scal[0];
-    double py[1] = {0};
+    const float2 c = scal_ff[0];
+    float2 py[1] = {make_float2(0.0f, 0.0f)};
+    float2* yf = reinterpret_cast<float2*>(a.y);
     for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
       const int i = a.rows[p];
       const long long k = a.rp[i + 1] - a.rp[i];
-      const double sbg = (double)((long long)(a.lrp[p + 1] - a.lrp[p]) - k * kg / 2 / a.M);
-      const float2 rsum = a.rs[p];
-      const double v0 = a.vd[cur + p];
-      const double corr = __dadd_rn(__dmul_rn(c, (double)k), __dmul_rn(__dsub_rn(sbg, beta), v0));
-      const double t = __dsub_rn(__dadd_rn((double)rsum.x, (double)rsum.y), corr);
-      a.y[p] = t;
-      py[0] = __dadd_rn(py[0], __dmul_rn(t, t));
+      const float2 sbg =
+          ff_from_ll((long long)(a.lrp[p + 1] - a.lrp[p]) - k * kg / 2 / a.M);
+      const float2 v0 = a.vf[cur + p];
+      const float2 corr = ff_add(ff_mulf(c, (float)k), ff_mul(ff_add(sbg, nbeta), v0));
+      const float2 t = ff_add(a.rs[p], ff_neg(corr));
+      yf[p] = t;
+      py[0] = ff_add(py[0], ff_mul(t, t));
     }
     double ty[1];
-    block_partials<1>(py, a.parts, 1, aw, ty);
+    block_partials_ff<1>(py, a.parts, 1, aw, ty);
     if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 1, a.limit_ns, ty)) return false;
     if (threadIdx.x == 0) {  // VectorNorm (:383-389) and its reciprocal, one sequence
-      scal[2] = rsqrt(ty[0]);
-      scal[1] = ty[0] == 0.0 ? 0.0 : __dmul_rn(ty[0], scal[2]);  // sqrt(0) = 0
+      const double inv = rsqrt(ty[0]);
+      scal[1] = ty[0] == 0.0 ? 0.0 : __dmul_rn(ty[0], inv);  // sqrt(0) = 0
+      scal_ff[1] = mod_split(inv);
     }
     __syncthreads();
     vn = scal[1];
-    const double inv = scal[2];
-    // v = y / |y|, |v - v0|^2, |v + v0|^2, v.k (:349-357, :333-335); the
-    // block's own positions, so no cross-block read
-    double pe[3] = {0, 0, 0};
+    const float2 inv = scal_ff[1];
+    // v = y / |y|, |v - v0|^2, |v + v0|^2, v.k (:349-357, :333-335) in
+    // float-float; the block's own positions, so no cross-block read
+    float2 pe[3] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
     for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
       const int i = a.rows[p];
-      const double x = __dmul_rn(a.y[p], inv);  // y / |y| through the reciprocal
-      const double old = a.vd[cur + p];
-      a.vd[nxt + p] = x;
-      const float2 xf = mod_split(x);
-      a.vf[nxt + p] = xf;
-      if (self_stage) stage[p - off] = xf;  // phase A of this step is over
-      const double d = __dsub_rn(x, old), s = __dadd_rn(x, old);
-      pe[0] = __dadd_rn(pe[0], __dmul_rn(d, d));
-      pe[1] = __dadd_rn(pe[1], __dmul_rn(s, s));
-      pe[2] = __dadd_rn(pe[2], __dmul_rn(x, (double)(a.rp[i + 1] - a.rp[i])));
+      const float2 x = ff_mul(yf[p], inv);  // y / |y| through the reciprocal
+      const float2 old = a.vf[cur + p];
+      a.vf[nxt + p] = x;
+      if (self_stage) stage[p - off] = x;  // phase A of this step is over
+      const float2 d = ff_add(x, ff_neg(old)), s = ff_add(x, old);
+      pe[0] = ff_add(pe[0], ff_mul(d, d));
+      pe[1] = ff_add(pe[1], ff_mul(s, s));
+      pe[2] = ff_add(pe[2], ff_mulf(x, (float)(a.rp[i + 1] - a.rp[i])));
     }
     double te[3];
-    block_partials<3>(pe, a.parts, 2, aw, te);
+    block_partials_ff<3>(pe, a.parts, 2, aw, te);
     if (nb > 1 && !group_sync_reduce<3>(g, nb, b0, a.parts, 2, a.limit_ns, te)) return false;
     err1 = te[0];
     err2 = te[1];
@@ -490,6 +573,10 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   // eigenvalue sign (:369-375): the first node of G with the largest |v|
   // (node 0 when none exceeds |v[0]|, v[0] taken as 0 off G); side sizes (:276-281)
   const size_t fin = (size_t)(it & 1) * a.nrows, prv = (size_t)((it + 1) & 1) * a.nrows;
+  for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
+    a.vd[fin + p] = ff_to_d(a.vf[fin + p]);
+    a.vd[prv + p] = ff_to_d(a.vf[prv + p]);
+  }
   double best = 0.0;
   int bq = 0x7fffffff;  // position of the maximum (positions ascend with node index)
   long long sp = 0, sn = 0;
