@@ -22,12 +22,14 @@
 // The host then takes the decisions in round order, which numbers the
 // children exactly as the sequential loop does.
 //
-// Arithmetic: GB300's FP64 rate is ~1/64 of its FP32 rate, so the SpMV sum
-// over a row runs in float-float ("double-float", Knuth's TwoSum) on the
-// iterate kept as a (hi, lo) float pair beside its double value: about 48
-// significant bits, the same order as the reference's sequential FP64 sum.
-// The correction term, the normalisation, the norms and the stop test stay in
-// FP64, with fixed-order reductions, so a run is deterministic.
+// Arithmetic: GB300's FP64 rate is ~1/64 of its FP32 rate and a dependent
+// FP64 operation takes ~0.3 us, so a power step runs in float-float
+// ("double-float": TwoSum, FMA TwoProduct) on the iterate kept as a (hi, lo)
+// float pair: about 44-48 significant bits per operation, the same order as
+// the reference's sequential FP64 sums.  The SpMV, the correction term, the
+// normalisation, the norms, the stop test and the reductions (fixed order,
+// so a run is deterministic) all use it; the final iterate is widened to
+// double for the sign rule and the division.
 #include <algorithm>
 #include <cmath>
 
@@ -51,7 +53,7 @@ struct ModGroup {
   long long subp, subn;
   int fbuf;      // buffer (0/1) of the final eigenvector iterate
   unsigned int bar_count, bar_gen;
-  double res[8];  // totals published by the last block to reach a barrier
+  float2 res[8];  // totals published by the last block to reach a barrier
 };
 
 constexpr int kModThreads = 1024;
@@ -114,24 +116,44 @@ __device__ __forceinline__ float2 ff_from_ll(long long x) {
   return make_float2(h, (float)(x - (long long)h));
 }
 
+// Float-float comparison a > b (both normalised).
+__device__ __forceinline__ bool ff_gt(float2 a, float2 b) {
+  return a.x > b.x || (a.x == b.x && a.y > b.y);
+}
+
+// 1 / sqrt(y) in float-float: rsqrtf's estimate r0 and one Newton step
+// r1 = r0 + r0 (1 - y r0^2) / 2 (the correction is ~2^-22 relative, so float
+// precision suffices for it).  y = 0 gives (inf, 0).
+__device__ __forceinline__ float2 ff_rsqrt(float2 y) {
+  const float r0 = rsqrtf(y.x);
+  if (y.x == 0.0f || !isfinite(r0)) return make_float2(r0, 0.0f);
+  const float2 t = ff_mulf(ff_mulf(y, r0), r0);            // y r0^2 ~ 1
+  const float2 e = ff_add(make_float2(1.0f, 0.0f), ff_neg(t));  // 1 - y r0^2
+  float h, l;
+  mod_two_sum(r0, __fmul_rn(__fmul_rn(r0, e.x), 0.5f), h, l);
+  return make_float2(h, l);
+}
+
+__device__ __forceinline__ float2 ff_shfl_xor(float2 a, int o) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+
 // Block sum of W float-float values per thread (warp butterflies, then a
-// butterfly over the warps' sums: a fixed order) into parts[...k0 + w] as
-// doubles (hi + lo is exact in a double) and into tot for every thread.
+// butterfly over the warps' sums: a fixed order) into partial slots
+// k0 .. k0 + W - 1 of this block and into tot for every thread.  Only the
+// first `aw` warps can hold non-zero values; with one such warp the second
+// butterfly is skipped.
 template <int W>
-__device__ __forceinline__ void block_partials_ff(float2 (&a)[W], double* parts, int k0, int aw,
-                                                  double (&tot)[W]) {
+__device__ __forceinline__ void block_partials_ff(float2 (&a)[W], float2* parts, int k0, int aw,
+                                                  float2 (&tot)[W]) {
   __shared__ float2 wsf[kModWarps][W];
-  __shared__ double btf[W];
+  __shared__ float2 btf[W];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp < aw) {
 #pragma unroll
     for (int w = 0; w < W; ++w)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float2 b = make_float2(__shfl_xor_sync(0xffffffffu, a[w].x, o),
-                                     __shfl_xor_sync(0xffffffffu, a[w].y, o));
-        a[w] = ff_add(a[w], b);
-      }
+      for (int o = 16; o > 0; o >>= 1) a[w] = ff_add(a[w], ff_shfl_xor(a[w], o));
     if (lane == 0)
 #pragma unroll
       for (int w = 0; w < W; ++w) wsf[warp][w] = a[w];
@@ -141,16 +163,12 @@ __device__ __forceinline__ void block_partials_ff(float2 (&a)[W], double* parts,
 #pragma unroll
     for (int w = 0; w < W; ++w) {
       float2 t = lane < aw ? wsf[lane][w] : make_float2(0.0f, 0.0f);
+      if (aw > 1)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float2 b = make_float2(__shfl_xor_sync(0xffffffffu, t.x, o),
-                                     __shfl_xor_sync(0xffffffffu, t.y, o));
-        t = ff_add(t, b);
-      }
+        for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_xor(t, o));
       if (lane == 0) {
-        const double d = ff_to_d(t);
-        parts[(size_t)blockIdx.x * kModParts + k0 + w] = d;
-        btf[w] = d;
+        parts[(size_t)blockIdx.x * kModParts + k0 + w] = t;
+        btf[w] = t;
       }
     }
   }
@@ -195,72 +213,35 @@ __device__ __forceinline__ bool group_barrier(ModGroup* g, int nb, uint64_t limi
   return ok_s != 0;
 }
 
-// Block sum of W per-thread values into parts[blockIdx.x * kModParts + k0 ..]
-// (warp butterflies, then a butterfly over the warps' sums: a fixed order).
-// Only the first `aw` warps can hold non-zero values (FP64 work is scarce on
-// this GPU: the other warps skip it).  A dependent FP64 add costs ~0.3 us
-// here, so the warps' sums are not added one after the other.
-template <int W>
-__device__ __forceinline__ void block_partials(double (&a)[W], double* parts, int k0, int aw,
-                                               double (&tot)[W]) {
-  __shared__ double ws[kModWarps][W];
-  __shared__ double bt[W];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (warp < aw) {
-#pragma unroll
-    for (int w = 0; w < W; ++w)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a[w] += __shfl_xor_sync(0xffffffffu, a[w], o);
-    if (lane == 0)
-#pragma unroll
-      for (int w = 0; w < W; ++w) ws[warp][w] = a[w];
-  }
-  __syncthreads();
-  if (warp == 0) {  // the warps' sums by a second butterfly (5 dependent adds, not aw)
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      double t = lane < aw ? ws[lane][w] : 0.0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) {
-        parts[(size_t)blockIdx.x * kModParts + k0 + w] = t;
-        bt[w] = t;
-      }
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int w = 0; w < W; ++w) tot[w] = bt[w];
-}
-
 // Warps holding thread-per-position work for `cnt` positions.
 __device__ __forceinline__ int active_warps(int cnt) {
   const int w = (cnt + 31) >> 5;
   return w < kModWarps ? w : kModWarps;
 }
 
-// Sum over the group's blocks [b0, b0 + nb) of partial k0 .. k0 + W - 1 in a
-// fixed order (thread-strided sums, warp butterflies, a butterfly over the
-// warps' sums), so the result does not depend on timing.  Every thread gets
-// the totals.
+// Sum over the group's blocks [b0, b0 + nb) of float-float partial
+// k0 .. k0 + W - 1 in a fixed order (thread-strided sums, warp butterflies, a
+// butterfly over the warps' sums when more than one warp holds values), so
+// the result does not depend on timing.  Every thread gets the totals.
 template <int W>
-__device__ __forceinline__ void group_reduce(const double* parts, int b0, int nb, int k0,
-                                             double (&out)[W]) {
-  __shared__ double ws[kModWarps][W];
-  __shared__ double tot[W];
+__device__ __forceinline__ void group_reduce(const float2* parts, int b0, int nb, int k0,
+                                             float2 (&out)[W]) {
+  __shared__ float2 ws[kModWarps][W];
+  __shared__ float2 tot[W];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double s[W];
+  float2 s[W];
 #pragma unroll
-  for (int w = 0; w < W; ++w) s[w] = 0;
+  for (int w = 0; w < W; ++w) s[w] = make_float2(0.0f, 0.0f);
   for (int b = threadIdx.x; b < nb; b += kModThreads)
 #pragma unroll
-    for (int w = 0; w < W; ++w) s[w] += __ldcg(parts + (size_t)(b0 + b) * kModParts + k0 + w);
+    for (int w = 0; w < W; ++w)
+      s[w] = ff_add(s[w], __ldcg(parts + (size_t)(b0 + b) * kModParts + k0 + w));
   const int aw = active_warps(nb);
   if (warp < aw) {
 #pragma unroll
     for (int w = 0; w < W; ++w)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s[w] += __shfl_xor_sync(0xffffffffu, s[w], o);
+      for (int o = 16; o > 0; o >>= 1) s[w] = ff_add(s[w], ff_shfl_xor(s[w], o));
     if (lane == 0)
 #pragma unroll
       for (int w = 0; w < W; ++w) ws[warp][w] = s[w];
@@ -269,9 +250,10 @@ __device__ __forceinline__ void group_reduce(const double* parts, int b0, int nb
   if (warp == 0)
 #pragma unroll
     for (int w = 0; w < W; ++w) {
-      double t = lane < aw ? ws[lane][w] : 0.0;
+      float2 t = lane < aw ? ws[lane][w] : make_float2(0.0f, 0.0f);
+      if (aw > 1)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        for (int o = 16; o > 0; o >>= 1) t = ff_add(t, ff_shfl_xor(t, o));
       if (lane == 0) tot[w] = t;
     }
   __syncthreads();
@@ -359,8 +341,8 @@ __global__ void mod_fill_kernel(int nrows, const int32_t* __restrict__ rows,
 // so each value is read from the partials once, not once per block.
 template <int W>
 __device__ __forceinline__ bool group_sync_reduce(ModGroup* g, int nb, int b0,
-                                                  const double* parts, int k0,
-                                                  uint64_t limit_ns, double (&out)[W]) {
+                                                  const float2* parts, int k0,
+                                                  uint64_t limit_ns, float2 (&out)[W]) {
   __shared__ int last_s, ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -388,7 +370,7 @@ __device__ __forceinline__ bool group_sync_reduce(ModGroup* g, int nb, int b0,
   }
   __syncthreads();
   if (last_s) {
-    double t[W];
+    float2 t[W];
     group_reduce<W>(parts, b0, nb, k0, t);
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -454,33 +436,36 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   const bool staged = stage != nullptr;
   const int eb0 = __ldg(a.lrp + p0);
   // v = (G ? i : 0) (:322-324); v.k for the first step
-  double p1s[1] = {0};
+  float2 p1s[1] = {make_float2(0.0f, 0.0f)};
   // a single-block group keeps its staged iterate current itself (no reload per step)
   const bool self_stage = staged && nb == 1;
   for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
     const int i = a.rows[p];
-    const double x = (double)i;
-    a.vd[p] = x;
-    a.vf[p] = mod_split(x);
-    if (self_stage) stage[p - off] = mod_split(x);
-    p1s[0] += x * (double)(a.rp[i + 1] - a.rp[i]);
+    const float2 x = ff_from_ll(i);
+    a.vf[p] = x;
+    if (self_stage) stage[p - off] = x;
+    p1s[0] = ff_add(p1s[0], ff_mulf(ff_from_ll(i), (float)(a.rp[i + 1] - a.rp[i])));
   }
   const int aw = active_warps(p1 - p0);
-  __shared__ double scal[4];  // per-step scalars, computed by one thread
-  __shared__ float2 scal_ff[2];
+  // per-step scalars, computed by one thread, and every sum of a step in
+  // float-float: a dependent FP64 operation costs ~0.3 us on this GPU and
+  // these chains sit between the group barriers
+  __shared__ float2 scal_ff[3];
   const float2 nbeta = mod_split(-beta);
-  // v_k / 2 / M as v_k * RN(0.5 / M); the stop test on squared norms (no
-  // square root per step): a dependent FP64 operation costs ~0.3 us here
-  const double half_inv_m = 0.5 / Md;
-  const double eps2 = a.eps * a.eps;
+  // v_k / 2 / M as v_k * (0.5 / M); the stop test on squared norms (no
+  // square root per step)
+  const float2 half_inv_m = mod_split(0.5 / Md);
+  const float2 eps2 = mod_split(a.eps * a.eps);
+  float2* parts2 = reinterpret_cast<float2*>(a.parts);
   // a group of one block takes its own totals: no global barrier, no L2 round trip
-  double t1[1];
-  block_partials<1>(p1s, a.parts, 0, aw, t1);
-  if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 0, a.limit_ns, t1)) return false;
-  double vk = t1[0];
-  double err1 = 1, err2 = 1, vn = 0;  // squared norms |v -+ v0|^2 during the loop
+  float2 t1[1];
+  block_partials_ff<1>(p1s, parts2, 0, aw, t1);
+  if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, parts2, 0, a.limit_ns, t1)) return false;
+  float2 vk = t1[0];
+  // squared norms |v -+ v0|^2 during the loop
+  float2 err1 = make_float2(1.0f, 0.0f), err2 = err1, vn = make_float2(0.0f, 0.0f);
   int it = 0;
-  while (err1 > eps2 && err2 > eps2 && it < a.max_iter) {
+  while (ff_gt(err1, eps2) && ff_gt(err2, eps2) && it < a.max_iter) {
     const size_t cur = (size_t)(it & 1) * a.nrows, nxt = (size_t)((it + 1) & 1) * a.nrows;
     const float2* vfc = a.vf + cur + off;  // the group's iterate, group-local index
     if (staged && !self_stage) {
@@ -521,7 +506,7 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
     __syncthreads();
     // y = A_G v0 - (v_k / 2 / M k + (sumBG - beta) v0) (:344), thread per position
     // in float-float; sumBG = |adj(i) ∩ G| - k K_G / 2 / M in integers (:258-266)
-    if (threadIdx.x == 0) scal_ff[0] = mod_split(__dmul_rn(vk, half_inv_m));  // v_k / 2 / M
+    if (threadIdx.x == 0) scal_ff[0] = ff_mul(vk, half_inv_m);  // v_k / 2 / M
     __syncthreads();
     const float2 c = scal_ff[0];
     float2 py[1] = {make_float2(0.0f, 0.0f)};
@@ -537,17 +522,17 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       yf[p] = t;
       py[0] = ff_add(py[0], ff_mul(t, t));
     }
-    double ty[1];
-    block_partials_ff<1>(py, a.parts, 1, aw, ty);
-    if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, a.parts, 1, a.limit_ns, ty)) return false;
+    float2 ty[1];
+    block_partials_ff<1>(py, parts2, 1, aw, ty);
+    if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, parts2, 1, a.limit_ns, ty)) return false;
     if (threadIdx.x == 0) {  // VectorNorm (:383-389) and its reciprocal, one sequence
-      const double inv = rsqrt(ty[0]);
-      scal[1] = ty[0] == 0.0 ? 0.0 : __dmul_rn(ty[0], inv);  // sqrt(0) = 0
-      scal_ff[1] = mod_split(inv);
+      const float2 inv = ff_rsqrt(ty[0]);
+      scal_ff[1] = ty[0].x == 0.0f ? make_float2(0.0f, 0.0f) : ff_mul(ty[0], inv);  // sqrt(0) = 0
+      scal_ff[2] = inv;
     }
     __syncthreads();
-    vn = scal[1];
-    const float2 inv = scal_ff[1];
+    vn = scal_ff[1];
+    const float2 inv = scal_ff[2];
     // v = y / |y|, |v - v0|^2, |v + v0|^2, v.k (:349-357, :333-335) in
     // float-float; the block's own positions, so no cross-block read
     float2 pe[3] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
@@ -562,9 +547,9 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       pe[1] = ff_add(pe[1], ff_mul(s, s));
       pe[2] = ff_add(pe[2], ff_mulf(x, (float)(a.rp[i + 1] - a.rp[i])));
     }
-    double te[3];
-    block_partials_ff<3>(pe, a.parts, 2, aw, te);
-    if (nb > 1 && !group_sync_reduce<3>(g, nb, b0, a.parts, 2, a.limit_ns, te)) return false;
+    float2 te[3];
+    block_partials_ff<3>(pe, parts2, 2, aw, te);
+    if (nb > 1 && !group_sync_reduce<3>(g, nb, b0, parts2, 2, a.limit_ns, te)) return false;
     err1 = te[0];
     err2 = te[1];
     vk = te[2];
@@ -648,9 +633,11 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   } else if (__ldg(a.label) == r) {  // max_index stays 0, node 0 in G: its position is off
     prod = __ldcg(a.vd + fin + off) * __ldcg(a.vd + prv + off);
   }
-  *lambda = prod > 0 ? vn : -vn;
+  const double vnd = ff_to_d(vn);
+  *lambda = prod > 0 ? vnd : -vnd;
   *iters = it;
-  *resid = sqrt(err1 < err2 ? err1 : err2);
+  const double e1 = ff_to_d(err1), e2 = ff_to_d(err2);
+  *resid = sqrt(e1 < e2 ? e1 : e2);
   *fbuf = it & 1;
   *subp = gp;
   *subn = gn;
