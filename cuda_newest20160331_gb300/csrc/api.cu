@@ -2102,7 +2102,7 @@ int32_t bna_modularity(bna_ctx* ctx, const bna_csr* csr, double lambda_min, int3
   ENSURE(S_MOD_VD, (size_t)2 * n * 8, vd);
   ENSURE(S_MOD_VF, (size_t)2 * n * 8, vf);
   ENSURE(S_MOD_RS, (size_t)n * 8, rs);
-  ENSURE(S_MOD_Y, (size_t)n * 8, y);
+  ENSURE(S_MOD_Y, (size_t)2 * n * 8, y);
   ENSURE(S_MOD_PARTS, (size_t)grid0 * mod_parts_per_block() * 8, parts);
   ENSURE(S_MOD_BLKGRP, (size_t)grid0 * 4, blkgrp);
   ENSURE(S_MOD_GROUPS, (size_t)grid0 * gbytes, groups);  // at most one group per block

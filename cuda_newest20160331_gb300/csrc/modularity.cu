@@ -59,7 +59,8 @@ struct ModGroup {
 constexpr int kModThreads = 1024;
 constexpr int kModWarps = kModThreads / 32;
 // Partial sums per block, each phase in slots of its own: 0 start vector,
-// 1 |y|^2, 2-4 the norms and v.k, 8-11 the eigenvalue sign and side sizes.
+// 1-4 a power step's |y|^2, y.k and the two norms, 8-11 the eigenvalue sign
+// and side sizes.
 constexpr int kModParts = 12;
 // Groups of at most this many nodes keep their iterate ((hi, lo) floats) in
 // shared memory during the gathers: 96 KB.
@@ -403,7 +404,7 @@ struct ModArgs {
   double* vd;              // [2][nrows] iterate (double), by position
   float2* vf;              // [2][nrows] iterate (hi, lo), by position
   float2* rs;              // [nrows] float-float row sums of a step
-  double* y;               // [nrows]
+  double* y;               // [2][nrows] unnormalised iterates (hi, lo floats)
   double* parts;           // [grid][kModParts]
   int nrows;
   int stage_max;           // groups of at most this many nodes gather from shared memory
@@ -439,10 +440,12 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   float2 p1s[1] = {make_float2(0.0f, 0.0f)};
   // a single-block group keeps its staged iterate current itself (no reload per step)
   const bool self_stage = staged && nb == 1;
+  float2* const yb = reinterpret_cast<float2*>(a.y);  // [2][nrows] unnormalised iterates y_s
   for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
     const int i = a.rows[p];
     const float2 x = ff_from_ll(i);
     a.vf[p] = x;
+    yb[p] = x;  // y_0 = x_0 with 1 / |y_0| taken as 1
     if (self_stage) stage[p - off] = x;
     p1s[0] = ff_add(p1s[0], ff_mulf(ff_from_ll(i), (float)(a.rp[i + 1] - a.rp[i])));
   }
@@ -461,18 +464,27 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   float2 t1[1];
   block_partials_ff<1>(p1s, parts2, 0, aw, t1);
   if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, parts2, 0, a.limit_ns, t1)) return false;
-  float2 vk = t1[0];
-  // squared norms |v -+ v0|^2 during the loop
-  float2 err1 = make_float2(1.0f, 0.0f), err2 = err1, vn = make_float2(0.0f, 0.0f);
-  int it = 0;
-  while (ff_gt(err1, eps2) && ff_gt(err2, eps2) && it < a.max_iter) {
-    const size_t cur = (size_t)(it & 1) * a.nrows, nxt = (size_t)((it + 1) & 1) * a.nrows;
-    const float2* vfc = a.vf + cur + off;  // the group's iterate, group-local index
+  // Power steps (:327-366) with one group barrier each.  Step s gathers the
+  // unnormalised y_{s-1} (published before the previous barrier) and scales
+  // the row sums by 1 / |y_{s-1}|, since A (y / |y|) = (A y) / |y|; it forms
+  // x_{s-1} = y_{s-1} / |y_{s-1}| for its own positions, y_s, and the sums
+  // |y_s|^2, y_s.k, |x_{s-1} -+ x_{s-2}|^2 in one reduction.  So the stop test
+  // of iteration s - 1 (:358-361: the norms computed directly, as there) is
+  // read one step later, and the step that revealed it is discarded.
+  float2 inv = make_float2(1.0f, 0.0f);            // 1 / |y_{s-1}|
+  float2 c = ff_mul(t1[0], half_inv_m);            // v_k / 2 / M of x_{s-1}
+  float2 vn = make_float2(0.0f, 0.0f);             // |y_{s-1}|: the eigenvalue estimate
+  float2 err1 = make_float2(1.0f, 0.0f), err2 = err1;  // of iteration s - 1
+  int it = 0;  // iterations done: x_it is the current iterate
+  for (int s = 1; a.max_iter > 0; ++s) {
+    const size_t yprv = (size_t)((s - 1) & 1) * a.nrows, ycur = (size_t)(s & 1) * a.nrows;
+    const size_t xcur = (size_t)((s - 1) & 1) * a.nrows, xold = (size_t)(s & 1) * a.nrows;
+    const float2* ypc = yb + yprv + off;  // y_{s-1} of the group, group-local index
     if (staged && !self_stage) {
-      for (int q = threadIdx.x; q < nr; q += kModThreads) stage[q] = __ldcg(vfc + q);
+      for (int q = threadIdx.x; q < nr; q += kModThreads) stage[q] = __ldcg(ypc + q);
       __syncthreads();
     }
-    // A_G v0 over the in-group edges (:342-343), float-float: warp per position
+    // A_G y_{s-1} over the in-group edges (:342-343), float-float: warp per position
     for (int p = p0 + warp; p < p1; p += kModWarps) {
       const int eb = __ldg(a.lrp + p), ee = __ldg(a.lrp + p + 1);
       float sh = 0.0f, sl = 0.0f;
@@ -482,13 +494,13 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
         for (int m = 0; m < 4; ++m) {
           const int e = e0 + lane + 32 * m;
           const int q = e < ee ? edge_col(a, s16, s32, eb0, e) : -1;
-          x[m] = q < 0 ? make_float2(0.0f, 0.0f) : (staged ? stage[q] : __ldcg(vfc + q));
+          x[m] = q < 0 ? make_float2(0.0f, 0.0f) : (staged ? stage[q] : __ldcg(ypc + q));
         }
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-          float s, e;
-          mod_two_sum(sh, x[m].x, s, e);
-          sh = s;
+          float t, e;
+          mod_two_sum(sh, x[m].x, t, e);
+          sh = t;
           sl = __fadd_rn(sl, __fadd_rn(e, x[m].y));
         }
       }
@@ -496,64 +508,60 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       for (int o = 16; o > 0; o >>= 1) {
         const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
         const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
-        float s, e;
-        mod_two_sum(sh, oh, s, e);
-        sh = s;
+        float t, e;
+        mod_two_sum(sh, oh, t, e);
+        sh = t;
         sl = __fadd_rn(sl, __fadd_rn(ol, e));
       }
       if (lane == 0) a.rs[p] = make_float2(sh, sl);
     }
     __syncthreads();
-    // y = A_G v0 - (v_k / 2 / M k + (sumBG - beta) v0) (:344), thread per position
-    // in float-float; sumBG = |adj(i) ∩ G| - k K_G / 2 / M in integers (:258-266)
-    if (threadIdx.x == 0) scal_ff[0] = ff_mul(vk, half_inv_m);  // v_k / 2 / M
-    __syncthreads();
-    const float2 c = scal_ff[0];
-    float2 py[1] = {make_float2(0.0f, 0.0f)};
-    float2* yf = reinterpret_cast<float2*>(a.y);
+    // thread per position: x_{s-1} = y_{s-1} / |y_{s-1}| (:349-351), its
+    // distances to x_{s-2} (:352-357), and y_s = A_G x_{s-1} - (v_k / 2 / M k
+    // + (sumBG - beta) x_{s-1}) (:344); sumBG = |adj(i) ∩ G| - k K_G / 2 / M
+    // in integers (:258-266)
+    float2 pe[4] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f),
+                    make_float2(0.0f, 0.0f)};
     for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
       const int i = a.rows[p];
       const long long k = a.rp[i + 1] - a.rp[i];
+      const float2 x = s == 1 ? a.vf[p] : ff_mul(yb[yprv + p], inv);
+      if (s > 1) {
+        const float2 old = a.vf[xold + p];
+        a.vf[xcur + p] = x;
+        const float2 d = ff_add(x, ff_neg(old)), u = ff_add(x, old);
+        pe[2] = ff_add(pe[2], ff_mul(d, d));
+        pe[3] = ff_add(pe[3], ff_mul(u, u));
+      }
       const float2 sbg =
           ff_from_ll((long long)(a.lrp[p + 1] - a.lrp[p]) - k * kg / 2 / a.M);
-      const float2 v0 = a.vf[cur + p];
-      const float2 corr = ff_add(ff_mulf(c, (float)k), ff_mul(ff_add(sbg, nbeta), v0));
-      const float2 t = ff_add(a.rs[p], ff_neg(corr));
-      yf[p] = t;
-      py[0] = ff_add(py[0], ff_mul(t, t));
+      const float2 corr = ff_add(ff_mulf(c, (float)k), ff_mul(ff_add(sbg, nbeta), x));
+      const float2 y = ff_add(ff_mul(a.rs[p], inv), ff_neg(corr));
+      yb[ycur + p] = y;
+      if (self_stage) stage[p - off] = y;  // the gathers of this step are over
+      pe[0] = ff_add(pe[0], ff_mul(y, y));
+      pe[1] = ff_add(pe[1], ff_mulf(y, (float)k));
     }
-    float2 ty[1];
-    block_partials_ff<1>(py, parts2, 1, aw, ty);
-    if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, parts2, 1, a.limit_ns, ty)) return false;
-    if (threadIdx.x == 0) {  // VectorNorm (:383-389) and its reciprocal, one sequence
-      const float2 inv = ff_rsqrt(ty[0]);
-      scal_ff[1] = ty[0].x == 0.0f ? make_float2(0.0f, 0.0f) : ff_mul(ty[0], inv);  // sqrt(0) = 0
-      scal_ff[2] = inv;
+    float2 te[4];
+    block_partials_ff<4>(pe, parts2, 1, aw, te);
+    if (nb > 1 && !group_sync_reduce<4>(g, nb, b0, parts2, 1, a.limit_ns, te)) return false;
+    it = s - 1;
+    if (s > 1) {
+      err1 = te[2];
+      err2 = te[3];
+      if (!(ff_gt(err1, eps2) && ff_gt(err2, eps2) && it < a.max_iter)) break;
+    }
+    // VectorNorm (:383-389), its reciprocal and v_k / 2 / M of x_s, one thread
+    if (threadIdx.x == 0) {
+      const float2 r = ff_rsqrt(te[0]);
+      scal_ff[0] = r;
+      scal_ff[1] = te[0].x == 0.0f ? make_float2(0.0f, 0.0f) : ff_mul(te[0], r);  // sqrt(0) = 0
+      scal_ff[2] = ff_mul(ff_mul(te[1], r), half_inv_m);
     }
     __syncthreads();
+    inv = scal_ff[0];
     vn = scal_ff[1];
-    const float2 inv = scal_ff[2];
-    // v = y / |y|, |v - v0|^2, |v + v0|^2, v.k (:349-357, :333-335) in
-    // float-float; the block's own positions, so no cross-block read
-    float2 pe[3] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
-    for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
-      const int i = a.rows[p];
-      const float2 x = ff_mul(yf[p], inv);  // y / |y| through the reciprocal
-      const float2 old = a.vf[cur + p];
-      a.vf[nxt + p] = x;
-      if (self_stage) stage[p - off] = x;  // phase A of this step is over
-      const float2 d = ff_add(x, ff_neg(old)), s = ff_add(x, old);
-      pe[0] = ff_add(pe[0], ff_mul(d, d));
-      pe[1] = ff_add(pe[1], ff_mul(s, s));
-      pe[2] = ff_add(pe[2], ff_mulf(x, (float)(a.rp[i + 1] - a.rp[i])));
-    }
-    float2 te[3];
-    block_partials_ff<3>(pe, parts2, 2, aw, te);
-    if (nb > 1 && !group_sync_reduce<3>(g, nb, b0, parts2, 2, a.limit_ns, te)) return false;
-    err1 = te[0];
-    err2 = te[1];
-    vk = te[2];
-    ++it;
+    c = scal_ff[2];
   }
   // eigenvalue sign (:369-375): the first node of G with the largest |v|
   // (node 0 when none exceeds |v[0]|, v[0] taken as 0 off G); side sizes (:276-281)
