@@ -53,14 +53,14 @@ struct ModGroup {
   long long subp, subn;
   int fbuf;      // buffer (0/1) of the final eigenvector iterate
   unsigned int bar_count, bar_gen;
-  float2 res[8];  // totals published by the last block to reach a barrier
+  unsigned int arrive;  // blocks' arrivals at the summing barriers of this launch
 };
 
 constexpr int kModThreads = 1024;
 constexpr int kModWarps = kModThreads / 32;
-// Partial sums per block, each phase in slots of its own: 0 start vector,
-// 1-4 a power step's |y|^2, y.k and the two norms, 8-11 the eigenvalue sign
-// and side sizes.
+// Partial sums per block: slots 0-3 and 4-7 hold the sums of the summing
+// barriers (start vector; a power step's |y|^2, y.k and the two norms) of
+// even and odd barrier number, 8-11 the eigenvalue sign and side sizes.
 constexpr int kModParts = 12;
 // Groups of at most this many nodes keep their iterate ((hi, lo) floats) in
 // shared memory during the gathers: 96 KB.
@@ -336,31 +336,36 @@ __global__ void mod_fill_kernel(int nrows, const int32_t* __restrict__ rows,
   }
 }
 
-// Barrier among the group's blocks that also sums partial k0 .. k0 + W - 1
-// of every block: the last block to arrive reduces them in a fixed order
-// (as group_reduce), publishes the totals in g->res and releases the others,
-// so each value is read from the partials once, not once per block.
+// Summing barrier number `epoch` (1, 2, ... in every block of the group, in
+// the same sequence): the block's W float-float values go to its partial
+// slots of the barrier's parity, the block counts its arrival, waits for the
+// group's nb * epoch arrivals (bounded: a longer wait than limit_ns raises
+// g->err and returns false) and then sums every block's partials itself in
+// the group's fixed order, so all blocks hold the same totals.  Two slot sets
+// suffice: a block can rewrite a set only after every block has arrived at
+// the barrier in between, that is, after every block has read the set.
 template <int W>
-__device__ __forceinline__ bool group_sync_reduce(ModGroup* g, int nb, int b0,
-                                                  const float2* parts, int k0,
-                                                  uint64_t limit_ns, float2 (&out)[W]) {
-  __shared__ int last_s, ok_s;
-  __syncthreads();
+__device__ __forceinline__ bool group_sums(float2 (&a)[W], ModGroup* g, int nb, int b0, int aw,
+                                           float2* parts, unsigned int& epoch, uint64_t limit_ns,
+                                           float2 (&out)[W]) {
+  __shared__ int ok_s;
+  ++epoch;
+  const int k0 = (int)(epoch & 1u) * 4;
+  block_partials_ff<W>(a, parts, k0, aw, out);  // ends with __syncthreads
+  if (nb == 1) return true;  // a group of one block takes its own totals
   if (threadIdx.x == 0) {
-    volatile unsigned int* gen = &g->bar_gen;
-    const unsigned int g0 = *gen;  // cannot advance before this block arrives
-    __threadfence();
-    const bool last = atomicAdd(&g->bar_count, 1u) == (unsigned int)nb - 1;
-    last_s = last ? 1 : 0;
-    ok_s = 1;
-    if (!last) {
+    const unsigned int target = (unsigned int)nb * epoch;
+    __threadfence();  // the block's partials before its arrival
+    int ok = 1;
+    if (atomicAdd(&g->arrive, 1u) + 1u < target) {
+      volatile unsigned int* c = &g->arrive;
       uint64_t t0;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-      while (*gen == g0) {
+      while (*c < target) {
         uint64_t t1;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
         if (t1 - t0 > limit_ns) {
-          ok_s = 0;
+          ok = 0;
           atomicExch(&g->err, 1);
           break;
         }
@@ -368,26 +373,11 @@ __device__ __forceinline__ bool group_sync_reduce(ModGroup* g, int nb, int b0,
       }
     }
     __threadfence();
+    ok_s = ok;
   }
   __syncthreads();
-  if (last_s) {
-    float2 t[W];
-    group_reduce<W>(parts, b0, nb, k0, t);
-    if (threadIdx.x == 0) {
-#pragma unroll
-      for (int w = 0; w < W; ++w) g->res[k0 + w] = t[w];
-      g->bar_count = 0;
-      __threadfence();
-      atomicAdd(&g->bar_gen, 1u);
-    }
-#pragma unroll
-    for (int w = 0; w < W; ++w) out[w] = t[w];
-    __syncthreads();
-    return true;
-  }
   if (!ok_s) return false;
-#pragma unroll
-  for (int w = 0; w < W; ++w) out[w] = __ldcg(&g->res[k0 + w]);
+  group_reduce<W>(parts, b0, nb, k0, out);
   return true;
 }
 
@@ -430,7 +420,7 @@ __device__ __forceinline__ int edge_col(const ModArgs& a, const uint16_t* s16, c
 __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb, int p0, int p1,
                             long long kg, double beta, float2* stage, const uint16_t* s16,
                             const int32_t* s32, double* lambda, int* iters, double* resid,
-                            int* fbuf, long long* subp, long long* subn) {
+                            int* fbuf, long long* subp, long long* subn, unsigned int& epoch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int off = g->row_off, nr = g->rows;
   const double Md = (double)a.M;
@@ -445,6 +435,7 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
     const int i = a.rows[p];
     const float2 x = ff_from_ll(i);
     a.vf[p] = x;
+    a.vd[p] = (double)i;  // the double iterate of a node without edges
     yb[p] = x;  // y_0 = x_0 with 1 / |y_0| taken as 1
     if (self_stage) stage[p - off] = x;
     p1s[0] = ff_add(p1s[0], ff_mulf(ff_from_ll(i), (float)(a.rp[i + 1] - a.rp[i])));
@@ -462,8 +453,7 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   float2* parts2 = reinterpret_cast<float2*>(a.parts);
   // a group of one block takes its own totals: no global barrier, no L2 round trip
   float2 t1[1];
-  block_partials_ff<1>(p1s, parts2, 0, aw, t1);
-  if (nb > 1 && !group_sync_reduce<1>(g, nb, b0, parts2, 0, a.limit_ns, t1)) return false;
+  if (!group_sums<1>(p1s, g, nb, b0, aw, parts2, epoch, a.limit_ns, t1)) return false;
   // Power steps (:327-366) with one group barrier each.  Step s gathers the
   // unnormalised y_{s-1} (published before the previous barrier) and scales
   // the row sums by 1 / |y_{s-1}|, since A (y / |y|) = (A y) / |y|; it forms
@@ -525,6 +515,28 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
     for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
       const int i = a.rows[p];
       const long long k = a.rp[i + 1] - a.rp[i];
+      if (k == 0) {
+        // A node without edges: y = beta x (no gather term, sumBG = 0), so
+        // under beta > 0 its entry shrinks by a factor per step and can fall
+        // far below float's range while staying positive in the reference's
+        // doubles (and so counted on the positive side).  Its iterate stays
+        // in double (vd, by the parity of the float-float buffers).
+        double xd = a.vd[p];  // x_0 = i
+        if (s > 1) {
+          const double xo = a.vd[xold + p];
+          xd = __dmul_rn(__dmul_rn(beta, xo), ff_to_d(inv));
+          a.vd[xcur + p] = xd;
+          const double d = __dsub_rn(xd, xo), u = __dadd_rn(xd, xo);
+          pe[2] = ff_add(pe[2], mod_split(__dmul_rn(d, d)));
+          pe[3] = ff_add(pe[3], mod_split(__dmul_rn(u, u)));
+        }
+        const double yd = __dmul_rn(beta, xd);
+        const float2 y = mod_split(yd);
+        yb[ycur + p] = y;
+        if (self_stage) stage[p - off] = y;
+        pe[0] = ff_add(pe[0], mod_split(__dmul_rn(yd, yd)));
+        continue;
+      }
       const float2 x = s == 1 ? a.vf[p] : ff_mul(yb[yprv + p], inv);
       if (s > 1) {
         const float2 old = a.vf[xold + p];
@@ -543,8 +555,7 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
       pe[1] = ff_add(pe[1], ff_mulf(y, (float)k));
     }
     float2 te[4];
-    block_partials_ff<4>(pe, parts2, 1, aw, te);
-    if (nb > 1 && !group_sync_reduce<4>(g, nb, b0, parts2, 1, a.limit_ns, te)) return false;
+    if (!group_sums<4>(pe, g, nb, b0, aw, parts2, epoch, a.limit_ns, te)) return false;
     it = s - 1;
     if (s > 1) {
       err1 = te[2];
@@ -567,6 +578,8 @@ __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb
   // (node 0 when none exceeds |v[0]|, v[0] taken as 0 off G); side sizes (:276-281)
   const size_t fin = (size_t)(it & 1) * a.nrows, prv = (size_t)((it + 1) & 1) * a.nrows;
   for (int p = p0 + (int)threadIdx.x; p < p1; p += kModThreads) {
+    const int i = a.rows[p];
+    if (a.rp[i + 1] == a.rp[i]) continue;  // kept in double during the steps
     a.vd[fin + p] = ff_to_d(a.vf[fin + p]);
     a.vd[prv + p] = ff_to_d(a.vf[prv + p]);
   }
@@ -697,8 +710,9 @@ __global__ __launch_bounds__(kModThreads, 1) void mod_level_kernel(ModArgs a) {
   double lambda = 0, l2 = 0, res = 0;
   int its = 0, fb = 0;
   long long sp = 0, sn = 0;
+  unsigned int epoch = 0;  // summing barriers passed (the same count in every block of the group)
   if (!lead_vector(a, g, r, b0, nb, p0, p1, kg, 0.0, stage, s16, s32, &lambda, &its, &res, &fb,
-                   &sp, &sn))
+                   &sp, &sn, epoch))
     return;
   if (lb == 0 && threadIdx.x == 0) {
     g->iters[0] = its;
@@ -708,7 +722,7 @@ __global__ __launch_bounds__(kModThreads, 1) void mod_level_kernel(ModArgs a) {
   }
   if (lambda < 0) {  // the leading eigenvalue of B - lambda I (:271-272)
     if (!lead_vector(a, g, r, b0, nb, p0, p1, kg, -lambda, stage, s16, s32, &l2, &its, &res, &fb,
-                     &sp, &sn))
+                     &sp, &sn, epoch))
       return;
     lambda += l2;
     if (lb == 0 && threadIdx.x == 0) {
