@@ -1,0 +1,33 @@
+"""Small graphs with isolated nodes and tiny components, shared by the oracle
+and device modularity tests: a graph of two cliques, a pair and isolated
+nodes; a star beside a path; a sparse random graph of 500 nodes (many
+isolated nodes, pairs and small trees)."""
+import numpy as np
+
+
+def sym_csr(n, edges):
+    """Symmetric binary CSR (no self loops, no duplicates) of an edge list."""
+    adj = [set() for _ in range(n)]
+    for a, b in edges:
+        if a != b:
+            adj[a].add(int(b))
+            adj[b].add(int(a))
+    R = np.zeros(n + 1, np.int32)
+    C = []
+    for i in range(n):
+        C += sorted(adj[i])
+        R[i + 1] = len(C)
+    return R, np.array(C, np.int32)
+
+
+def sparse_graphs():
+    e = ([(i, j) for i in range(5) for j in range(i + 1, 5)] +
+         [(5 + i, 5 + j) for i in range(4) for j in range(i + 1, 4)] + [(12, 13)])
+    yield "cliques_isolated", sym_csr(16, e)
+    e = [(0, i) for i in range(1, 21)] + [(21 + i, 22 + i) for i in range(9)]
+    yield "star_path", sym_csr(31, e)
+    rng = np.random.default_rng(5)
+    yield "sparse500", sym_csr(500, [tuple(x) for x in rng.integers(0, 500, (375, 2))])
+
+
+SPARSE_CASES = ["cliques_isolated", "star_path", "sparse500"]

@@ -11,6 +11,7 @@ import pytest
 
 import cuda_newest20160331_gb300 as bna
 import oracle
+from sparse_graphs import SPARSE_CASES, sparse_graphs
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -615,37 +616,14 @@ def test_modularity_without_edges(builder):
     assert m == 1 and np.all(labels.cpu().numpy() == 1) and np.isnan(q)
 
 
-def _sym_csr(n, edges):
-    adj = [set() for _ in range(n)]
-    for a, b in edges:
-        if a != b:
-            adj[a].add(int(b))
-            adj[b].add(int(a))
-    R = np.zeros(n + 1, np.int32)
-    C = []
-    for i in range(n):
-        C += sorted(adj[i])
-        R[i + 1] = len(C)
-    return R, np.array(C, np.int32)
 
-
-def _sparse_graphs():
-    e = ([(i, j) for i in range(5) for j in range(i + 1, 5)] +
-         [(5 + i, 5 + j) for i in range(4) for j in range(i + 1, 4)] + [(12, 13)])
-    yield "cliques_isolated", _sym_csr(16, e)
-    e = [(0, i) for i in range(1, 21)] + [(21 + i, 22 + i) for i in range(9)]
-    yield "star_path", _sym_csr(31, e)
-    rng = np.random.default_rng(5)
-    yield "sparse500", _sym_csr(500, [tuple(x) for x in rng.integers(0, 500, (375, 2))])
-
-
-@pytest.mark.parametrize("name", ["cliques_isolated", "star_path", "sparse500"])
+@pytest.mark.parametrize("name", SPARSE_CASES)
 def test_modularity_isolated_nodes_and_small_components(builder, name):
     """Graphs with isolated nodes, two-node components, a star and a path:
     groups whose iterate collapses to zero (|y| = 0 stops with a NaN
     iterate, as in the reference), two-node groups and retries with
     beta = -lambda; labels, Q and every round against the oracle."""
-    R, C = dict(_sparse_graphs())[name]
+    R, C = dict(sparse_graphs())[name]
     csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), None, {})
     log, log_o = [], []
     labels, m, q = builder.modularity(csr, log=log)
