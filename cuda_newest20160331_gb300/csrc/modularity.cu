@@ -391,7 +391,8 @@ struct ModArgs {
   const int32_t* lci;      // group-local columns
   ModGroup* groups;
   const int32_t* blk_grp;  // group index of every block
-  double* vd;              // [2][nrows] iterate (double), by position
+  double* vd;              // [2][nrows] by position: the final and previous iterates in double;
+                           // during the steps, the iterate of nodes without edges
   float2* vf;              // [2][nrows] iterate (hi, lo), by position
   float2* rs;              // [nrows] float-float row sums of a step
   double* y;               // [2][nrows] unnormalised iterates (hi, lo floats)
@@ -406,10 +407,6 @@ struct ModArgs {
   uint64_t limit_ns;
 };
 
-// One Lead_Vector call (Modularity_CPU.cpp:315-377) of group g with the
-// given beta, run by the group's blocks; block lb owns positions [p0, p1).
-// Returns false when a barrier wait expired.  On return: *lambda,
-// iterations, residual, final buffer, the sizes of the two signs.
 // Column (group-local index) of in-group edge e: from the block's slice in
 // shared memory (s16 / s32, first edge eb0) when it was loaded there.
 __device__ __forceinline__ int edge_col(const ModArgs& a, const uint16_t* s16, const int32_t* s32,
@@ -417,6 +414,11 @@ __device__ __forceinline__ int edge_col(const ModArgs& a, const uint16_t* s16, c
   return s16 ? (int)s16[e - eb0] : s32 ? s32[e - eb0] : __ldg(a.lci + e);
 }
 
+// One Lead_Vector call (Modularity_CPU.cpp:315-377) of group g with the
+// given beta, run by the group's blocks; this block owns positions [p0, p1).
+// Returns false when a barrier wait expired.  On return: *lambda,
+// iterations, residual, final buffer (the final and the previous iterate
+// in vd, double), the sizes of the two signs.
 __device__ bool lead_vector(const ModArgs& a, ModGroup* g, int r, int b0, int nb, int p0, int p1,
                             long long kg, double beta, float2* stage, const uint16_t* s16,
                             const int32_t* s32, double* lambda, int* iters, double* resid,
