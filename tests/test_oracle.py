@@ -10,7 +10,7 @@ import pytest
 
 import cuda_newest20160331_gb300 as bna
 import oracle
-from sparse_graphs import SPARSE_CASES, sparse_graphs
+from sparse_graphs import SPARSE_CASES, sparse_graphs, sym_csr
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = [
@@ -233,6 +233,23 @@ def test_modularity_oracle_against_compiled_reference_random():
         lab_r, m_r = oracle.ref_modularity(R, C)
         lab_o, _, m_o, _ = oracle.modularity(R, C)
         assert m_r == m_o and np.array_equal(lab_r, lab_o)
+
+
+def test_modularity_oracle_against_compiled_reference_random_sparse():
+    """Random edge lists of 0.2 to 3 edges per node (isolated nodes, pairs,
+    trees and one larger component): the reference tool's labels."""
+    if oracle.ref_m() is None:
+        pytest.skip("reference tree not present on this host")
+    rng = np.random.default_rng(2026)
+    for _ in range(10):
+        n = int(rng.integers(5, 700))
+        m = int(rng.integers(1, max(2, int(n * rng.uniform(0.2, 3.0)))))
+        R, C = sym_csr(n, [tuple(x) for x in rng.integers(0, n, (m, 2))])
+        if len(C) == 0:
+            continue
+        lab_r, m_r = oracle.ref_modularity(R, C)
+        lab_o, _, m_o, _ = oracle.modularity(R, C)
+        assert m_r == m_o and np.array_equal(lab_r, lab_o), (n, m)
 
 
 @pytest.mark.parametrize("name", SPARSE_CASES)
