@@ -279,8 +279,9 @@ int32_t bna_zscore_ld(int32_t T);
  * the norm used in the last iteration.  Values are read as float and
  * promoted to double (weighted-net.cu:295-297); a NULL val means every entry
  * is 1 (U/CUEC/CUEC/CUEC_unweighted.cu:47-52).  Only the first 2*floor(nnz/2)
- * entries are used (weighted-net.cu:61).  Vectors, norms and the stop test are
- * FP64.  Returns BNA_NOT_CONVERGED (outputs still written) at max_iter. */
+ * entries are used (weighted-net.cu:61).  Each row sum runs in float-float
+ * (about 48 significant bits); vectors, norms and the stop test are FP64.
+ * Returns BNA_NOT_CONVERGED (outputs still written) at max_iter. */
 int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr_dev, int32_t max_iter, double eps, double* ec_dev,
                double* lambda, int32_t* iters, void* stream);
 
