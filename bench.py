@@ -2,8 +2,11 @@
 
 One step = one pass of the path over the workload's BOLD already resident in
 HBM: z-score, count pass, near-threshold recompute, offset scan, fill pass.
-Default workload: N=45,000 voxels x T=240 (float32, seeded factor model,
-K=40), weighted CSR at 1 % density (tau = the FP64 quantile).
+Default workload: the 180k-voxel network, N=180,000 voxels x T=1,200
+(float32, seeded factor model, K=60 networks of contiguous 500-voxel blocks),
+r >= 0.4 into a weighted CSR (about 1.6e8 directed entries), then eigenvector
+centrality on the device-resident CSR.  The line also times the plain FP32
+and TF32 forms on the same input and reports max |r - r_fp64| of each form.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P]
                   [--workload n45k|small|n180k|n45k_density|batch64|serving]
@@ -18,8 +21,9 @@ budget), latency p50/p99 and each request's slowdown against running alone.
 --gpus N > 1 runs under torchrun: every rank builds its own replica of the
 workload (the path has no cross-GPU exchange: replicas only), barrier + max
 over ranks; value = all ranks' edges / time.  --impl reference times the
-reference's own multi-threaded CPU correlation tool (its arithmetic restated
-in the oracle) on a bounded row sample of the same workload.
+reference's own multi-threaded CPU tool (correlation, FormFullGraph and
+FormCSRGraph, restated in the oracle) on a bounded row sample of the same
+workload, fed by the oracle's copy of the generator.
 """
 from __future__ import annotations
 
@@ -46,7 +50,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--precision", default="bf16x3")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison")
-    p.add_argument("--workload", default="n45k")
+    p.add_argument("--workload", default="n180k")
     p.add_argument("--impl", default="gb300")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -99,35 +103,108 @@ def cpu_model() -> str:
     return "unknown"
 
 
-def cpu_sample(w, bold, seconds: float, threads: int) -> dict:
-    """Reference CPU arithmetic (CorMat_cpu_MT + |r| > tau) on a row sample,
-    sized from a calibration run to take about `seconds`; edges/s over the
-    sampled pairs (the fixed per-call transpose is part of the timed work)."""
-    import oracle
-    N, T = w.N, w.T
-    t0 = time.perf_counter()
-    oracle.rows_mt_f32_count(bold, 0, 1, w.value, threads)
-    fixed = time.perf_counter() - t0
-    rows = 64
-    t0 = time.perf_counter()
-    oracle.rows_mt_f32_count(bold, 0, rows, w.value, threads)
-    dt = max(time.perf_counter() - t0 - fixed, 1e-3)
-    pairs_per_s = sum(N - 1 - i for i in range(rows)) / dt
-    target_pairs = pairs_per_s * max(seconds - fixed, 0.5)
-    acc, r1 = 0, 0
-    while acc < target_pairs and r1 < N:
-        acc += N - 1 - r1
-        r1 += 1
-    t0 = time.perf_counter()
-    edges = oracle.rows_mt_f32_count(bold, 0, r1, w.value, threads)
-    dt = time.perf_counter() - t0
-    pairs = sum(N - 1 - i for i in range(r1))
-    return {"value": 2 * edges / dt, "unit": "edges/s", "cores": threads, "kind": "port",
-            "sample": f"rows 0..{r1} of N={N} (pairs i<j: {pairs}), T={T}; "
-                      f"CorMat_cpu_MT arithmetic (float accumulation, |r| > tau), "
-                      f"{2 * edges} directed edges in {dt:.2f} s on {cpu_model()}",
-            "seconds": dt, "pairs_per_s": pairs / dt,
-            "tflops": pairs * 2 * T / dt / 1e12}
+def sample_rows(N: int, n: int):
+    """n rows spread evenly over [0, N) (their pairs j > i average N / 2)."""
+    return sorted({min(N - 1, int((k + 0.5) * N / n)) for k in range(n)})
+
+
+class CpuReference:
+    """The reference's CPU tool on a bounded sample of the workload.
+
+    U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp: CorMat_cpu_MT's cross terms
+    (float accumulation, all host threads) for the pairs (i, j > i) of a set
+    of rows spread over the matrix, then its FormFullGraph / FormCSRGraph
+    steps (single-threaded, as in the reference) restricted to those pairs,
+    with the workload's threshold rule and the pair values in the CSR (the
+    weighted tree's FormCSRGraph).  Restated in the oracle's C; the one-time
+    transpose and centring run once, outside the sample."""
+
+    def __init__(self, w, bold_h, threads: int):
+        import oracle
+        self.w, self.threads, self.oracle = w, threads, oracle
+        t0 = time.perf_counter()
+        self.bt, self.m2 = oracle.mt_prepare(bold_h)
+        self.prepare_s = time.perf_counter() - t0
+        self.rate = None
+
+    def run(self, n_rows: int) -> dict:
+        w = self.w
+        rows = sample_rows(w.N, n_rows)
+        t0 = time.perf_counter()
+        R, Cc, V, secs = self.oracle.mt_rows_csr(self.bt, self.m2, rows, w.mode, w.value,
+                                                 self.threads, weighted=w.weighted)
+        dt = time.perf_counter() - t0
+        pairs = sum(w.N - 1 - i for i in rows)
+        self.rate = pairs / dt
+        return {"rows": len(rows), "pairs": pairs, "nnz": len(Cc), "seconds": dt,
+                "step_seconds": [float(x) for x in secs]}
+
+    def sample(self, seconds: float) -> dict:
+        """One sample sized to take about `seconds` (from the last run's rate)."""
+        w = self.w
+        if self.rate is None:
+            self.run(4)
+        n = max(2, min(w.N, int(seconds * self.rate / max(1.0, (w.N - 1) / 2.0))))
+        r = self.run(n)
+        total = w.N * (w.N - 1) // 2
+        r.update({
+            "value": r["nnz"] / r["seconds"], "unit": "edges/s", "cores": self.threads,
+            "kind": "port", "pairs_per_s": r["pairs"] / r["seconds"],
+            "tflops": r["pairs"] * 2.0 * w.T / r["seconds"] / 1e12,
+            "full_job_s_extrapolated": self.prepare_s + total * r["seconds"] / r["pairs"],
+            "sample": (f"{r['rows']} rows spread over N={w.N} (pairs i<j with i in the sample: "
+                       f"{r['pairs']}, {r['pairs'] / total:.3%} of all), T={w.T}; the reference "
+                       f"CPU tool (CorMat_cpu_MT cross terms on {self.threads} threads, then "
+                       f"FormFullGraph + FormCSRGraph on the sample's pairs, single-threaded as "
+                       f"in the reference; {w.describe()}): {r['nnz']} directed CSR entries in "
+                       f"{r['seconds']:.2f} s on {cpu_model()}; the one-time transpose and "
+                       f"centring ({self.prepare_s:.1f} s) are outside the sample"),
+        })
+        return r
+
+
+def bench_config(w, world: int) -> dict:
+    """The config both arms print (the same dict for the same workload)."""
+    return {"workload": w.describe(), "parallelism": f"replicas x{world} (no collective)",
+            "l2": "inputs larger than L2 on the GPU arm (and a 2x L2 buffer zeroed between "
+                  "timed steps, outside the events); host memory on the CPU arm"}
+
+
+def max_abs_err(b, bold, bold_h, precision: str, n_tiles: int = 16, seed: int = 7) -> dict:
+    """max |r - r_fp64| over sampled 128 x 128 tiles: the form's approximate r
+    (bna_corr_tile_values) against r computed in FP64 from the float input
+    (centred, L2-normalised, dotted in double); the diagonal is excluded."""
+    import numpy as np
+    T, N = bold_h.shape
+    nb = (N + 127) // 128
+    rng = np.random.default_rng(seed)
+    tiles = {(0, 0), (nb - 1, nb - 1), (0, nb - 1)}
+    while len(tiles) < min(n_tiles, nb * (nb + 1) // 2):
+        I, J = sorted(int(x) for x in rng.integers(0, nb, 2))
+        tiles.add((I, J))
+
+    def z64(blk):
+        x = bold_h[:, blk * 128:min(N, blk * 128 + 128)].astype(np.float64)
+        x = x - x.mean(axis=0)
+        return (x / np.sqrt((x * x).sum(axis=0))).T
+
+    worst, pairs = 0.0, 0
+    for I, J in sorted(tiles):
+        v = b.tile_values(bold, I, J, precision=precision).cpu().numpy().astype(np.float64)
+        zi, zj = z64(I), z64(J)
+        r64 = zi @ zj.T
+        d = np.abs(v[:r64.shape[0], :r64.shape[1]] - r64)
+        if I == J:
+            np.fill_diagonal(d, 0.0)
+            pairs += r64.shape[0] * (r64.shape[0] - 1) // 2
+        else:
+            pairs += r64.size
+        d = d[np.isfinite(d)]
+        if d.size:
+            worst = max(worst, float(d.max()))
+    return {"value": worst, "tiles": len(tiles), "pairs": pairs,
+            "sample": f"{len(tiles)} seeded 128x128 tiles ({pairs} pairs) against r in FP64 "
+                      "from the float input"}
 
 
 class ClockSampler:
@@ -414,33 +491,38 @@ def load_traffic(kernel: str, workload: str):
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores (rank 0 only): the oracle's
+    restatement of its CPU tool, fed by the oracle's copy of the generator, so
+    nothing of the product library is loaded."""
     rank, world, local = dist_env()
     if rank != 0:
         return
+    import oracle
     from cuda_newest20160331_gb300 import workloads
     w = workloads.get(args.workload)
-    bold = w.bold()
+    bold = oracle.synth_bold(**w.synth_args())
     cores = host_cores()
-    vals = []
+    ref = CpuReference(w, bold, cores)
+    per_step = args.cpu_seconds / max(1, args.steps)
     for _ in range(args.warmup):
-        cpu_sample(w, bold, min(2.0, args.cpu_seconds / 4), cores)
-    samples = [cpu_sample(w, bold, args.cpu_seconds / max(1, args.steps), cores)
-               for _ in range(args.steps)]
-    vals = [s["value"] for s in samples]
-    v = statistics.median(vals)
-    s0 = samples[0]
+        ref.sample(min(per_step, 1.0))
+    samples = [ref.sample(per_step) for _ in range(args.steps)]
+    v = statistics.median(s["value"] for s in samples)
+    s0 = samples[len(samples) // 2]
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "edges/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * statistics.median(s["seconds"] for s in samples),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded factor model)",
-        "config": {"workload": f"{w.name}: N={w.N} T={w.T} K={w.K} {w.mode} {'percent' if w.mode == 'density' else 'tau'}={w.value:.6f}",
-                   "l2": "inputs on host (CPU run)"},
+        "config": bench_config(w, world),
+        "precision": "f32 (float-accumulated cross terms)",
         "cpu_baseline": {"value": v, "unit": "edges/s", "cores": cores, "kind": "port",
                          "sample": s0["sample"]},
         "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "tflops_algorithmic": statistics.median(s["tflops"] for s in samples),
+        "pairs_per_s": statistics.median(s["pairs_per_s"] for s in samples),
+        "full_job_s_extrapolated": statistics.median(s["full_job_s_extrapolated"] for s in samples),
     }
     print(json.dumps(line), flush=True)
 
@@ -573,7 +655,8 @@ def main():
         return {"value": rp.nnz / (pm / 1000.0), "unit": "edges/s", "ms_per_step": pm,
                 "nnz": rp.nnz, "same_edge_count": rp.nnz == nnz,
                 "ms_count": rp.stats["ms_count"], "ms_recompute": rp.stats["ms_recompute"],
-                "band_candidates": rp.stats["band_candidates"], "delta": rp.stats["delta"],
+                "band_candidates": rp.stats["band_candidates"], "band_1e6": rp.stats["band_1e6"],
+                "delta": rp.stats["delta"],
                 "tflops_algorithmic": flop / (pm / 1000.0) / 1e12,
                 "speedup_of_chosen_form": pm / ms}
 
@@ -606,6 +689,15 @@ def main():
     h2d = N * T * 4
     d2h = (N + 1) * 4 + he_nnz * (8 if w.weighted else 4)
 
+    # max |r - r_fp64| of each form on sampled tiles (rewrites the context's
+    # z-scores, so it runs after every use of the step's CSR)
+    max_err = max_abs_err(b, bold, bold_h, precision)
+    if plain is not None:
+        plain["max_abs_r_minus_fp64"] = max_abs_err(b, bold, bold_h, "fp32")["value"]
+    if other_tc is not None:
+        other_tc["max_abs_r_minus_fp64"] = max_abs_err(
+            b, bold, bold_h, "tf32" if precision == "bf16x3" else "bf16x3")["value"]
+
     # dominant kernel: one correlation pass (count) over all N(N-1)/2 pairs
     cnt = statistics.median(s["ms_count"] for s in stats)
     fil = statistics.median(s["ms_fill"] for s in stats)
@@ -626,15 +718,14 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if precision == "fp32" else precision,
         "data": "synthetic (seeded factor model, device-resident input)",
-        "config": {"workload": f"{w.name}: N={N} T={T} K={w.K} {w.mode} {'percent' if w.mode == 'density' else 'tau'}={w.value:.6f} "
-                               f"weighted={w.weighted}",
-                   "precision": precision, "parallelism": f"replicas x{world}",
-                   "l2": "flushed between steps (2x L2 buffer zeroed outside the timed events)"},
+        "config": bench_config(w, world),
+        "precision": precision,
         "tflops_algorithmic": flop * world / (ms / 1000.0) / 1e12,
         "nnz": nnz, "stage_ms": {k: statistics.median(s[k] for s in stats) for k in
                                  ("ms_zscore", "ms_count", "ms_recompute", "ms_scan", "ms_fill")},
         "band_candidates": stats[-1]["band_candidates"], "band_1e6": stats[-1]["band_1e6"],
         "delta": stats[-1]["delta"],
+        "max_abs_r_minus_fp64": max_err,
         "roofline": roof,
         "plain_fp32": plain,
         ("tf32" if precision == "bf16x3" else "bf16x3"): other_tc,
@@ -648,8 +739,10 @@ def main():
     if serve is not None:
         line["serve"] = serve
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb = cpu_sample(w, bold_h, args.cpu_seconds, host_cores())
+        ref = CpuReference(w, bold_h, host_cores())
+        cb = ref.sample(args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"]["full_job_s_extrapolated"] = cb["full_job_s_extrapolated"]
         if "skipped" not in line["modularity"]:
             line["modularity"]["small_vs_cpu"] = modularity_small_pair(b, stream)
     if rank == 0:

@@ -41,8 +41,18 @@ class Workload:
 
     def bold(self, threads: int = 0):
         from . import synth_bold
-        return synth_bold(self.N, self.T, self.K, self.seed, kind=self.kind, threads=threads,
-                          **self.synth)
+        return synth_bold(**self.synth_args(), threads=threads)
+
+    def synth_args(self) -> dict:
+        """Generator arguments (the same for the library's and the oracle's generator)."""
+        return dict(N=self.N, T=self.T, K=self.K, seed=self.seed, kind=self.kind, **self.synth)
+
+    def describe(self) -> str:
+        rule = {"r_gt": "r > tau", "r_ge": "r >= tau", "abs_gt": "|r| > tau",
+                "abs_ge": "|r| >= tau", "density": "density"}[self.mode]
+        val = f"{self.value:g} %" if self.mode == "density" else f"tau={self.value:.6f}"
+        return (f"{self.name}: N={self.N} T={self.T} K={self.K} {self.kind} loadings, "
+                f"{rule} ({val}), {'weighted' if self.weighted else 'binary'} CSR")
 
 
 def n45k_tau() -> float:

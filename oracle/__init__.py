@@ -60,6 +60,13 @@ def lib():
         o.orc_modularity.argtypes = [P, P, C.c_int, C.c_double, P, C.POINTER(C.c_double),
                                      C.POINTER(C.c_int), P, C.POINTER(C.c_int)]
         o.orc_modularity.restype = C.c_int
+        o.orc_synth_bold.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double,
+                                     C.c_double, C.c_double, C.c_int, C.c_int, P, C.c_int]
+        o.orc_synth_bold.restype = C.c_int
+        o.orc_mt_prepare.argtypes = [P, C.c_int, C.c_int, P, P]
+        o.orc_mt_rows_csr.argtypes = [P, P, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_float,
+                                      C.c_int, P, P, P, C.c_int64, P]
+        o.orc_mt_rows_csr.restype = C.c_int64
         _o = o
     return _o
 
@@ -242,6 +249,54 @@ def rows_mt_f32_count(bold: np.ndarray, row0: int, row1: int, tau: float, thread
     bold = np.ascontiguousarray(bold, np.float32)
     T, N = bold.shape
     return int(lib().orc_rows_mt_f32_count(_p(bold), N, T, row0, row1, tau, threads))
+
+
+SYNTH_KINDS = {"iid": 0, "blocknet": 1}
+
+
+def synth_bold(N: int, T: int, K: int, seed: int, kind: str = "iid", phi: float = 0.7,
+               load_sd: float = 0.3, jitter_sd: float = 0.0, block: int = 500,
+               n_net: int = 60, threads: int = 0) -> np.ndarray:
+    """The workloads' seeded factor-model BOLD (float32 [T][N]), restated in
+    C so that a CPU-only run needs nothing from the product library."""
+    out = np.empty((T, N), np.float32)
+    th = threads or (os.cpu_count() or 1)
+    rc = lib().orc_synth_bold(N, T, K, SYNTH_KINDS[kind], seed, phi, load_sd, jitter_sd, block,
+                              n_net, _p(out), th)
+    if rc != 0:
+        raise ValueError("bad synthetic-input parameters")
+    return out
+
+
+def mt_prepare(bold: np.ndarray):
+    """-> (centred voxel-major rows [N][L], m2 [N]): CorMat_cpu_MT's one-time part."""
+    bold = np.ascontiguousarray(bold, np.float32)
+    L, N = bold.shape
+    bt = np.empty((N, L), np.float32)
+    m2 = np.empty(N, np.float32)
+    lib().orc_mt_prepare(_p(bold), N, L, _p(bt), _p(m2))
+    return bt, m2
+
+
+def mt_rows_csr(bt: np.ndarray, m2: np.ndarray, rows, mode: str, tau: float, threads: int,
+                weighted: bool = True):
+    """The reference CPU tool's per-pair work on the pairs (i in rows, j > i):
+    cross terms on `threads` threads, then its FormFullGraph / FormCSRGraph
+    steps restricted to the sample.  -> (R [N+1], C, V or None, seconds of
+    the three steps)."""
+    N, L = bt.shape
+    S = np.ascontiguousarray(np.unique(np.asarray(rows, np.int32)))
+    R = np.empty(N + 1, np.int32)
+    secs = np.zeros(3)
+    cap = max(1 << 20, int(2 * sum(N - 1 - int(i) for i in S) * 0.02))
+    while True:
+        Cc = np.empty(cap, np.int32)
+        V = np.empty(cap, np.float32) if weighted else None
+        nnz = lib().orc_mt_rows_csr(_p(bt), _p(m2), N, L, _p(S), len(S), MODES[mode], tau,
+                                    threads, _p(R), _p(Cc), _p(V), cap, _p(secs))
+        if nnz >= 0:
+            return R, Cc[:nnz], (V[:nnz] if weighted else None), secs
+        cap = -nnz - 1
 
 
 def csr_corr(bold: np.ndarray, mode: str, tau: float, weighted: bool = True, threads: int = 0):

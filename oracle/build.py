@@ -1,9 +1,9 @@
 """ORACLE build recipe — test infrastructure only.
 
 1. oracle/liboracle.so from oracle.c (the CPU restatement; builds anywhere).
-2. When the reference tree is present (it is only on the development host),
-   oracle/_ref/ gets the reference's own CPU sources compiled as they lie
-   there, with the Linux shim headers of refshim/:
+2. When the reference tree is present (it is only on the development host;
+   BNA_REFERENCE_ROOT names its root), oracle/_ref/ gets the reference's own
+   CPU sources compiled as they lie there, with the shim headers of refshim/:
      libref_w.so  W/CorMat/CUCorMat/CUCorMat/CorMat.cpp   + ref_glue_w.cpp
      libref_u.so  U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp + ref_glue_u.cpp
      libref_m.so  U/Newman_Modularity_CPU/Modularity_CPU/Modularity_CPU.cpp
@@ -18,7 +18,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference/cuda_newest20160331"
+# the reference tree (read-only); BNA_REFERENCE_ROOT points elsewhere, and
+# where the tree is absent only liboracle.so is built
+REF_ROOT = os.environ.get("BNA_REFERENCE_ROOT", "/root/reference/cuda_newest20160331")
 W_SRC = os.path.join(REF_ROOT, "BNAPlatform-weighted-win64-cuda7.0-20160331", "src",
                      "CorMat", "CUCorMat", "CUCorMat", "CorMat.cpp")
 U_SRC = os.path.join(REF_ROOT, "BNAPlatform-win64-cuda7.0-20160115", "src",

@@ -19,14 +19,21 @@
  *                                                  :652-666 (division, inv_fishertrans :44-50)
  *   orc_cormat_mt_f32   CorMat_cpu_MT/Cross_term   U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:283-383
  *                       (float accumulation; used as the multi-core CPU baseline)
+ *   orc_mt_prepare,     the same tool with its graph  CorMat_CPU.cpp:190-226, 283-383 (CSR
+ *   orc_mt_rows_csr     steps on a row sample      values as W's CorMat.cpp:889-918): the
+ *                                                  timed CPU baseline, CSR assembly included
+ *   orc_synth_bold      the workloads' seeded factor-model input (no reference counterpart),
+ *                       so the CPU baseline needs nothing from the product library
  * Built with -ffp-contract=off so every operation rounds like the reference's
  * scalar code.
  */
+#define _POSIX_C_SOURCE 200809L
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 enum { R_GT = 0, R_GE = 1, ABS_GT = 2, ABS_GE = 3 };
 
@@ -575,4 +582,272 @@ int orc_modularity(const int32_t* R, const int32_t* C, int N, double lambda_min,
   free(verr);
   free(sumbg);
   return modules;
+}
+
+/* ---- synthetic input, restated for the reference arm ---------------------
+ * The seeded factor-model generator of the workloads, restated here so the
+ * reference's CPU path can be fed without loading the product library:
+ *   x_i(t) = sum_k L_ik f_k(t) + eps_i(t), f_k AR(1) with coefficient phi and
+ *   unit stationary variance (innovation sqrt(1 - phi^2), 100 burn-in steps),
+ *   eps ~ N(0, 1); kind 0: L_ik = load_sd * N(0,1); kind 1 (block network):
+ *   voxel i is in block i / block, network (block mod n_net), L_ik =
+ *   load_sd * g[net][k] + jitter_sd * N(0,1).
+ * Random numbers: a counter hash (murmur3's 64-bit finaliser over the seed,
+ * stream, index and draw) mapped to (0, 1); normals by Marsaglia's polar
+ * method; ln by the atanh series of the mantissa (no libm), so every host
+ * gives the same bits.  Output float32 time-major [T][N]. */
+static uint64_t syn_mix(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdULL;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ULL;
+  k ^= k >> 33;
+  return k;
+}
+
+static double syn_u01(uint64_t seed, uint64_t stream, uint64_t idx, uint64_t draw) {
+  uint64_t h = syn_mix((seed * 0x9E3779B97F4A7C15ULL) ^ (stream * 0xD1B54A32D192ED03ULL));
+  h = syn_mix(h ^ (idx * 0x8CB92BA72F3D8DD7ULL));
+  h = syn_mix(h ^ (draw * 0xABC98388FB8FAC03ULL + 0x632BE59BD9B4E019ULL));
+  return (double)(h >> 11) * 0x1.0p-53 + 0x1.0p-54;
+}
+
+static double syn_ln(double x) {
+  uint64_t bits;
+  memcpy(&bits, &x, 8);
+  int ex = (int)((bits >> 52) & 0x7ff) - 1023;
+  bits = (bits & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+  double m;
+  memcpy(&m, &bits, 8);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    ex += 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0), s2 = s * s;
+  double acc = 1.0 / 25.0;
+  for (int k = 11; k >= 0; --k) acc = acc * s2 + 1.0 / (double)(2 * k + 1);
+  return (double)ex * 0x1.62e42fefa39efp-1 + 2.0 * s * acc;
+}
+
+static double syn_normal(uint64_t seed, uint64_t stream, uint64_t idx) {
+  for (uint64_t d = 0;; d += 2) {
+    const double a = 2.0 * syn_u01(seed, stream, idx, d) - 1.0;
+    const double b = 2.0 * syn_u01(seed, stream, idx, d + 1) - 1.0;
+    const double q = a * a + b * b;
+    if (q > 0.0 && q < 1.0) return a * sqrt(-2.0 * syn_ln(q) / q);
+  }
+}
+
+struct syn_job {
+  int N, T, K, kind, block, n_net, tid, nth;
+  uint64_t seed;
+  double load_sd, jitter_sd;
+  const double* f; const double* g;
+  float* out;
+};
+
+static void* syn_worker(void* p) {
+  struct syn_job* jb = (struct syn_job*)p;
+  const int K = jb->K, T = jb->T, N = jb->N;
+  double* L = (double*)malloc(sizeof(double) * (size_t)256 * (K > 0 ? K : 1));
+  for (int c = jb->tid; c * 256 < N; c += jb->nth) {
+    const int i0 = c * 256, i1 = i0 + 256 < N ? i0 + 256 : N;
+    for (int i = i0; i < i1; ++i)
+      for (int k = 0; k < K; ++k) {
+        const double h = syn_normal(jb->seed, 2, (uint64_t)i * K + k);
+        L[(size_t)(i - i0) * K + k] =
+            jb->kind == 1 ? jb->load_sd * jb->g[(size_t)((i / jb->block) % jb->n_net) * K + k] +
+                                jb->jitter_sd * h
+                          : jb->load_sd * h;
+      }
+    for (int t = 0; t < T; ++t)
+      for (int i = i0; i < i1; ++i) {
+        double x = 0.0;
+        for (int k = 0; k < K; ++k) x = x + L[(size_t)(i - i0) * K + k] * jb->f[(size_t)k * T + t];
+        x = x + syn_normal(jb->seed, 4, (uint64_t)i * T + t);
+        jb->out[(size_t)t * N + i] = (float)x;
+      }
+  }
+  free(L);
+  return NULL;
+}
+
+int orc_synth_bold(int N, int T, int K, int kind, uint64_t seed, double phi, double load_sd,
+                   double jitter_sd, int block, int n_net, float* out, int nthreads) {
+  if (N <= 0 || T <= 0 || K < 0 || (kind == 1 && (block <= 0 || n_net <= 0))) return -1;
+  const int burn = 100;
+  const double innov = sqrt(1.0 - phi * phi);
+  double* f = (double*)malloc(sizeof(double) * ((size_t)K * T + 1));
+  for (int k = 0; k < K; ++k) {
+    double v = 0.0;
+    for (int t = 0; t < burn + T; ++t) {
+      v = phi * v + innov * syn_normal(seed, 1, (uint64_t)k * (burn + T) + t);
+      if (t >= burn) f[(size_t)k * T + (t - burn)] = v;
+    }
+  }
+  double* g = NULL;
+  if (kind == 1) {
+    g = (double*)malloc(sizeof(double) * ((size_t)n_net * K + 1));
+    for (int n = 0; n < n_net; ++n)
+      for (int k = 0; k < K; ++k) g[(size_t)n * K + k] = syn_normal(seed, 3, (uint64_t)n * K + k);
+  }
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  struct syn_job jobs[256];
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t] = (struct syn_job){N, T, K, kind, block, n_net, t, nthreads, seed, load_sd, jitter_sd,
+                               f, g, out};
+    if (t > 0) pthread_create(&th[t], NULL, syn_worker, &jobs[t]);
+  }
+  syn_worker(&jobs[0]);
+  for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+  free(f);
+  free(g);
+  return 0;
+}
+
+/* ---- the reference's CPU tool on a row sample, CSR included --------------
+ * U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp runs CorMat_cpu_MT (:283-337:
+ * transpose, float-centred rows, m2 = sqrt(sum x^2 - (sum x)^2 / L) from
+ * double sums), Cross_term (:340-383: float-accumulated cross terms,
+ * r = sum3 / m2_i / m2_j, 0 when a moment is 0, j strided by thread id) into
+ * the packed triangle, then FormFullGraph (:190-206: the N x N bool matrix,
+ * cleared, both (i,j) and (j,i) set per edge) and FormCSRGraph (:209-226: a
+ * row-major scan of that matrix); the weighted tree's FormCSRGraph also
+ * copies each edge's r (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:889-918).
+ *
+ * orc_mt_prepare is the one-time part (transpose, moments, centring).
+ * orc_mt_rows_csr runs the per-pair part for the pairs (i, j > i) of a set
+ * of sample rows S (ascending): cross terms on `nthreads` threads as
+ * Cross_term does, then, single-threaded as in the reference, the graph and
+ * CSR steps restricted to the sample: the bool rows of S (full width N) and,
+ * for rows outside S, their bool columns at S, cleared and set like
+ * FormFullGraph, then scanned row by row like FormCSRGraph.  R has N + 1
+ * entries; C / V (cap entries, V may be NULL) receive the sample's directed
+ * entries in CSR order.  Returns nnz, or -nnz - 1 when nnz > cap (C / V
+ * untouched past cap).  secs (optional) gets the seconds of the three steps. */
+void orc_mt_prepare(const float* bold, int N, int L, float* bt, float* m2) {
+  /* the transpose in 64 x 64 blocks (a copy: the order does not change a value) */
+  for (int l0 = 0; l0 < L; l0 += 64)
+    for (int i0 = 0; i0 < N; i0 += 64)
+      for (int i = i0; i < i0 + 64 && i < N; ++i)
+        for (int l = l0; l < l0 + 64 && l < L; ++l) bt[(size_t)i * L + l] = bold[(size_t)l * N + i];
+  for (int i = 0; i < N; ++i) {
+    double s1 = 0, s2 = 0;
+    float* row = bt + (size_t)i * L;
+    for (int l = 0; l < L; ++l) {
+      s1 += row[l];
+      s2 += row[l] * row[l];
+    }
+    m2[i] = (float)sqrt(s2 - s1 * s1 / L);
+    s1 /= L;
+    for (int l = 0; l < L; ++l) row[l] -= (float)s1;
+  }
+}
+
+struct mts_job {
+  const float* bt; const float* m2; const int32_t* S; int ns, N, L, tid, nth;
+  const int64_t* off; float* out;
+};
+
+static void* mts_worker(void* p) {
+  struct mts_job* jb = (struct mts_job*)p;
+  for (int s = 0; s < jb->ns; ++s) {
+    const int i = jb->S[s];
+    float* o = jb->out + jb->off[s];
+    for (int j = i + 1 + jb->tid; j < jb->N; j += jb->nth) {
+      float s3 = 0;
+      for (int l = 0; l < jb->L; ++l) s3 += jb->bt[(size_t)i * jb->L + l] * jb->bt[(size_t)j * jb->L + l];
+      float r = s3 / jb->m2[i] / jb->m2[j];
+      if (jb->m2[i] == 0 || jb->m2[j] == 0) r = 0;
+      o[j - i - 1] = r;
+    }
+  }
+  return NULL;
+}
+
+static double orc_now(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+int64_t orc_mt_rows_csr(const float* bt, const float* m2, int N, int L, const int32_t* S, int ns,
+                        int mode, float tau, int nthreads, int32_t* R, int32_t* C, float* V,
+                        int64_t cap, double* secs) {
+  const double t0 = orc_now();
+  int64_t* off = (int64_t*)malloc(sizeof(int64_t) * ((size_t)ns + 1));
+  int32_t* pos = (int32_t*)malloc(sizeof(int32_t) * (size_t)N); /* row -> sample slot or -1 */
+  off[0] = 0;
+  for (int s = 0; s < ns; ++s) off[s + 1] = off[s] + (N - 1 - S[s]);
+  for (int i = 0; i < N; ++i) pos[i] = -1;
+  for (int s = 0; s < ns; ++s) pos[S[s]] = s;
+  float* rs = (float*)malloc(sizeof(float) * ((size_t)off[ns] + 1));
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  struct mts_job jobs[256];
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t] = (struct mts_job){bt, m2, S, ns, N, L, t, nthreads, off, rs};
+    if (t > 0) pthread_create(&th[t], NULL, mts_worker, &jobs[t]);
+  }
+  mts_worker(&jobs[0]);
+  for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+  const double t1 = orc_now();
+  /* FormFullGraph on the sample: rows of S at full width, other rows' columns at S */
+  unsigned char* rows = (unsigned char*)malloc((size_t)ns * N);
+  unsigned char* cols = (unsigned char*)malloc((size_t)N * ns);
+  memset(rows, 0, (size_t)ns * N);
+  memset(cols, 0, (size_t)N * ns);
+  for (int s = 0; s < ns; ++s) {
+    const int i = S[s];
+    const float* o = rs + off[s];
+    for (int j = i + 1; j < N; ++j) {
+      if (!is_edge(o[j - i - 1], mode, tau)) continue;
+      rows[(size_t)s * N + j] = 1;
+      if (pos[j] >= 0) rows[(size_t)pos[j] * N + i] = 1;
+      else cols[(size_t)j * ns + s] = 1;
+    }
+  }
+  const double t2 = orc_now();
+  /* FormCSRGraph: row-major scan; a value is the pair's r from the sample */
+  int64_t nnz = 0;
+  R[0] = 0;
+  for (int i = 0; i < N; ++i) {
+    if (pos[i] >= 0) {
+      const unsigned char* a = rows + (size_t)pos[i] * N;
+      for (int j = 0; j < N; ++j) {
+        if (!a[j]) continue;
+        if (nnz < cap) {
+          C[nnz] = j;
+          if (V) V[nnz] = i < j ? rs[off[pos[i]] + (j - i - 1)] : rs[off[pos[j]] + (i - j - 1)];
+        }
+        ++nnz;
+      }
+    } else {
+      const unsigned char* a = cols + (size_t)i * ns;
+      for (int s = 0; s < ns; ++s) {
+        if (!a[s]) continue;
+        if (nnz < cap) {
+          C[nnz] = S[s];
+          if (V) V[nnz] = rs[off[s] + (i - S[s] - 1)];
+        }
+        ++nnz;
+      }
+    }
+    R[i + 1] = (int32_t)nnz;
+  }
+  const double t3 = orc_now();
+  if (secs) {
+    secs[0] = t1 - t0;
+    secs[1] = t2 - t1;
+    secs[2] = t3 - t2;
+  }
+  free(rows);
+  free(cols);
+  free(rs);
+  free(pos);
+  free(off);
+  return nnz <= cap ? nnz : -nnz - 1;
 }
