@@ -17,7 +17,7 @@ BNA_NOT_CONVERGED = 4
 BNA_CAPACITY = 13
 BNA_OVER_BUDGET = 14
 OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1, "ec_iters_per_launch": 2}
-THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4}
+THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4, "r_eps": 5}
 PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2, "auto": 3}
 SYNTH_KINDS = {"iid": 0, "blocknet": 1}
 

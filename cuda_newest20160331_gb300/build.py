@@ -92,10 +92,14 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
     # command-line drop-ins (cli/*.cpp -> bin/bna_<name>), linked to libbna.so
     os.makedirs(BIN, exist_ok=True)
     tools = []
-    for src in sorted(glob.glob(os.path.join(PKG, "cli", "*.cpp"))):
-        exe = os.path.join(BIN, "bna_" + os.path.splitext(os.path.basename(src))[0])
+    # cormat.cpp also as bna_cormat_u, the unweighted tree's CUCorMat
+    variants = [(src, os.path.splitext(os.path.basename(src))[0], [])
+                for src in sorted(glob.glob(os.path.join(PKG, "cli", "*.cpp")))]
+    variants += [(os.path.join(PKG, "cli", "cormat.cpp"), "cormat_u", ["-DBNA_UNWEIGHTED_TREE"])]
+    for src, name, defs in variants:
+        exe = os.path.join(BIN, "bna_" + name)
         if _stale(exe, src, deps + [LIB]):
-            tools.append(["g++", "-O2", "-std=c++17", src, "-o", exe, "-I", INCLUDE,
+            tools.append(["g++", "-O2", "-std=c++17", *defs, src, "-o", exe, "-I", INCLUDE,
                           "-I", os.path.join(cuda, "include"), "-L", PKG, "-lbna",
                           "-L", os.path.join(cuda, "lib64"), "-lcudart",
                           "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath," + os.path.join(cuda, "lib64")])

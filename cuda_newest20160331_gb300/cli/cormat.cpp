@@ -12,6 +12,11 @@
 // letter f: Fisher z) to Dir/<dirname>_<files>_<N>_spa<s>%_cor<r>.csr.
 // The correlation form comes from BNA_PRECISION (bf16x3 by default, or tf32 /
 // fp32); every form gives the same edge set.
+//
+// Built a second time with BNA_UNWEIGHTED_TREE as bna_cormat_u, the drop-in
+// for the unweighted tree's CUCorMat (U/CorMat/CUCorMat/CUCORMAT/CorMat.cpp,
+// same arguments): per-subject files go to Dir/unweighted/<name>_<N>_spa<s>%
+// _cor<r>.csr and every .csr is binary (R and C only, :340-345).
 #include <cuda_runtime.h>
 #include <dirent.h>
 #include <sys/stat.h>
@@ -28,6 +33,16 @@
 namespace {
 
 bna_ctx* g_ctx = nullptr;
+
+#ifdef BNA_UNWEIGHTED_TREE
+const char* const kSubdir = "unweighted";  // U/.../CUCORMAT/CorMat.cpp:290-296
+const char* const kSuffix = "";
+constexpr bool kWeighted = false;
+#else
+const char* const kSubdir = "weighted";
+const char* const kSuffix = "_weighted";
+constexpr bool kWeighted = true;
+#endif
 
 void die(const char* what, int st) {
   std::fprintf(stderr, "%s: %s (%s)\n", what, bna_status_string(st),
@@ -75,7 +90,8 @@ void write_cormat(const std::string& path, const float* packed_dev, long long M1
   std::fclose(f);
 }
 
-// CSR to host and to the .csr file (CorMat.cpp:353-360).
+// CSR to host and to the .csr file (CorMat.cpp:353-360); the unweighted
+// tree's files hold no value section.
 void write_csr_dev(const std::string& path, const bna_csr& d) {
   bna_csr h{};
   h.n = d.n;
@@ -83,13 +99,15 @@ void write_csr_dev(const std::string& path, const bna_csr& d) {
   std::vector<int32_t> rp(d.n + 1), ci(std::max<int64_t>(d.nnz, 1));
   std::vector<float> va(std::max<int64_t>(d.nnz, 1));
   ck(cudaMemcpy(rp.data(), d.row_ptr, (size_t)(d.n + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+  const bool vals = kWeighted && d.val;
   if (d.nnz) {
     ck(cudaMemcpy(ci.data(), d.col_idx, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost), "copy");
-    ck(cudaMemcpy(va.data(), d.val, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost), "copy");
+    if (vals)
+      ck(cudaMemcpy(va.data(), d.val, (size_t)d.nnz * 4, cudaMemcpyDeviceToHost), "copy");
   }
   h.row_ptr = rp.data();
   h.col_idx = ci.data();
-  h.val = va.data();
+  h.val = vals ? va.data() : nullptr;
   std::printf("generating %s...\n", path.c_str());
   const int st = bna_csr_write(path.c_str(), &h);
   if (st) die("bna_csr_write", st);
@@ -181,11 +199,11 @@ int main(int argc, char* argv[]) {
   const int pk_prec = prec == BNA_PREC_FP32 ? BNA_PREC_BF16X3 : prec;
 
   if (per_subject) {
-    mkdir((dir + "/weighted").c_str(), 0755);
+    mkdir((dir + "/" + kSubdir).c_str(), 0755);
     for (size_t f = 0; f < files.size(); ++f) {
       std::printf("\ncalculating correlation for %s/%s ...\n", dir.c_str(), files[f].c_str());
       const std::string stem = files[f].substr(0, files[f].find_last_of('.'));
-      const std::string out = dir + "/weighted/" + stem + "_" + std::to_string(N);
+      const std::string out = dir + "/" + kSubdir + "/" + stem + "_" + std::to_string(N);
       if (cormat_flag) {
         if ((st = bna_corr_packed(g_ctx, 1, &bold_dev[f], N, &Ts[f], 0, pk_prec, packed, nullptr)))
           die("bna_corr_packed", st);
@@ -210,7 +228,7 @@ int main(int argc, char* argv[]) {
               (st = bna_csr_rethreshold(g_ctx, &base, BNA_THR_R_GT, t, &c, nullptr, nullptr)))
             die("bna_csr_rethreshold", st);
           const double spa = 100.0 * (double)c.nnz / (double)M1 / 2;  // CorMat.cpp:323
-          write_csr_dev(out + fmt_spa(spa, (float)t) + "_weighted.csr", c);
+          write_csr_dev(out + fmt_spa(spa, (float)t) + kSuffix + ".csr", c);
         }
       } else {
         for (double sp : thr) {
@@ -220,7 +238,7 @@ int main(int argc, char* argv[]) {
           bna_csr c{};
           if ((st = bna_corr_csr(g_ctx, bold_dev[f], N, Ts[f], &o, &c, &s, nullptr)))
             die("bna_corr_csr", st);
-          write_csr_dev(out + fmt_spa((float)sp, (float)s.tau) + "_weighted.csr", c);
+          write_csr_dev(out + fmt_spa((float)sp, (float)s.tau) + kSuffix + ".csr", c);
         }
       }
     }

@@ -806,12 +806,25 @@ int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* op
   return BNA_OK;
 }
 
+// Known threshold rules, and the float the kernels compare against: tau as
+// the reference's float, or for the 2mm tools' rule (r > tau - 1e-6 in
+// double) the smallest float above tau - 1e-6.
+static bool mode_known(int m) { return m >= BNA_THR_R_GT && m <= BNA_THR_R_EPS; }
+static float rule_tau(const bna_corr_opts* o) {
+  const float t = (float)o->value;
+  if (o->mode != BNA_THR_R_EPS) return t;
+  const double lo = (double)t - 1e-6;
+  float f = (float)lo;
+  if ((double)f <= lo) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
 int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
                      const bna_corr_opts* opts, bna_csr* out_dev, bna_corr_stats* stats,
                      void* stream) {
   if (!ctx || !bold_dev || !opts || !out_dev || N < 1 || T < 1)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: bad arguments");
-  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY)
+  if (!mode_known(opts->mode))
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown threshold mode %d", opts->mode);
   if (opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_AUTO)
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr: unknown precision %d", opts->precision);
@@ -886,7 +899,7 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
   for (int wtry = 0;; ++wtry) {
     if (!density) {
       a.th.mode = opts->mode;
-      a.th.tau = (float)opts->value;
+      a.th.tau = rule_tau(opts);
       a.th.delta = (float)delta;
     } else if (k_dens == 0) {
       a.th.mode = BNA_THR_R_GT;  // no edge at all
@@ -1424,9 +1437,11 @@ int32_t bna_corr_csr_avg(bna_ctx* ctx, int32_t nsub, const float* const* bold_de
   opts = &opts_r;
   s = avg_check(ctx, nsub, bold_dev, N, T, opts->precision);
   if (s) return s;
-  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
+  if (!mode_known(opts->mode) ||
       (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_avg: bad threshold rule");
+  if (opts->mode == BNA_THR_R_EPS)
+    return fail(ctx, BNA_UNSUPPORTED, "bna_corr_csr_avg: the 2mm tools' rule has no average");
   const int prec = opts->precision;
   s = set_device(ctx, as_stream(stream));
   if (s) return s;
@@ -1548,7 +1563,7 @@ int32_t batch_prep(bna_ctx* ctx, BatchSubj& b, const float* bold, const bna_corr
   b.k_dens = density ? bna_density_nnz(b.N, opts->value) / 2 : 0;
   if (!density) {
     a.th.mode = opts->mode;
-    a.th.tau = (float)opts->value;
+    a.th.tau = rule_tau(opts);
     a.th.delta = (float)b.delta;
   } else if (b.k_dens == 0) {
     a.th.mode = BNA_THR_R_GT;
@@ -1654,7 +1669,7 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
   for (int k = 0; k < nsub; ++k)
     if (!bold_dev[k] || N[k] < 1 || T[k] < 1)
       return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_batch: subject %d: bad arguments", k);
-  if (opts->mode < BNA_THR_R_GT || opts->mode > BNA_THR_DENSITY ||
+  if (!mode_known(opts->mode) ||
       opts->precision < BNA_PREC_FP32 || opts->precision > BNA_PREC_AUTO ||
       (opts->mode == BNA_THR_DENSITY && !(opts->value >= 0.0 && opts->value <= 100.0)))
     return fail(ctx, BNA_BAD_ARG, "bna_corr_csr_batch: bad options");

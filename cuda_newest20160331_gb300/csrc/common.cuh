@@ -76,10 +76,17 @@ struct AvgPass {
   float unc_lim;
 };
 
-// Exact decision on the reference's value r (after post_block clamping).
+// 1 + 1e-6 as the 2mm tools compare it, (double)r <= 1.0 + 1e-6: the largest
+// float not above it is 1 + 8 * 2^-23.
+constexpr float kEpsHi = 1.00000095367431640625f;
+
+// Exact decision on the reference's value r (after post_block clamping; the
+// raw value in BNA_THR_R_EPS, whose th.tau is the smallest float above
+// tau - 1e-6 in double, so r >= th.tau is the tools' r > tau - ep).
 __device__ __forceinline__ bool edge_exact(float r, const Threshold& th) {
   switch (th.mode) {
     case BNA_THR_R_GT: return r > th.tau;
+    case BNA_THR_R_EPS: return r >= th.tau && r <= kEpsHi;
     case BNA_THR_ABS_GT: return fabsf(r) > th.tau;
     case BNA_THR_ABS_GE: return fabsf(r) >= th.tau;
     default: return r >= th.tau;  // R_GE and DENSITY

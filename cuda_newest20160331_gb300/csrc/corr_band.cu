@@ -4,7 +4,8 @@
 // near 1) is evaluated with the reference CPU arithmetic of CorMat_cpu
 // (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:955-964): float products of the
 // float z-scores, accumulated in double in time order, rounded to float;
-// then post_block's clamp (CorMat.cpp:883) and the exact threshold rule.
+// then post_block's clamp (CorMat.cpp:883; not for the 2mm tools' rule,
+// BNA_THR_R_EPS) and the exact threshold rule.
 // Sequential per pair, so the value is bit-identical to the reference's.
 //
 // Scan: seg[b][i] (edges of row i in column block b) becomes the exclusive
@@ -55,7 +56,7 @@ __global__ void recompute_kernel(CorrArgs a) {
     const uint2 p = a.cand[c];
     if (p.x == kCandNone) continue;  // unused slot of a count-pass chunk
     const int i = (int)p.x, j = (int)p.y;
-    const float r = a.cand_val ? a.cand_val[c] : exact_r_warp(a, i, j, lane);
+    const float r = a.cand_val ? a.cand_val[c] : exact_r_rule(a, i, j, lane);
     if (lane != 0) continue;
     const unsigned long long key = pair_key(i, j);
     bool e = edge_exact(r, a.th);

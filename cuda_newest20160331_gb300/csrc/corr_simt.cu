@@ -180,6 +180,7 @@ __global__ __launch_bounds__(256, 2) void corr_simt_kernel(CorrArgs a, int nt, i
         acc[i][j] = 0.f;  // NaN voxel: the exact value is 0 (post_block)
         const float x = 0.0f - a.th.tau;
         c = x > a.th.delta ? CLS_EDGE : (x < -a.th.delta ? CLS_NO : CLS_BAND);
+        if (a.th.mode == BNA_THR_R_EPS) c = CLS_NO;  // NaN is never an edge there
       } else if (PACKED && ((a.avg_unc[packed_index(gi, gj, a.n) >> 5] >>
                               (packed_index(gi, gj, a.n) & 31)) & 1u)) {
         c = CLS_BAND;  // some subject's value may be clamped by post_block

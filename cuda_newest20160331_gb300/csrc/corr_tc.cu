@@ -345,8 +345,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // -1 can be an edge only through post_block's 0 for tau <= 0 in the signed
       // rules (|r| rules cover -1 like +1).
       simple = (tau < lim) && (ABS || lo_thr > 0.0f);
-      // a pair with a NaN voxel has the exact value 0 (post_block)
-      zero_int = (0.0f >= lo_thr) || (0.0f >= lim);
+      // a pair with a NaN voxel has the exact value 0 (post_block); in the 2mm
+      // tools' rule it stays NaN and is never an edge
+      zero_int = a.th.mode != BNA_THR_R_EPS && ((0.0f >= lo_thr) || (0.0f >= lim));
       if (PASS == 0) {
         long long x = 0;
         if (lane < 4) x = a.wstate[wid * 4 + lane];

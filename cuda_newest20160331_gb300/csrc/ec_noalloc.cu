@@ -1,27 +1,36 @@
 // Eigenvector centrality for callers that cannot allocate device memory.
 //
 // Some callers cannot call cudaMalloc at the point where they need
-// centrality: code running inside a host callback or a stream-ordered
-// allocator hook, processes whose device memory is fully reserved by their
-// own pool, or embedders that forbid the library any allocation after load.
-// bna_ec_noalloc serves them: it runs the same power-iteration kernels as
-// bna_ec, but its working vectors, block partials and iteration state live
-// in one file-scope __device__ array of fixed size, so the call itself
-// allocates nothing (no cudaMalloc / cudaFree, no context, no pinned buffer,
-// no graph).  The caller passes the CSR and the output vector.
+// centrality: a process whose device memory is fully reserved by its own
+// pool (another framework's caching allocator holding the rest of HBM), or
+// an embedder that forbids the library any allocation after load so that
+// its memory use stays fixed and known in advance.  bna_ec_noalloc serves
+// them: it runs the same power-iteration kernels as bna_ec, but its working
+// vectors, block partials and iteration state live in one file-scope
+// __device__ array of fixed size, so the call itself allocates nothing (no
+// cudaMalloc / cudaFree, no context, no pinned buffer, no graph).  The
+// caller passes the CSR and the output vector.
+//
+// It is called from ordinary host code: it issues CUDA calls (memset, kernel
+// launches, copies, a stream synchronisation), which CUDA does not allow
+// inside a stream callback or a cudaLaunchHostFunc function.
 //
 // Limits and sharing rules:
 //   - N <= kNoAllocMaxN (262,144 vertices); larger graphs get
-//     BNA_SCRATCH_LIMIT.  The array holds 2 * kNoAllocMaxN doubles plus block
+//     BNA_SCRATCH_LIMIT.  The array holds 4 * kNoAllocMaxN doubles plus block
 //     partials and state (about 8 MB); every GPU that loads the library keeps
 //     it until the process exits.
 //   - Every call shares the array.  Calls that overlap on a GPU (two host
 //     threads, or two streams running at once) race on it; serialise them.
 //   - The first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (a one-time set-up per device, done with that
-//     device current).  Make that first call before any stream capture.
+//     device current).  Make that first call before any stream capture.  The
+//     address is kept per CUDA context (its unique id): after a
+//     cudaDeviceReset the next call looks it up again in the new context.
 #include <algorithm>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "common.cuh"
 
@@ -60,12 +69,34 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 double* g_scratch_ptr[kMaxDevices] = {};
 int g_sms[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 
-// One-time set-up per device (the device must be current).
+// Unique id of the current CUDA context (cuCtxGetId through the runtime's
+// driver entry point), or 0 when it cannot be read.
+unsigned long long current_ctx_id() {
+  using Fn = CUresult (*)(CUcontext, unsigned long long*);
+  static Fn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (Fn) nullptr;
+    }
+    return reinterpret_cast<Fn>(p);
+  }();
+  unsigned long long id = 0;
+  if (!fn || fn(nullptr, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// One-time set-up per device and context (the device must be current).
 int32_t setup_device(int dev, double** ptr, int* sms) {
   if (dev < 0 || dev >= kMaxDevices) return BNA_BAD_ARG;
   std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
+  const unsigned long long ctx = current_ctx_id();
+  if (!g_scratch_ptr[dev] || ctx == 0 || ctx != g_ctx_id[dev]) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_ec_scratch) != cudaSuccess || p == nullptr) {
       cudaGetLastError();
@@ -78,6 +109,7 @@ int32_t setup_device(int dev, double** ptr, int* sms) {
     }
     g_sms[dev] = n;
     g_scratch_ptr[dev] = static_cast<double*>(p);
+    g_ctx_id[dev] = ctx;
   }
   *ptr = g_scratch_ptr[dev];
   *sms = g_sms[dev];

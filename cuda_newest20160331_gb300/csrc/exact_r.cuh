@@ -12,10 +12,11 @@ namespace bna {
 // partial sum is then representable).  A warp evaluates one pair: lanes take
 // t = lane, lane+32, ..., the exact sum is an int64 fixed-point reduction
 // across the warp, and only when the condition fails does lane 0 run the
-// sequential double adds.  Returns the value after post_block's clamp.
-__device__ __forceinline__ float exact_r_warp_z(const float* z, const uint8_t* bad, int ldz,
-                                                int T, int i, int j, int lane) {
-  if (bad[i] | bad[j]) return 0.0f;  // NaN -> 0 in post_block
+// sequential double adds.  Returns the raw value (NaN for a voxel with a NaN
+// z-score); exact_r_warp_z gives it after post_block's clamp.
+__device__ __forceinline__ float exact_r_warp_raw(const float* z, const uint8_t* bad, int ldz,
+                                                  int T, int i, int j, int lane) {
+  if (bad[i] | bad[j]) return __int_as_float(0x7fc00000);  // NaN
   const float* zi = z + (size_t)i * ldz;
   const float* zj = z + (size_t)j * ldz;
   int emin = 1 << 20;
@@ -64,11 +65,22 @@ __device__ __forceinline__ float exact_r_warp_z(const float* z, const uint8_t* b
       r = __double2float_rn(s);
     }
   }
-  return post_block(__shfl_sync(0xffffffffu, r, 0));
+  return __shfl_sync(0xffffffffu, r, 0);
+}
+
+__device__ __forceinline__ float exact_r_warp_z(const float* z, const uint8_t* bad, int ldz,
+                                                int T, int i, int j, int lane) {
+  return post_block(exact_r_warp_raw(z, bad, ldz, T, i, j, lane));
 }
 
 __device__ __forceinline__ float exact_r_warp(const CorrArgs& a, int i, int j, int lane) {
   return exact_r_warp_z(a.z, a.bad, a.ldz, a.T, i, j, lane);
+}
+
+// The value a rule decides on: post_block's, or the raw one for BNA_THR_R_EPS.
+__device__ __forceinline__ float exact_r_rule(const CorrArgs& a, int i, int j, int lane) {
+  const float raw = exact_r_warp_raw(a.z, a.bad, a.ldz, a.T, i, j, lane);
+  return a.th.mode == BNA_THR_R_EPS ? raw : post_block(raw);
 }
 
 // Binary search in ascending keys[0..n).

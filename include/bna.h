@@ -50,17 +50,26 @@ typedef enum bna_status {
 
 /* Threshold rules.  r below is the reference's value after post_block
  * (W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:869-884): a correlation outside
- * [-1, 1] (or NaN from a zero-variance voxel) becomes 0.  The diagonal is
- * never an edge. */
+ * [-1, 1] (or NaN from a zero-variance voxel) becomes 0, except in
+ * BNA_THR_R_EPS, which compares the unclamped value.  The diagonal is never
+ * an edge. */
 typedef enum bna_thr_mode {
   BNA_THR_R_GT = 0,   /* r >  tau : FormFullGraph, CorMat.cpp:696 (CUCorMat "r" mode) */
   BNA_THR_R_GE = 1,   /* r >= tau */
   BNA_THR_ABS_GT = 2, /* |r| > tau: FormFullGraph, U/CorMat/CorMat_CPU/CorMat/CorMat_CPU.cpp:198 */
   BNA_THR_ABS_GE = 3, /* |r| >= tau */
-  BNA_THR_DENSITY = 4 /* value = sparsity s in percent: exactly k = Clength/2 undirected edges,
+  BNA_THR_DENSITY = 4, /* value = sparsity s in percent: exactly k = Clength/2 undirected edges,
                          Clength = floor(2*M1*s/100) rounded up to even (CorMat.cpp:327-328);
                          tau = the k-th largest r; ties at tau kept in row-major (i<j) scan
                          order (FormFullGraph_s, CorMat.cpp:743-822) */
+  BNA_THR_R_EPS = 5   /* tau - 1e-6 < r <= 1 + 1e-6, both sides in double (r and tau as float,
+                         ep = 1e-6 a double): the 2mm and chunk GPU builders' rule,
+                         W/CuCorMat-2mm/CorMat-2mm.cu:13,140,156 and
+                         "CuCorMat-2mm - spa - GPUhisto-10n6 -chunk"/step2-dense2csr.cu:17,52.
+                         r is the reference CPU value without post_block's clamp (a
+                         zero-variance voxel's NaN never passes; 1 < r <= 1 + 8 ulp does).
+                         Single-subject and batch builds; not the averaging or
+                         re-thresholding entry points */
 } bna_thr_mode;
 
 /* Arithmetic of the correlation tiles.  Whatever the form, every pair whose
@@ -287,16 +296,18 @@ int32_t bna_ec(bna_ctx* ctx, const bna_csr* csr_dev, int32_t max_iter, double ep
 
 /* Eigenvector centrality without any allocation.  No counterpart in the
  * reference: for callers that cannot allocate device memory when they need
- * the result (a host callback or allocator hook, a process whose device
- * memory is held by its own pool, an embedder that forbids allocation after
- * load).  Same kernels and results as bna_ec, but the working vectors and
- * iteration state live in a fixed __device__ array of the library (about
- * 8 MB, kept by every GPU that loads the library until exit), so the call
- * allocates nothing; no context is needed.  Limit: n <= 262,144 vertices,
- * else BNA_SCRATCH_LIMIT.  All calls share that array: calls that overlap on
- * a GPU race, so serialise them.  The first call on a device looks up the
- * array's address (once per device); make it before any stream capture.
- * Synchronous: returns after ec_dev is written. */
+ * the result (a process whose device memory is held by its own pool, an
+ * embedder that forbids allocation after load).  Same kernels and results as
+ * bna_ec, but the working vectors and iteration state live in a fixed
+ * __device__ array of the library (about 8 MB, kept by every GPU that loads
+ * the library until exit), so the call allocates nothing; no context is
+ * needed.  Call it from ordinary host code, not from a stream callback or a
+ * cudaLaunchHostFunc function: it issues CUDA calls (launches, copies, a
+ * stream synchronisation), which CUDA forbids there.  Limit: n <= 262,144
+ * vertices, else BNA_SCRATCH_LIMIT.  All calls share that array: calls that
+ * overlap on a GPU race, so serialise them.  The first call on a device (and
+ * the first after a cudaDeviceReset) looks up the array's address; make it
+ * before any stream capture.  Synchronous: returns after ec_dev is written. */
 int32_t bna_ec_noalloc(const bna_csr* csr_dev, int32_t max_iter, double eps, double* ec_dev,
                        double* lambda, int32_t* iters, void* stream);
 

@@ -19,7 +19,7 @@ import numpy as np
 from . import build as _build
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3}
+MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "r_eps": 5}
 
 _o = None
 _rw = None
@@ -38,6 +38,9 @@ def lib():
         o.orc_pair_r.argtypes = [P, C.c_int, C.c_int, C.c_int]
         o.orc_pair_r.restype = C.c_float
         o.orc_cormat_packed.argtypes = [P, C.c_int, C.c_int, P, C.c_int]
+        o.orc_cormat_packed2.argtypes = [P, C.c_int, C.c_int, P, C.c_int, C.c_int]
+        o.orc_pair_r_raw.argtypes = [P, C.c_int, C.c_int, C.c_int]
+        o.orc_pair_r_raw.restype = C.c_float
         o.orc_threshold_csr.argtypes = [P, C.c_int, C.c_int, C.c_float, P, C.c_int64, P, P, P]
         o.orc_threshold_csr.restype = C.c_int64
         o.orc_density.argtypes = [P, C.c_int, C.c_double, C.POINTER(C.c_int64), P, C.c_int64,
@@ -160,11 +163,14 @@ def pair_r(z: np.ndarray, i: int, j: int) -> float:
     return float(lib().orc_pair_r(_p(z), z.shape[1], i, j))
 
 
-def cormat_packed(z: np.ndarray, threads: int = 0) -> np.ndarray:
+def cormat_packed(z: np.ndarray, threads: int = 0, raw: bool = False) -> np.ndarray:
+    """Packed upper triangle of the reference values (raw: without
+    post_block's clamp, NaN for a zero-variance voxel)."""
     z = np.ascontiguousarray(z, np.float32)
     N, T = z.shape
     out = np.empty(N * (N - 1) // 2, np.float32)
-    lib().orc_cormat_packed(_p(z), N, T, _p(out), threads or (os.cpu_count() or 1))
+    lib().orc_cormat_packed2(_p(z), N, T, _p(out), threads or (os.cpu_count() or 1),
+                             1 if raw else 0)
     return out
 
 
@@ -302,7 +308,7 @@ def mt_rows_csr(bt: np.ndarray, m2: np.ndarray, rows, mode: str, tau: float, thr
 def csr_corr(bold: np.ndarray, mode: str, tau: float, weighted: bool = True, threads: int = 0):
     """Full restated path: z-score -> packed r -> CSR."""
     z = zscore(bold)
-    packed = cormat_packed(z, threads)
+    packed = cormat_packed(z, threads, raw=(mode == "r_eps"))
     return threshold_csr(packed, bold.shape[1], mode, tau, weighted=weighted)
 
 

@@ -35,7 +35,7 @@
 #include <string.h>
 #include <time.h>
 
-enum { R_GT = 0, R_GE = 1, ABS_GT = 2, ABS_GE = 3 };
+enum { R_GT = 0, R_GE = 1, ABS_GT = 2, ABS_GE = 3, R_EPS = 5 };
 
 /* z[i*T + t] (voxel-major) from bold[t*N + i] (time-major). */
 void orc_zscore(const float* bold, int N, int T, float* z) {
@@ -53,8 +53,9 @@ void orc_zscore(const float* bold, int N, int T, float* z) {
 }
 
 /* The reference value of one pair: float products, double accumulation in
- * time order, rounded to float; then post_block's clamp. */
-float orc_pair_r(const float* z, int T, int i, int j) {
+ * time order, rounded to float (NaN for a zero-variance voxel); orc_pair_r
+ * then applies post_block's clamp. */
+float orc_pair_r_raw(const float* z, int T, int i, int j) {
   const float* a = z + (size_t)i * T;
   const float* b = z + (size_t)j * T;
   double s = 0;
@@ -62,7 +63,11 @@ float orc_pair_r(const float* z, int T, int i, int j) {
     const float p = a[l] * b[l];
     s += p;
   }
-  const float r = (float)s;
+  return (float)s;
+}
+
+float orc_pair_r(const float* z, int T, int i, int j) {
+  const float r = orc_pair_r_raw(z, T, i, j);
   return (r >= -1.0f && r <= 1.0f) ? r : 0.0f;
 }
 
@@ -70,32 +75,43 @@ static int64_t packed_index(int64_t N, int64_t i, int64_t j) { /* i < j, CorMat.
   return i * N - (1 + i) * i / 2 + j - (i + 1);
 }
 
-struct pk_job { const float* z; int N, T, tid, nth; float* out; };
+struct pk_job { const float* z; int N, T, tid, nth, raw; float* out; };
 
 static void* pk_worker(void* p) {
   struct pk_job* jb = (struct pk_job*)p;
   for (int i = jb->tid; i < jb->N; i += jb->nth)
     for (int j = i + 1; j < jb->N; ++j)
-      jb->out[packed_index(jb->N, i, j)] = orc_pair_r(jb->z, jb->T, i, j);
+      jb->out[packed_index(jb->N, i, j)] =
+          jb->raw ? orc_pair_r_raw(jb->z, jb->T, i, j) : orc_pair_r(jb->z, jb->T, i, j);
   return NULL;
 }
 
-/* packed[M1], M1 = N(N-1)/2, row-major over i < j. */
-void orc_cormat_packed(const float* z, int N, int T, float* packed, int nthreads) {
+/* packed[M1], M1 = N(N-1)/2, row-major over i < j; raw: without
+ * post_block's clamp (the values the 2mm tools' rule compares). */
+void orc_cormat_packed2(const float* z, int N, int T, float* packed, int nthreads, int raw) {
   if (nthreads < 1) nthreads = 1;
   pthread_t th[256];
   struct pk_job jobs[256];
   if (nthreads > 256) nthreads = 256;
   for (int t = 0; t < nthreads; ++t) {
-    jobs[t] = (struct pk_job){z, N, T, t, nthreads, packed};
+    jobs[t] = (struct pk_job){z, N, T, t, nthreads, raw, packed};
     if (t > 0) pthread_create(&th[t], NULL, pk_worker, &jobs[t]);
   }
   pk_worker(&jobs[0]);
   for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
 }
 
+void orc_cormat_packed(const float* z, int N, int T, float* packed, int nthreads) {
+  orc_cormat_packed2(z, N, T, packed, nthreads, 0);
+}
+
+/* R_EPS: the 2mm / chunk GPU tools' rule, CorMat-2mm.cu:140,156 and
+ * step2-dense2csr.cu:52, on the raw value: out > (r_thresh - ep) &&
+ * out <= (1 + ep) with ep the double 1e-6 (CorMat-2mm.cu:13), so both
+ * comparisons run in double. */
 static int is_edge(float r, int mode, float tau) {
   switch (mode) {
+    case R_EPS: return (double)r > (double)tau - 1e-6 && (double)r <= 1.0 + 1e-6;
     case R_GT: return r > tau;
     case ABS_GT: return fabsf(r) > tau;
     case ABS_GE: return fabsf(r) >= tau;
@@ -320,7 +336,9 @@ static void* rows_worker(void* p) {
     int64_t base = jb->R ? jb->R[i - jb->row0] : 0;
     for (int j = 0; j < jb->N; ++j) {
       if (j == i) continue;
-      const float r = orc_pair_r(jb->z, jb->T, i < j ? i : j, i < j ? j : i);
+      const int lo = i < j ? i : j, hi = i < j ? j : i;
+      const float r = jb->mode == R_EPS ? orc_pair_r_raw(jb->z, jb->T, lo, hi)
+                                        : orc_pair_r(jb->z, jb->T, lo, hi);
       if (!is_edge(r, jb->mode, jb->tau)) continue;
       if (jb->C) jb->C[base + c] = j;
       if (jb->V) jb->V[base + c] = r;

@@ -31,3 +31,22 @@ def sparse_graphs():
 
 
 SPARSE_CASES = ["cliques_isolated", "star_path", "sparse500"]
+
+
+def random_graph(n, deg, seed):
+    """Symmetric random graph, columns ascending per row, values in (0, 1)."""
+    rng = np.random.default_rng(seed)
+    i = rng.integers(0, n, n * deg // 2)
+    j = rng.integers(0, n, n * deg // 2)
+    keep = i != j
+    i, j = i[keep], j[keep]
+    w = rng.uniform(0.05, 1.0, len(i)).astype(np.float32)
+    rows = np.concatenate([i, j])
+    cols = np.concatenate([j, i])
+    vals = np.concatenate([w, w])
+    key = rows.astype(np.int64) * n + cols
+    key, first = np.unique(key, return_index=True)
+    rows, cols, vals = (key // n).astype(np.int32), (key % n).astype(np.int32), vals[first]
+    R = np.zeros(n + 1, np.int32)
+    np.add.at(R, rows + 1, 1)
+    return np.cumsum(R).astype(np.int32), cols, vals

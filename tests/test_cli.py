@@ -1,5 +1,6 @@
 """Command-line drop-ins: bna_cormat (CUCorMat's arguments and outputs,
-W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:52-670) and bna_cuec (CUEC,
+W/CorMat/CUCorMat/CUCorMat/CorMat.cpp:52-670), bna_cormat_u (the unweighted
+tree's CUCorMat, U/CorMat/CUCorMat/CUCORMAT/CorMat.cpp) and bna_cuec (CUEC,
 W/CUEC/weighted-net.cu:222-331), run on NIfTI files written here; outputs
 checked against the oracle."""
 import glob
@@ -90,6 +91,39 @@ def test_cormat_density_mode(tmp_path):
     assert re.search(rf"_cor{np.float32(tau):.3f}_weighted", f[0])
     rp, ci, va = bna.csr_read(f[0])
     assert len(ci) == 2 * k
+
+
+def test_unweighted_tree_cormat(tmp_path):
+    """bna_cormat_u (U/CorMat/CUCorMat/CUCORMAT/CorMat.cpp): the same
+    arguments, per-subject files in Dir/unweighted without the _weighted
+    suffix, binary .csr (no value section); r and density thresholds; the
+    binary files feed bna_cuec like the reference's unweighted CUEC."""
+    N, bolds = _subjects(tmp_path)
+    M1 = N * (N - 1) // 2
+    _run("bna_cormat_u", tmp_path, tmp_path / "mask.nii", 0.5, "n", "n", "r", 0.3, 0.45)
+    for k, b in enumerate(bolds, 1):
+        for tau in (0.3, 0.45):
+            R, C, _ = oracle.csr_corr(b, "r_gt", tau)
+            spa = 100.0 * len(C) / M1 / 2
+            f = tmp_path / "unweighted" / f"s{k}_{N}_spa{spa:.3f}%_cor{tau:.3f}.csr"
+            assert f.exists(), sorted(os.listdir(tmp_path / "unweighted"))
+            rp, ci, va = bna.csr_read(str(f))
+            assert va is None
+            assert np.array_equal(rp, R) and np.array_equal(ci, C)
+            # file layout: int Rlength, R, int Clength, C and nothing more
+            assert os.path.getsize(f) == 4 * (1 + len(R) + 1 + len(C))
+    assert not (tmp_path / "weighted").exists()
+    out = _run("bna_cormat_u", tmp_path, tmp_path / "mask.nii", 0.5, "n", "n", "s", 2.5)
+    tau, k, drop = oracle.density(oracle.cormat_packed(oracle.zscore(bolds[0])), N, 2.5)
+    f = glob.glob(str(tmp_path / "unweighted" / f"s1_{N}_spa2.500%_cor*.csr"))
+    assert len(f) == 1, out
+    rp, ci, va = bna.csr_read(f[0])
+    assert va is None and len(ci) == 2 * k
+    _run("bna_cuec", tmp_path / "unweighted")
+    rp, ci, _ = bna.csr_read(f[0])
+    e, lam, it, conv = oracle.ec(rp, ci)
+    ec = np.fromfile(f[0][:-4] + "_ec.nm", np.float32, offset=4)
+    assert np.max(np.abs(ec - e)) <= 1e-5 * np.max(np.abs(e)) + 1e-6
 
 
 def test_degree_tool_and_api(tmp_path, builder):

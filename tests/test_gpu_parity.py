@@ -11,7 +11,7 @@ import pytest
 
 import cuda_newest20160331_gb300 as bna
 import oracle
-from sparse_graphs import SPARSE_CASES, sparse_graphs
+from sparse_graphs import SPARSE_CASES, random_graph as _random_graph, sparse_graphs
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -239,6 +239,44 @@ def test_density_sampled_window_miss_falls_back(builder):
         assert np.array_equal(res.col_idx, ref.col_idx)
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_2mm_rule_matches_oracle(builder, precision):
+    """BNA_THR_R_EPS, the 2mm / chunk GPU tools' rule (CorMat-2mm.cu:140,156,
+    step2-dense2csr.cu:52): tau - 1e-6 < r <= 1 + 1e-6 in double on the raw
+    value.  Thresholds at an actual r + 5e-7 (an edge here, not under r > tau),
+    negative (a zero-variance voxel is never an edge, unlike post_block's 0),
+    duplicated voxels (r = 1)."""
+    N, T = 1100, 240
+    b = bna.synth_bold(N, T, 20, 808)
+    for k in range(6):
+        b[:, 500 + k] = b[:, 3 * k] * np.float32(2.0) + np.float32(k)
+    b[:, 33] = 1.5
+    z = oracle.zscore(b)
+    P = oracle.cormat_packed(z, raw=True)
+    r0 = float(np.sort(P[np.isfinite(P)])[-4000])
+    for tau in (np.float32(r0 + 5e-7), np.float32(0.4), np.float32(-0.2)):
+        R, C, V = oracle.threshold_csr(P, N, "r_eps", float(tau))
+        res = builder.corr_csr(dev(b), mode="r_eps", value=float(tau), precision=precision)
+        g = res.numpy()
+        assert np.array_equal(g.row_ptr, R) and np.array_equal(g.col_idx, C), tau
+        assert np.max(np.abs(g.val - V)) <= res.stats["delta"]
+    Rg, Cg, _ = oracle.threshold_csr(oracle.cormat_packed(z), N, "r_gt", float(np.float32(r0 + 5e-7)))
+    R2, C2, _ = oracle.threshold_csr(P, N, "r_eps", float(np.float32(r0 + 5e-7)))
+    assert len(C2) > len(Cg)  # the band below tau holds edges only under this rule
+
+
+def test_2mm_rule_in_a_batch_and_refused_by_average(builder):
+    shapes = [(1500, 100), (700, 300)]
+    bolds = [dev(bna.synth_bold(N, T, 12, 900 + k)) for k, (N, T) in enumerate(shapes)]
+    batch = builder.corr_csr_batch(bolds, mode="r_eps", value=0.35, precision="bf16x3")
+    for k, bd in enumerate(bolds):
+        R, C, V = oracle.csr_corr(bd.cpu().numpy(), "r_eps", 0.35)
+        g = batch[k].numpy()
+        assert np.array_equal(g.row_ptr, R) and np.array_equal(g.col_idx, C)
+    with pytest.raises(bna.BnaError):
+        builder.corr_csr_avg([bolds[0], bolds[0]], mode="r_eps", value=0.35)
+
+
 def test_host_buffer_path_equals_device_path(builder):
     b = bna.synth_bold(1000, 64, 10, 13)
     h = builder.corr_csr_host(b, mode="r_gt", value=0.45)
@@ -344,25 +382,6 @@ def test_ec_matches_oracle(builder):
         csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C), None, {})
         ec, lam, it, _ = builder.ec(csr)
         assert np.max(np.abs(ec.cpu().numpy() - ec_o)) <= 1e-5 * np.max(np.abs(ec_o))
-
-
-def _random_graph(n, deg, seed):
-    """Symmetric random graph, columns ascending per row, values in (0, 1)."""
-    rng = np.random.default_rng(seed)
-    i = rng.integers(0, n, n * deg // 2)
-    j = rng.integers(0, n, n * deg // 2)
-    keep = i != j
-    i, j = i[keep], j[keep]
-    w = rng.uniform(0.05, 1.0, len(i)).astype(np.float32)
-    rows = np.concatenate([i, j])
-    cols = np.concatenate([j, i])
-    vals = np.concatenate([w, w])
-    key = rows.astype(np.int64) * n + cols
-    key, first = np.unique(key, return_index=True)
-    rows, cols, vals = (key // n).astype(np.int32), (key % n).astype(np.int32), vals[first]
-    R = np.zeros(n + 1, np.int32)
-    np.add.at(R, rows + 1, 1)
-    return np.cumsum(R).astype(np.int32), cols, vals
 
 
 @pytest.mark.parametrize("unsorted", [False, True])

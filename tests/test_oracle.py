@@ -269,3 +269,30 @@ def test_modularity_oracle_against_compiled_reference_sparse(name):
 def test_modularity_without_edges_is_one_module():
     labels, q, m, _ = oracle.modularity(np.zeros(5, np.int32), np.zeros(0, np.int32))
     assert m == 1 and np.all(labels == 1) and np.isnan(q)
+
+
+def test_2mm_rule_restatement():
+    """The oracle's BNA_THR_R_EPS rule against the 2mm tools' comparison
+    written out directly (CorMat-2mm.cu:13,140,156: out > (r_thresh - ep) &&
+    out <= (1 + ep), ep = 1e-6 a double, the diagonal excluded) on the raw
+    values: NaN never passes, a zero-variance voxel never is an edge."""
+    N = 260
+    b = bna.synth_bold(N, 60, 8, 71)
+    b[:, 11] = 4.0
+    b[:, 40] = b[:, 2] * np.float32(3.0)
+    z = oracle.zscore(b)
+    P = oracle.cormat_packed(z, raw=True)
+    assert np.isnan(P).sum() == N - 1
+    for tau in (np.float32(0.25), np.float32(-0.3), np.float32(float(np.nanmax(P)))):
+        R, C, V = oracle.threshold_csr(P, N, "r_eps", float(tau))
+        want = []
+        for i in range(N):
+            for j in range(N):
+                if i == j:
+                    continue
+                a, c = min(i, j), max(i, j)
+                r = P[a * N - (1 + a) * a // 2 + c - (a + 1)]
+                if np.float64(r) > np.float64(tau) - 1e-6 and np.float64(r) <= 1.0 + 1e-6:
+                    want.append(j)
+        assert np.array_equal(C, want)
+
