@@ -380,6 +380,12 @@ def batch_run(n_subjects: int, precision: str = "auto", plain: bool = True) -> d
     # warm-up: the autotuner's choice, arenas grown
     res = b.corr_csr_batch(bolds, mode="density", value=1.0, precision=precision, copy=False)
     chosen = res[0].stats
+    names = {0: "fp32", 1: "bf16x3", 2: "tf32"}
+    shape = {"form": names.get(chosen["precision"]), "tile_band": chosen["tile_band"],
+             "tile": "128 x 256 (rows x columns), K block 64 BF16 x 3 products, 2 stages"
+             if chosen["precision"] == 1 else "128 x 256, K block 32 TF32, 4 stages",
+             "chosen_by": "bna_autotune_shape for the largest subject's size bucket"
+             if precision == "auto" else "fixed by the caller"}
     times = []
     for _ in range(2):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -396,7 +402,7 @@ def batch_run(n_subjects: int, precision: str = "auto", plain: bool = True) -> d
     exact = all(r.nnz == bna.density_nnz(N, 1.0) for r, (N, _, _, _) in zip(res, subs))
     out = {"subjects": n_subjects, "batch_ms": batch_ms,
            "subjects_per_s": n_subjects / (batch_ms / 1000.0), "edges_per_s": nnz / (batch_ms / 1000.0),
-           "exact_edge_counts": exact, "precision": precision,
+           "exact_edge_counts": exact, "precision": precision, "shape": shape,
            "flop_algorithmic": float(sum(N * (N - 1) / 2 * 2 * T for (N, T, _, _) in subs)),
            "sample": f"{n_subjects} subjects, N {min(s[0] for s in subs)}..{max(s[0] for s in subs)}, "
                      f"T {min(s[1] for s in subs)}..{max(s[1] for s in subs)}, density 1 %, weighted"}

@@ -135,9 +135,25 @@ class Builder:
         names = {v: k for k, v in L.PRECISIONS.items()}
         return names[best.value], {"bf16x3": ms[0], "tf32": ms[1]}
 
+    TUNE_BANDS = (16, 32, 64)
+
+    def autotune_shape(self, N: int, T: int, mode: str = "r_gt", value: float = 0.5,
+                       weighted: bool = True):
+        """bna_autotune_shape: -> ((precision name, band), {(form, band): ms})."""
+        o = _opts(mode, value, "auto", weighted, None)
+        best = C.c_int32()
+        band = C.c_int32()
+        ms = (C.c_float * 6)()
+        _check(lib().bna_autotune_shape(self._h, N, T, C.byref(o), C.byref(best),
+                                        C.byref(band), ms), self._h)
+        names = {v: k for k, v in L.PRECISIONS.items()}
+        times = {(f, b): ms[i * 3 + j] for i, f in enumerate(("bf16x3", "tf32"))
+                 for j, b in enumerate(self.TUNE_BANDS)}
+        return (names[best.value], band.value), times
+
     def set_option(self, name: str, value: int):
-        """bna_ctx_set_option: "tiles_per_launch", "max_nnz" or "ec_iters_per_launch"
-        (0 = default)."""
+        """bna_ctx_set_option: "tiles_per_launch", "max_nnz", "ec_iters_per_launch"
+        or "tile_band" (0 = default)."""
         _check(lib().bna_ctx_set_option(self._h, L.OPTIONS[name], int(value)), self._h)
 
     GATE = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64)

@@ -16,7 +16,7 @@ BNA_OK = 0
 BNA_NOT_CONVERGED = 4
 BNA_CAPACITY = 13
 BNA_OVER_BUDGET = 14
-OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1, "ec_iters_per_launch": 2}
+OPTIONS = {"tiles_per_launch": 0, "max_nnz": 1, "ec_iters_per_launch": 2, "tile_band": 3}
 THR_MODES = {"r_gt": 0, "r_ge": 1, "abs_gt": 2, "abs_ge": 3, "density": 4, "r_eps": 5}
 PRECISIONS = {"fp32": 0, "bf16x3": 1, "tf32": 2, "auto": 3}
 SYNTH_KINDS = {"iid": 0, "blocknet": 1}
@@ -45,7 +45,8 @@ class CorrStats(C.Structure):
                 ("ms_zscore", C.c_float), ("ms_count", C.c_float), ("ms_recompute", C.c_float),
                 ("ms_scan", C.c_float), ("ms_fill", C.c_float), ("ms_total", C.c_float),
                 ("passes", C.c_int32), ("kernel_launches", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("precision", C.c_int32), ("tile_band", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -122,6 +123,8 @@ SIGNATURES = {
     "bna_density_nnz": (C.c_int64, [C.c_int32, C.c_double]),
     "bna_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CorrOpts),
                                  C.POINTER(C.c_int32), C.c_void_p]),
+    "bna_autotune_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CorrOpts),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p]),
     "bna_corr_csr_batch": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.POINTER(CorrOpts), C.c_void_p, C.c_void_p,
                                        C.c_void_p]),

@@ -71,9 +71,9 @@ cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const fl
                            const double* vald, long long nnz_used, double* u, float2* uf,
                            double* parts, void* st, int grid, int it_end, int max_iter,
                            double eps, cudaStream_t stream);
-void tc_tile_list(int nb, std::vector<int2>& out);
+void tc_tile_list(int nb, int band, std::vector<int2>& out);
 long long tc_tile_count(int nb);
-cudaError_t launch_tile_lists(int nb, int2* tiles, long long n_smp, int s, int2* smp,
+cudaError_t launch_tile_lists(int nb, int band, int2* tiles, long long n_smp, int s, int2* smp,
                               cudaStream_t st);
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
@@ -162,6 +162,21 @@ constexpr int kGraphIters = 32;
 // Density rule: the histogram that locates the k-th value runs on about this
 // many tiles (every s-th tile) when the problem has at least 4x as many.
 constexpr int kSampleTiles = 2048;
+// Row blocks per band of the tensor-core tile list (BNA_OPT_TILE_BAND): 64
+// keeps a band's row operands (T = 1200: 64 x 0.6 MB) and the column pairs in
+// flight in L2 and reads every column pair from DRAM once per band (measured
+// on the 180k x 1200 network: count pass 76.6 ms with a row-major list,
+// 61.4 / 59.4 / 72.1 ms with bands of 32 / 64 / 128).
+constexpr int kDefaultBand = 64;
+// Autotuner shapes: operand forms x tile bands.
+struct TuneChoice {
+  int prec = BNA_PREC_BF16X3;
+  int band = 0;  // 0: the context's band
+};
+constexpr int kTuneForms[2] = {BNA_PREC_BF16X3, BNA_PREC_TF32};
+constexpr int kTuneBandCount = 3;
+constexpr int kTuneBands[kTuneBandCount] = {16, 32, 64};
+constexpr int kTuneShapes = 2 * kTuneBandCount;
 // Row-block chunks of the fill pass when the CSR goes to host buffers: chunk
 // c's rows are copied out while chunk c + 1 is filled.
 constexpr int kFillChunks = 8;
@@ -181,6 +196,9 @@ struct bna_ctx {
   long long elist_cap = 1LL << 23;  // edge-list pool entries (grows on demand)
   EcGraph ecg;
   int tiles_nb = -1;  // block count the uploaded tensor-core tile list was built for
+  int tiles_band = 0; // and its band height (row blocks listed column by column together)
+  int band = kDefaultBand;  // BNA_OPT_TILE_BAND
+  int band_now = kDefaultBand;  // the band of the current call (the autotuner's for AUTO)
   int ntiles = 0;
   int ntiles_smp = 0;  // sampled tile list (density histogram), same block count
   int tiles_per_launch = 0;  // BNA_OPT_TILES_PER_LAUNCH
@@ -203,9 +221,10 @@ struct bna_ctx {
   unsigned int* hist_host = nullptr;
   size_t hist_host_cap = 0;
   std::vector<int> batch_nb;
+  int batch_band = 0;
   int batch_ntiles = 0;
   // autotuner choices: bucket key -> precision
-  std::map<long long, int> tune;
+  std::map<long long, TuneChoice> tune;
   bool tune_loaded = false;
   cudaStream_t cur = nullptr;  // stream of the call in progress (arena growth is ordered on it)
   long long max_nnz = 0;     // BNA_OPT_MAX_NNZ
@@ -388,7 +407,7 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
   ENSURE(S_BLOCKBAD, (size_t)a.nb, bb);
   CK(launch_block_bad(a.bad, a.nb, bb, st));
   ctx->klaunch += 1;
-  if (ctx->tiles_nb != a.nb) {
+  if (ctx->tiles_nb != a.nb || ctx->tiles_band != ctx->band_now) {
     // built on the device in stream order: no host wait for the work ahead
     const long long nt = tc_tile_count(a.nb);
     // every s-th tile: the sample the density histogram may be taken on
@@ -397,9 +416,10 @@ int32_t tc_prepare(bna_ctx* ctx, const CorrArgs& a, cudaStream_t st) {
     int2 *d, *ds;
     ENSURE(S_TILES, (size_t)nt * sizeof(int2), d);
     ENSURE(S_TILES_SMP, (size_t)nsmp * sizeof(int2), ds);
-    CK(launch_tile_lists(a.nb, d, nsmp, s, ds, st));
+    CK(launch_tile_lists(a.nb, ctx->band_now, d, nsmp, s, ds, st));
     ctx->klaunch += 2;
     ctx->tiles_nb = a.nb;
+    ctx->tiles_band = ctx->band_now;
     ctx->ntiles = (int)nt;
     ctx->ntiles_smp = (int)nsmp;
   }
@@ -605,6 +625,11 @@ int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value) {
       if (value > 1000000) return fail(ctx, BNA_BAD_ARG, "iterations per launch too large");
       ctx->ec_seg = (int)value;
       return BNA_OK;
+    case BNA_OPT_TILE_BAND:
+      if (value > 4096) return fail(ctx, BNA_BAD_ARG, "band of %lld row blocks too large",
+                                    (long long)value);
+      ctx->band = value > 0 ? (int)value : kDefaultBand;
+      return BNA_OK;
     default: return fail(ctx, BNA_BAD_ARG, "unknown option %d", option);
   }
 }
@@ -711,6 +736,19 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
                              const bna_corr_opts* opts, int prec, double delta, bna_csr* out_dev,
                              bna_corr_stats* stats, cudaStream_t st);
 
+// Known threshold rules, and the float the kernels compare against: tau as
+// the reference's float, or for the 2mm tools' rule (r > tau - 1e-6 in
+// double) the smallest float above tau - 1e-6.
+static bool mode_known(int m) { return m >= BNA_THR_R_GT && m <= BNA_THR_R_EPS; }
+static float rule_tau(const bna_corr_opts* o) {
+  const float t = (float)o->value;
+  if (o->mode != BNA_THR_R_EPS) return t;
+  const double lo = (double)t - 1e-6;
+  float f = (float)lo;
+  if ((double)f <= lo) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
 // Autotuner bucket: half-octaves of N and T, and the rule kind.
 static long long tune_key(int N, int T, int mode) {
   const int nb = (int)std::floor(2.0 * std::log2((double)std::max(N, 2)));
@@ -718,6 +756,10 @@ static long long tune_key(int N, int T, int mode) {
   return ((long long)nb << 24) | ((long long)tb << 8) | (mode == BNA_THR_DENSITY ? 1 : 0);
 }
 
+static bool band_ok(int b) { return b >= 1 && b <= 4096; }
+
+// Cache lines: key precision band [N T times...]; a line without a valid band
+// keeps the default band.
 static void tune_load(bna_ctx* ctx) {
   if (ctx->tune_loaded) return;
   ctx->tune_loaded = true;
@@ -725,34 +767,44 @@ static void tune_load(bna_ctx* ctx) {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  long long key;
-  int prec;
-  while (std::fscanf(f, "%lld %d%*[^\n]", &key, &prec) == 2)
-    if (prec == BNA_PREC_BF16X3 || prec == BNA_PREC_TF32) ctx->tune[key] = prec;
+  char line[512];
+  while (std::fgets(line, sizeof line, f)) {
+    long long key;
+    int prec, band = 0;
+    const int n = std::sscanf(line, "%lld %d %d", &key, &prec, &band);
+    if (n < 2 || (prec != BNA_PREC_BF16X3 && prec != BNA_PREC_TF32)) continue;
+    ctx->tune[key] = TuneChoice{prec, n == 3 && band_ok(band) ? band : 0};
+  }
   std::fclose(f);
 }
 
+// The precision and tile band of a call: the caller's, or for BNA_PREC_AUTO
+// the autotuner's choice for the size bucket (tuned now if not known yet).
 static int32_t resolve_precision(bna_ctx* ctx, int N, int T, const bna_corr_opts* opts,
                                  int* prec) {
   *prec = opts->precision;
+  ctx->band_now = ctx->band;
   if (opts->precision != BNA_PREC_AUTO) return BNA_OK;
   tune_load(ctx);
   auto it = ctx->tune.find(tune_key(N, T, opts->mode));
-  if (it != ctx->tune.end()) {
-    *prec = it->second;
-    return BNA_OK;
+  if (it == ctx->tune.end()) {
+    int32_t best = BNA_PREC_BF16X3, band = 0;
+    const int32_t s = bna_autotune_shape(ctx, N, T, opts, &best, &band, nullptr);
+    if (s) return s;
+    it = ctx->tune.find(tune_key(N, T, opts->mode));
+    if (it == ctx->tune.end()) return fail(ctx, BNA_INTERNAL, "autotuner kept no choice");
   }
-  int32_t best = BNA_PREC_BF16X3;
-  const int32_t s = bna_autotune(ctx, N, T, opts, &best, nullptr);
-  if (s) return s;
-  *prec = best;
+  *prec = it->second.prec;
+  ctx->band_now = it->second.band > 0 ? it->second.band : ctx->band;
   return BNA_OK;
 }
 
-int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
-                     int32_t* precision_out, float* ms_out) {
-  if (!ctx || N < 2 || T < 2 || !opts || !precision_out)
+int32_t bna_autotune_shape(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
+                           int32_t* precision_out, int32_t* band_out, float* ms_out) {
+  if (!ctx || N < 2 || T < 2 || !opts || !precision_out || !band_out)
     return fail(ctx, BNA_BAD_ARG, "bna_autotune: bad arguments");
+  if (!mode_known(opts->mode))
+    return fail(ctx, BNA_BAD_ARG, "bna_autotune: unknown threshold mode %d", opts->mode);
   tune_load(ctx);
   int32_t s = set_device(ctx);
   if (s) return s;
@@ -774,49 +826,59 @@ int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* op
     cudaFree(bold);
     return fail(ctx, BNA_CUDA_ERROR, "bna_autotune: %s", cudaGetErrorString(ce));
   }
-  const int forms[2] = {BNA_PREC_BF16X3, BNA_PREC_TF32};
-  float best_ms[2] = {INFINITY, INFINITY};
-  for (int f = 0; f < 2 && s == BNA_OK; ++f) {
+  // the shapes: operand form (K depth per stage, ring stages, recompute band)
+  // x tile band (row blocks listed column by column)
+  float ms[kTuneShapes];
+  for (int k = 0; k < kTuneShapes; ++k) ms[k] = INFINITY;
+  const int saved_band = ctx->band;
+  for (int k = 0; k < kTuneShapes && s == BNA_OK; ++k) {
     bna_corr_opts o = *opts;
-    o.precision = forms[f];
+    o.precision = kTuneForms[k / kTuneBandCount];
+    ctx->band = kTuneBands[k % kTuneBandCount];
     for (int rep = 0; rep < 3 && s == BNA_OK; ++rep) {  // first run warms up
       bna_csr c{};
       bna_corr_stats st{};
       s = bna_corr_csr(ctx, bold, N, T, &o, &c, &st, nullptr);
-      if (s == BNA_OK && rep > 0) best_ms[f] = std::min(best_ms[f], st.ms_total);
+      if (s == BNA_OK && rep > 0) ms[k] = std::min(ms[k], st.ms_total);
     }
   }
+  ctx->band = saved_band;
   cudaFree(bold);
   if (s) return s;
-  const int32_t best = best_ms[1] < best_ms[0] ? BNA_PREC_TF32 : BNA_PREC_BF16X3;
+  int bk = 0;
+  for (int k = 1; k < kTuneShapes; ++k)
+    if (ms[k] < ms[bk]) bk = k;
+  const TuneChoice best{kTuneForms[bk / kTuneBandCount], kTuneBands[bk % kTuneBandCount]};
   const long long key = tune_key(N, T, opts->mode);
   ctx->tune[key] = best;
   const char* path = std::getenv("BNA_TUNE_CACHE");
   if (path && *path) {
     if (FILE* f = std::fopen(path, "a")) {
-      std::fprintf(f, "%lld %d %d %d %.4f %.4f\n", key, best, N, T, best_ms[0], best_ms[1]);
+      std::fprintf(f, "%lld %d %d %d %d", key, best.prec, best.band, N, T);
+      for (int k = 0; k < kTuneShapes; ++k) std::fprintf(f, " %.4f", ms[k]);
+      std::fprintf(f, "\n");
       std::fclose(f);
     }
   }
-  *precision_out = best;
-  if (ms_out) {
-    ms_out[0] = best_ms[0];
-    ms_out[1] = best_ms[1];
-  }
+  *precision_out = best.prec;
+  *band_out = best.band;
+  if (ms_out)
+    for (int k = 0; k < kTuneShapes; ++k) ms_out[k] = ms[k];
   return BNA_OK;
 }
 
-// Known threshold rules, and the float the kernels compare against: tau as
-// the reference's float, or for the 2mm tools' rule (r > tau - 1e-6 in
-// double) the smallest float above tau - 1e-6.
-static bool mode_known(int m) { return m >= BNA_THR_R_GT && m <= BNA_THR_R_EPS; }
-static float rule_tau(const bna_corr_opts* o) {
-  const float t = (float)o->value;
-  if (o->mode != BNA_THR_R_EPS) return t;
-  const double lo = (double)t - 1e-6;
-  float f = (float)lo;
-  if ((double)f <= lo) f = std::nextafter(f, INFINITY);
-  return f;
+int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
+                     int32_t* precision_out, float* ms_out) {
+  int32_t band = 0;
+  float ms[kTuneShapes];
+  const int32_t s = bna_autotune_shape(ctx, N, T, opts, precision_out, &band, ms);
+  if (s == BNA_OK && ms_out)
+    for (int f = 0; f < 2; ++f) {  // the best time of each form
+      ms_out[f] = INFINITY;
+      for (int b = 0; b < kTuneBandCount; ++b)
+        ms_out[f] = std::min(ms_out[f], ms[f * kTuneBandCount + b]);
+    }
+  return s;
 }
 
 int32_t bna_corr_csr(bna_ctx* ctx, const float* bold_dev, int32_t N, int32_t T,
@@ -1209,6 +1271,8 @@ static int32_t corr_csr_core(bna_ctx* ctx, CorrArgs& a, int32_t N, int32_t T,
     stats->ties_dropped = ties_dropped;
     stats->passes = passes + (density && k_dens > 0 ? 1 : 0);
     stats->kernel_launches = ctx->klaunch + fill_launches;
+    stats->precision = prec;
+    stats->tile_band = prec != BNA_PREC_FP32 ? ctx->band_now : 0;
     cudaEventElapsedTime(&stats->ms_zscore, ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&stats->ms_count, ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&stats->ms_recompute, ctx->ev[2], ctx->ev[3]);
@@ -1696,6 +1760,7 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
   auto single = [&](int k) -> int32_t {  // the one-subject path (retries, fallbacks)
     bna_ctx* kid = ctx->kids[k];
     kid->tiles_per_launch = ctx->tiles_per_launch;
+    kid->band = kid->band_now = ctx->band_now;
     const int32_t r = bna_corr_csr(kid, bold_dev[k], N[k], T[k], opts, &out_dev[k],
                                    stats ? &stats[k] : nullptr, stream);
     if (r) return fail(ctx, r, "subject %d: %s", k, kid->last_error.c_str());
@@ -1745,11 +1810,11 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
   }
   std::vector<int> nbs(nsub);
   for (int k = 0; k < nsub; ++k) nbs[k] = bs[k].a.nb;
-  if (nbs != ctx->batch_nb) {
+  if (nbs != ctx->batch_nb || ctx->batch_band != ctx->band_now) {
     std::vector<int4> t4;
     for (int k = 0; k < nsub; ++k) {
       std::vector<int2> t;
-      tc_tile_list(nbs[k], t);
+      tc_tile_list(nbs[k], ctx->band_now, t);
       for (const int2& x : t) t4.push_back(make_int4(x.x, x.y, k, 0));
     }
     int4* d;
@@ -1757,6 +1822,7 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
     CK(cudaMemcpyAsync(d, t4.data(), t4.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
     ctx->batch_nb = nbs;
+    ctx->batch_band = ctx->band_now;
     ctx->batch_ntiles = (int)t4.size();
   }
   void* table_dev;
@@ -1848,6 +1914,8 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
       o.band_edges = (int64_t)hs->stats[0];
       o.band_1e6 = (int64_t)hs->stats[1];
       o.passes = 1 + (density && b.k_dens > 0 ? 1 : 0);
+      o.precision = prec;
+      o.tile_band = ctx->band_now;
     }
   }
   // ---- fill (one synchronisation)

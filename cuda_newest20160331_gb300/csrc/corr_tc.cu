@@ -742,30 +742,55 @@ bool make_map(CUtensorMap* m, const void* base, int ld, int rows, bool fp32) {
 
 }  // namespace
 
-// Tile list (I, Jp) of the upper triangle in 128 x 256 tiles, row-major.
-void tc_tile_list(int nb, std::vector<int2>& out) {
-  out.clear();
-  const int njp = (nb + 1) / 2;
-  for (int I = 0; I < nb; ++I)
-    for (int jp = I / 2; jp < njp; ++jp) out.push_back(make_int2(I, jp));
-}
-
-// The same list built on the device (no host round trip): row block I holds
-// (I, jp) for jp = I/2 .. njp-1 and starts at I * njp - sum_{I' < I} floor(I'/2),
-// which is m(m-1) for I = 2m and m^2 for I = 2m+1.  One warp per row block.
+// Tile list (I, Jp) of the upper triangle in 128 x 256 tiles (rows of block
+// I, columns of blocks 2Jp and 2Jp+1, Jp >= I/2), in bands of `band` row
+// blocks: band b holds rows [b*band, (b+1)*band) and lists them column by
+// column (Jp ascending, then I ascending).  The CTAs of a persistent launch
+// take consecutive tiles, so at any time they work on a few column pairs of
+// one band: every column pair's operands are read from DRAM about once per
+// band and the band's row operands stay in L2 (a row-major list sweeps all
+// columns at once and re-reads them from DRAM for every row block).
 __host__ __device__ inline long long tile_row_offset(int I, int njp) {
+  // tiles in rows [0, I): row I' holds njp - floor(I'/2) tiles
   const long long m = I / 2;
   return (long long)I * njp - ((I & 1) ? m * m : m * (m - 1));
 }
 
 long long tc_tile_count(int nb) { return tile_row_offset(nb, (nb + 1) / 2); }
 
-__global__ void tile_list_kernel(int nb, int2* out) {
-  const int I = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (I >= nb) return;
-  const int njp = (nb + 1) / 2, m = I / 2;
-  const long long off = tile_row_offset(I, njp);
-  for (int jp = m + lane; jp < njp; jp += 32) out[off + jp - m] = make_int2(I, jp);
+// Position of column pair jp's first tile inside band [i0, i1).
+__host__ __device__ inline long long band_col_offset(int i0, int i1, int jp) {
+  long long off = 0;
+  for (int I = i0; I < i1; ++I) off += jp > I / 2 ? jp - I / 2 : 0;
+  return off;
+}
+
+void tc_tile_list(int nb, int band, std::vector<int2>& out) {
+  out.clear();
+  const int njp = (nb + 1) / 2;
+  if (band < 1) band = 1;
+  for (int i0 = 0; i0 < nb; i0 += band) {
+    const int i1 = i0 + band < nb ? i0 + band : nb;
+    for (int jp = i0 / 2; jp < njp; ++jp)
+      for (int I = i0; I < i1 && I / 2 <= jp; ++I) out.push_back(make_int2(I, jp));
+  }
+}
+
+// The same list built on the device (no host round trip): one thread per
+// (band, column pair) writes that column's tiles of the band.
+__global__ void tile_list_kernel(int nb, int band, long long total, int2* out) {
+  const int njp = (nb + 1) / 2;
+  const int nbands = (nb + band - 1) / band;
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (long long)nbands * njp) return;
+  const int b = (int)(k / njp), jp = (int)(k % njp);
+  const int i0 = b * band, i1 = i0 + band < nb ? i0 + band : nb;
+  if (jp < i0 / 2) return;
+  const long long base = tile_row_offset(i0, njp) + band_col_offset(i0, i1, jp);
+  for (int I = i0; I < i1 && I / 2 <= jp; ++I) {
+    const long long pos = base + (I - i0);
+    if (pos < total) out[pos] = make_int2(I, jp);
+  }
 }
 
 // Every s-th tile of the list (the density histogram's sample).
@@ -774,10 +799,13 @@ __global__ void tile_sample_kernel(const int2* tiles, long long n_smp, int s, in
   if (k < n_smp) out[k] = tiles[k * s];
 }
 
-cudaError_t launch_tile_lists(int nb, int2* tiles, long long n_smp, int s, int2* smp,
+cudaError_t launch_tile_lists(int nb, int band, int2* tiles, long long n_smp, int s, int2* smp,
                               cudaStream_t st) {
   if (nb <= 0) return cudaSuccess;
-  tile_list_kernel<<<(nb + 7) / 8, 256, 0, st>>>(nb, tiles);
+  if (band < 1) band = 1;
+  const long long work = (long long)((nb + band - 1) / band) * ((nb + 1) / 2);
+  tile_list_kernel<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(nb, band, tc_tile_count(nb),
+                                                                   tiles);
   if (n_smp > 0)
     tile_sample_kernel<<<(unsigned)((n_smp + 255) / 256), 256, 0, st>>>(tiles, n_smp, s, smp);
   return cudaGetLastError();

@@ -9,6 +9,8 @@ not distributed).  Sizes follow the reference's typical runs (N up to
   n45k_density  the same subject through the exact density rule (1 %)
   n180k      N=180,000 T=1200 K=60  block-network loadings (500-voxel blocks),
              tau = 0.4, weighted CSR, then centrality
+  n40k_t1200 the same generator and rule at N=40,000 (a case small enough for
+             detailed profiler captures)
   batch64    64 subjects, N uniform in [20,000, 70,000], T uniform in [150, 1200],
              seeds 1000 + s, 1 % density each, weighted CSRs, in one batch
   serving    Poisson arrivals at 4 requests/s; each request a subject with N
@@ -68,6 +70,9 @@ def get(name: str) -> Workload:
         return Workload("n45k_density", 45000, 240, 40, 2, "density", 1.0, True)
     if name == "n180k":
         return Workload("n180k", 180000, 1200, 60, 3, "r_ge", 0.4, True, kind="blocknet",
+                        synth={"load_sd": 0.117, "jitter_sd": 0.08, "block": 500, "n_net": 60})
+    if name == "n40k_t1200":  # the 180k network's generator at 40,000 voxels (profiling size)
+        return Workload("n40k_t1200", 40000, 1200, 60, 3, "r_ge", 0.4, True, kind="blocknet",
                         synth={"load_sd": 0.117, "jitter_sd": 0.08, "block": 500, "n_net": 60})
     raise KeyError(name)
 

@@ -112,7 +112,9 @@ typedef struct bna_corr_stats {
   float ms_zscore, ms_count, ms_recompute, ms_scan, ms_fill, ms_total; /* device time per stage */
   int32_t passes;          /* GEMM passes run */
   int32_t kernel_launches; /* kernels this call launched */
-  int32_t reserved[6];
+  int32_t precision;       /* the form that ran (BNA_PREC_AUTO resolved) */
+  int32_t tile_band;       /* tensor-core forms: row blocks per band of the tile order */
+  int32_t reserved[4];
 } bna_corr_stats;
 
 typedef struct bna_ctx bna_ctx;
@@ -143,11 +145,16 @@ int64_t bna_ctx_arena_bytes(const bna_ctx* ctx);
  *   BNA_OPT_EC_ITERS_PER_LAUNCH: power iterations per centrality launch or
  *     graph replay, rounded up to even for replays (0 = automatic: the whole
  *     iteration for small graphs and 32 per replay for larger ones; with a
- *     launch gate, about a millisecond of iterations). */
+ *     launch gate, about a millisecond of iterations);
+ *   BNA_OPT_TILE_BAND: row blocks (of 128 voxels) per band of the tensor-core
+ *     tile order (0 = the default, 32): a persistent launch takes the tiles of
+ *     a band column by column, so each column block is read from HBM once per
+ *     band; the result does not depend on it. */
 typedef enum bna_option {
   BNA_OPT_TILES_PER_LAUNCH = 0,
   BNA_OPT_MAX_NNZ = 1,
-  BNA_OPT_EC_ITERS_PER_LAUNCH = 2
+  BNA_OPT_EC_ITERS_PER_LAUNCH = 2,
+  BNA_OPT_TILE_BAND = 3
 } bna_option;
 int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value);
 
@@ -165,16 +172,24 @@ typedef enum bna_phase { BNA_PHASE_CORR = 0, BNA_PHASE_FILL = 1, BNA_PHASE_EC = 
 typedef void (*bna_gate_fn)(void* user, void* stream, int32_t phase, int64_t done);
 int32_t bna_ctx_set_gate(bna_ctx* ctx, bna_gate_fn gate, void* user);
 
-/* Autotuner (no reference counterpart).  The two tensor-core forms differ in
- * their tile shape along K (64 BF16 values x 3 products vs 32 TF32 values x 1
- * per 128-byte stage row, 2 vs 4 pipeline stages) and in the width of the
- * exact-recompute band; which one builds a CSR faster depends on N, T and the
- * rule.  bna_autotune times both on a seeded synthetic subject of size N x T
- * under `opts` (rule and value), remembers the faster one for the size bucket
- * (half-octaves of N and T) and rule kind, and returns it; BNA_PREC_AUTO
- * calls resolve through these choices.  With the environment variable
- * BNA_TUNE_CACHE set, choices are read from and appended to that file.
- * ms_out (optional, 2 floats): the times of split-BF16 and TF32. */
+/* Autotuner (no reference counterpart).  The shapes it searches: the two
+ * tensor-core forms differ in their tile shape along K (64 BF16 values x 3
+ * products vs 32 TF32 values x 1 per 128-byte stage row of a 128 x 256 tile,
+ * 2 vs 4 pipeline stages) and in the width of the exact-recompute band; the
+ * tile band (BNA_OPT_TILE_BAND: 16, 32 or 64 row blocks listed column by
+ * column) sets how much of the operands a persistent launch re-reads from
+ * HBM.  Which shape builds a CSR fastest depends on N, T and the rule.
+ * bna_autotune_shape times the six on a seeded synthetic subject of size
+ * N x T under `opts` (rule and value), remembers the fastest for the size
+ * bucket (half-octaves of N and T) and rule kind, and returns its form and
+ * band; BNA_PREC_AUTO calls resolve through these choices (form and band).
+ * With the environment variable BNA_TUNE_CACHE set, choices are read from and
+ * appended to that file, one line per bucket: key form band N T and the six
+ * times (form-major: split-BF16 at bands 16, 32, 64, then TF32).  ms_out
+ * (optional, 6 floats): those times.  bna_autotune is the same search with
+ * ms_out holding the best time of each form (2 floats). */
+int32_t bna_autotune_shape(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
+                           int32_t* precision_out, int32_t* band_out, float* ms_out);
 int32_t bna_autotune(bna_ctx* ctx, int32_t N, int32_t T, const bna_corr_opts* opts,
                      int32_t* precision_out, float* ms_out);
 

@@ -277,6 +277,31 @@ def test_2mm_rule_in_a_batch_and_refused_by_average(builder):
         builder.corr_csr_avg([bolds[0], bolds[0]], mode="r_eps", value=0.35)
 
 
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32"])
+def test_tile_band_does_not_change_the_csr(precision):
+    """The tensor-core tile order (bands of row blocks listed column by
+    column, BNA_OPT_TILE_BAND) changes only which CTA computes which tile:
+    the CSR is the same bit for bit, single builds and batches."""
+    import torch
+    b = dev(bna.synth_bold(5000, 200, 16, 611))
+    small = dev(bna.synth_bold(1300, 90, 8, 612))
+    ref = None
+    with bna.Builder(0) as bl:
+        for band in (1, 5, 32, 4096, 0):
+            bl.set_option("tile_band", band)
+            got = bl.corr_csr(b, mode="r_ge", value=0.3, precision=precision).numpy()
+            bat = bl.corr_csr_batch([small, b], mode="density", value=1.5, precision=precision)
+            bat = [x.numpy() for x in bat]
+            if ref is None:
+                ref = (got, bat)
+                continue
+            assert np.array_equal(got.row_ptr, ref[0].row_ptr)
+            assert np.array_equal(got.col_idx, ref[0].col_idx)
+            assert np.array_equal(got.val, ref[0].val), band
+            for x, y in zip(bat, ref[1]):
+                assert np.array_equal(x.col_idx, y.col_idx) and np.array_equal(x.val, y.val)
+
+
 def test_host_buffer_path_equals_device_path(builder):
     b = bna.synth_bold(1000, 64, 10, 13)
     h = builder.corr_csr_host(b, mode="r_gt", value=0.45)
@@ -577,6 +602,30 @@ def test_autotune_picks_a_form_and_auto_resolves(builder, tmp_path, monkeypatch)
         assert len([x for x in lines if x.strip()]) == 1
     finally:
         t2.close()
+
+
+def test_autotune_shapes_listed_and_all_give_the_same_csr(tmp_path, monkeypatch):
+    """bna_autotune_shape times every (form, band) shape, the cache line lists
+    the chosen form and band with the six times, and every shape builds the
+    same CSR (row_ptr / col_idx bit-exact; values within the forms' bands)."""
+    monkeypatch.setenv("BNA_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    b = dev(bna.synth_bold(4000, 300, 12, 78))
+    with bna.Builder(0) as t:
+        (prec, band), times = t.autotune_shape(4000, 300, mode="r_ge", value=0.35)
+        assert prec in ("bf16x3", "tf32") and band in bna.Builder.TUNE_BANDS
+        assert len(times) == 6 and all(v > 0 for v in times.values())
+        assert times[(prec, band)] == min(times.values())
+        f = (tmp_path / "tune.txt").read_text().split()
+        assert int(f[1]) == bna._lib.PRECISIONS[prec] and int(f[2]) == band and len(f) == 11
+        ref = t.corr_csr(b, mode="r_ge", value=0.35, precision="fp32").numpy()
+        for form, bd in times:
+            t.set_option("tile_band", bd)
+            g = t.corr_csr(b, mode="r_ge", value=0.35, precision=form).numpy()
+            assert np.array_equal(g.row_ptr, ref.row_ptr) and np.array_equal(g.col_idx, ref.col_idx)
+            assert np.max(np.abs(g.val - ref.val)) <= g.stats["delta"] + ref.stats["delta"]
+        t.set_option("tile_band", 0)
+        auto = t.corr_csr(b, mode="r_ge", value=0.35, precision="auto").numpy()
+        assert np.array_equal(auto.col_idx, ref.col_idx)
 
 
 MOD_CASES = ["planted60", "planted300", "planted1000", "noisy500", "cliques", "small_c1"]
