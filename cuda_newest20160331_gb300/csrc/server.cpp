@@ -30,7 +30,10 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <deque>
 #include <map>
 #include <mutex>
@@ -68,9 +71,11 @@ struct Slot {
   int level = 0;                  // priority level of the running request
   double work = 0;                // its N^2 T (launch gate order)
   int64_t seq = 0;                // its start order (ties of work)
+  int64_t job_id = 0;             // the running request (trace)
   int phase = 0;                  // its pass and progress at its last gate call
   int64_t progress = 0;
   cudaEvent_t fence[2] = {};      // launch gate: queue-depth events
+  cudaEvent_t tev[2] = {};        // trace: around the series upload
   int nfence = 0;
   bna_ctx* ctx = nullptr;
   cudaStream_t stream[kLevels] = {};  // stream[0]: highest priority
@@ -106,6 +111,20 @@ constexpr int64_t kLongEc = 1000;
 }  // namespace
 
 struct bna_server {
+  // optional host-side trace (environment variable BNA_SERVER_TRACE = a file
+  // path, written when the server is destroyed): one line per event with the
+  // time, slot, request id, event name and a value
+  struct TraceEv {
+    double t;
+    int slot;
+    int64_t id;
+    const char* what;
+    int64_t v;
+  };
+  bool tracing = false;
+  std::string trace_path;
+  std::mutex trace_mu;
+  std::vector<TraceEv> trace;
   int device = 0;
   int sms = 1;
   int64_t budget = 0;
@@ -132,6 +151,13 @@ struct bna_server {
 };
 
 namespace {
+
+void trace(bna_server* srv, const Slot* s, int64_t id, const char* what, int64_t v = 0) {
+  if (!srv->tracing) return;
+  const double t = srv->now();
+  std::lock_guard<std::mutex> lk(srv->trace_mu);
+  srv->trace.push_back({t, s ? s->index : -1, id, what, v});
+}
 
 // Grow-only slot buffer, stream-ordered (no wait for other slots' work), from
 // the library's pool.
@@ -179,7 +205,10 @@ void slot_gate(void* user, void* stream, int32_t phase, int64_t done) {
   if (s->level > 0) {
     // queue depth: the launch before the previous one has finished
     cudaEventRecord(s->fence[s->nfence & 1], st);
+    const double t0 = srv->tracing ? srv->now() : 0.0;
     if (s->nfence > 0) cudaEventSynchronize(s->fence[(s->nfence + 1) & 1]);
+    if (srv->tracing && srv->now() - t0 > 5e-4)
+      trace(srv, s, s->job_id, "fence_wait_us", (int64_t)((srv->now() - t0) * 1e6));
     ++s->nfence;
   }
   lk.lock();
@@ -197,10 +226,15 @@ void slot_gate(void* user, void* stream, int32_t phase, int64_t done) {
   };
   if (!higher()) return;
   lk.unlock();
+  const double t0 = srv->now();
   cudaStreamSynchronize(st);  // nothing of this request stays queued
   lk.lock();
   const auto until = Clock::now() + std::chrono::milliseconds(kGateWaitMs);
   while (higher() && srv->cv.wait_until(lk, until) != std::cv_status::timeout) {
+  }
+  if (srv->tracing) {
+    lk.unlock();
+    trace(srv, s, s->job_id, "gate_wait_us", (int64_t)((srv->now() - t0) * 1e6));
   }
 }
 
@@ -210,21 +244,31 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
   bna_reply& out = j->reply;
   cudaStream_t st = s->stream[level_of(j->work, srv->levels)];
   const size_t bytes = (size_t)r.N * r.T * sizeof(float);
+  const size_t cap0 = s->bold_cap;
   int32_t rc = grow(srv->device, reinterpret_cast<void**>(&s->bold), &s->bold_cap, bytes, st);
+  trace(srv, s, j->id, "bold_grown_bytes", (int64_t)(s->bold_cap - cap0));
+  if (srv->tracing) cudaEventRecord(s->tev[0], st);
   // the series by an SM-driven copy from the caller's page-locked buffer
   // (copy-engine uploads slowed to a few GB/s while other requests shared
   // the device); a pageable buffer takes the copy engine
+  const double tu0 = srv->tracing ? srv->now() : 0.0;
   if (rc == BNA_OK && bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st) != cudaSuccess &&
       cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = BNA_CUDA_ERROR;
+  if (srv->tracing) {
+    trace(srv, s, j->id, "upload_call_us", (int64_t)((srv->now() - tu0) * 1e6));
+    cudaEventRecord(s->tev[1], st);
+  }
   bna_csr csr{};
   if (rc == BNA_OK) {
     // no CSR larger than the caller's buffers is built (a cap of 0 admits
     // only the empty graph)
     bna_ctx_set_option(s->ctx, BNA_OPT_MAX_NNZ, r.cap > 0 ? r.cap : 1);
     bna_ctx_set_option(s->ctx, BNA_OPT_TILES_PER_LAUNCH, tiles_per_launch(r.T));
+    const int64_t arena0 = bna_ctx_arena_bytes(s->ctx);
     rc = bna_corr_csr(s->ctx, s->bold, r.N, r.T, &r.opts, &csr, &out.stats, st);
     out.t_corr = srv->now();
+    trace(srv, s, j->id, "corr_arena_grown_bytes", bna_ctx_arena_bytes(s->ctx) - arena0);
     out.nnz = rc == BNA_OK || rc == BNA_CAPACITY ? out.stats.nnz : 0;
     if (rc == BNA_OK && csr.nnz > r.cap) rc = BNA_CAPACITY;
   }
@@ -259,7 +303,15 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
       }
     }
   }
+  trace(srv, s, j->id, "ec_issued", out.ec_iters);
   if (cudaStreamSynchronize(st) != cudaSuccess && rc == BNA_OK) rc = BNA_CUDA_ERROR;
+  if (srv->tracing) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, s->tev[0], s->tev[1]) == cudaSuccess)
+      trace(srv, s, j->id, "upload_device_us", (int64_t)(ms * 1000));
+    cudaGetLastError();
+  }
+  trace(srv, s, j->id, "done");
   out.status = rc;
 }
 
@@ -288,7 +340,9 @@ void worker(bna_server* srv, Slot* s) {
     if (s->trim) {
       s->trim = false;
       lk.unlock();
+      trace(srv, s, 0, "trim_bytes", slot_bytes(s));
       release_slot_memory(s);
+      trace(srv, s, 0, "trimmed");
       lk.lock();
       s->held = 0;
       srv->cv.notify_all();
@@ -312,6 +366,7 @@ void worker(bna_server* srv, Slot* s) {
     s->level = level_of(j->work, srv->levels);
     s->work = j->work;
     s->seq = srv->next_seq++;
+    s->job_id = j->id;
     s->phase = BNA_PHASE_CORR;
     s->progress = 0;
     s->nfence = 0;
@@ -319,6 +374,7 @@ void worker(bna_server* srv, Slot* s) {
     j->reply.t_start = srv->now();
     j->reply.slot = s->index;
     lk.unlock();
+    trace(srv, s, j->id, "start", (int64_t)j->work);
     run_job(srv, s, j);
     lk.lock();
     j->reply.t_done = srv->now();
@@ -353,6 +409,12 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
     srv->sms = 1;
   srv->budget = hbm_budget_bytes;
   srv->t0 = Clock::now();
+  if (const char* tp = std::getenv("BNA_SERVER_TRACE")) {
+    if (*tp) {
+      srv->tracing = true;
+      srv->trace_path = tp;
+    }
+  }
   // numerically lower = higher priority; greatest <= least
   srv->levels = std::min(kLevels, least - greatest + 1);
   int32_t rc = BNA_OK;
@@ -365,6 +427,8 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
     for (auto& e : s->fence)
       if (rc == BNA_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
         rc = BNA_CUDA_ERROR;
+    for (auto& e : s->tev)
+      if (rc == BNA_OK && cudaEventCreate(&e) != cudaSuccess) rc = BNA_CUDA_ERROR;
     if (rc == BNA_OK) rc = bna_ctx_set_gate(s->ctx, slot_gate, s);
     for (int l = 0; l < srv->levels && rc == BNA_OK; ++l)
       if (cudaStreamCreateWithPriority(&s->stream[l], cudaStreamNonBlocking, greatest + l) !=
@@ -377,6 +441,8 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
       for (cudaStream_t& q : s->stream)
         if (q) cudaStreamDestroy(q);
       for (cudaEvent_t e : s->fence)
+        if (e) cudaEventDestroy(e);
+      for (cudaEvent_t e : s->tev)
         if (e) cudaEventDestroy(e);
       if (s->ctx) bna_ctx_destroy(s->ctx);
       delete s;
@@ -412,6 +478,7 @@ int32_t bna_server_submit(bna_server* srv, const bna_request* req, int64_t* tick
   srv->jobs[j->id] = j;
   srv->queue.push_back(j);
   *ticket = j->id;
+  trace(srv, nullptr, j->id, "submit_N_T", (int64_t)req->N * 100000 + req->T);
   srv->cv.notify_all();
   return BNA_OK;
 }
@@ -459,10 +526,21 @@ int32_t bna_server_destroy(bna_server* srv) {
       if (q) cudaStreamDestroy(q);
     for (cudaEvent_t e : s->fence)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->tev)
+      if (e) cudaEventDestroy(e);
     bna_ctx_destroy(s->ctx);
     delete s;
   }
   for (auto& kv : srv->jobs) delete kv.second;
+  if (srv->tracing) {
+    if (FILE* f = std::fopen(srv->trace_path.c_str(), "w")) {
+      std::fprintf(f, "t,slot,id,event,value\n");
+      for (const auto& e : srv->trace)
+        std::fprintf(f, "%.6f,%d,%lld,%s,%lld\n", e.t, e.slot, (long long)e.id, e.what,
+                     (long long)e.v);
+      std::fclose(f);
+    }
+  }
   delete srv;
   return BNA_OK;
 }
