@@ -58,6 +58,7 @@ def parse():
                    help="Newman modularity of the step's CSR (auto: N <= 100,000)")
     p.add_argument("--serve-requests", type=int, default=120)
     p.add_argument("--serve-slots", type=int, default=4)
+    p.add_argument("--serve-budget-gb", type=float, default=160.0)
     p.add_argument("--serve-dump", default="", help="write per-request records (JSON) here")
     return p.parse_args()
 
@@ -560,7 +561,8 @@ def main():
         return
     if args.workload == "serving":
         sv = serve_run(1000 if args.serve_requests == 120 else args.serve_requests,
-                       slots=args.serve_slots, dump=args.serve_dump)
+                       slots=args.serve_slots, dump=args.serve_dump,
+                       budget=int(args.serve_budget_gb * 2**30))
         if rank == 0:
             print(json.dumps({"metric": "serving latency p50/p99 (corr -> CSR -> centrality)",
                               "value": sv["p99_ms"], "unit": "ms", "higher_is_better": False,
@@ -571,7 +573,8 @@ def main():
     # would share the device with them)
     serve = None
     if rank == 0 and args.serve_requests > 0:
-        serve = serve_run(args.serve_requests, slots=args.serve_slots, dump=args.serve_dump)
+        serve = serve_run(args.serve_requests, slots=args.serve_slots, dump=args.serve_dump,
+                       budget=int(args.serve_budget_gb * 2**30))
     w = workloads.get(args.workload)
     precision = args.precision
     bold_h = w.bold()

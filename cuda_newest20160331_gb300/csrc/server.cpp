@@ -122,6 +122,7 @@ struct bna_server {
     int64_t v;
   };
   bool tracing = false;
+  bool upload_ce = false;  // BNA_SERVER_UPLOAD=copy_engine: uploads by cudaMemcpyAsync
   std::string trace_path;
   std::mutex trace_mu;
   std::vector<TraceEv> trace;
@@ -252,7 +253,8 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
   // (copy-engine uploads slowed to a few GB/s while other requests shared
   // the device); a pageable buffer takes the copy engine
   const double tu0 = srv->tracing ? srv->now() : 0.0;
-  if (rc == BNA_OK && bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st) != cudaSuccess &&
+  if (rc == BNA_OK && (srv->upload_ce ||
+                       bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st) != cudaSuccess) &&
       cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = BNA_CUDA_ERROR;
   if (srv->tracing) {
@@ -375,6 +377,11 @@ void worker(bna_server* srv, Slot* s) {
     j->reply.slot = s->index;
     lk.unlock();
     trace(srv, s, j->id, "start", (int64_t)j->work);
+    if (srv->tracing) {
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) trace(srv, s, j->id, "device_free_mb", (int64_t)(fr >> 20));
+      cudaGetLastError();
+    }
     run_job(srv, s, j);
     lk.lock();
     j->reply.t_done = srv->now();
@@ -409,6 +416,8 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
     srv->sms = 1;
   srv->budget = hbm_budget_bytes;
   srv->t0 = Clock::now();
+  if (const char* up = std::getenv("BNA_SERVER_UPLOAD"))
+    srv->upload_ce = std::strcmp(up, "copy_engine") == 0;
   if (const char* tp = std::getenv("BNA_SERVER_TRACE")) {
     if (*tp) {
       srv->tracing = true;
