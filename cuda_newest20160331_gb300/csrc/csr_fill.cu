@@ -30,6 +30,7 @@ namespace bna {
 
 constexpr int kFillWarps = 8;
 constexpr long long kFillDenseE = 1024;  // entries above which a sub-tile takes the dense path
+constexpr int kFillDenseLoads = 8;       // edge-list loads in flight per thread (dense path)
 
 __device__ __forceinline__ int popc_before4(const uint32_t* m, int pos) {
   const int w = pos >> 5;
@@ -215,18 +216,29 @@ __global__ __launch_bounds__(256) void csr_fill_dense_kernel(CorrArgs a, const i
     const bool diag = (I == J);
     // 1. bitmasks and values (ranges were checked by csr_dense_list_kernel)
     const long long p1 = S.cnt[0], p2 = p1 + S.cnt[1], p3 = p2 + S.cnt[2], E = p3 + S.cnt[3];
-    for (long long e = tid; e < E; e += 256) {
-      const int q = e < p1 ? 0 : e < p2 ? 1 : e < p3 ? 2 : 3;
-      const long long off = e - (q == 0 ? 0 : q == 1 ? p1 : q == 2 ? p2 : p3);
-      const uint2 en = a.elist[S.start[q] + off];
-      const int il = en.x & 127, jl = (en.x >> 7) & 127;
-      float v = __uint_as_float(en.y);
-      bool edge = true;
-      if ((en.x >> 14) & 1u) hash_lookup(a, pair_key(I * 128 + il, J * 128 + jl), v, edge);
-      if (edge) {
-        S.val[il][jl] = v;
-        atomicOr(&S.rm[il][jl >> 5], 1u << (jl & 31));
-        atomicOr(&S.cm[jl][il >> 5], 1u << (il & 31));
+    const long long s0 = S.start[0], s1 = S.start[1] - p1, s2 = S.start[2] - p2,
+                    s3 = S.start[3] - p3;  // entry e of quadrant q is elist[s_q + e]
+    // kFillDenseLoads independent loads per thread in flight before any is used
+    for (long long e0 = tid; e0 < E; e0 += 256 * kFillDenseLoads) {
+      uint2 en[kFillDenseLoads];
+#pragma unroll
+      for (int u = 0; u < kFillDenseLoads; ++u) {
+        const long long e = e0 + 256 * u;
+        en[u] = make_uint2(0u, 0u);
+        if (e < E) en[u] = a.elist[(e < p1 ? s0 : e < p2 ? s1 : e < p3 ? s2 : s3) + e];
+      }
+#pragma unroll
+      for (int u = 0; u < kFillDenseLoads; ++u) {
+        if (e0 + 256 * u >= E) break;
+        const int il = en[u].x & 127, jl = (en[u].x >> 7) & 127;
+        float v = __uint_as_float(en[u].y);
+        bool edge = true;
+        if ((en[u].x >> 14) & 1u) hash_lookup(a, pair_key(I * 128 + il, J * 128 + jl), v, edge);
+        if (edge) {
+          S.val[il][jl] = v;
+          atomicOr(&S.rm[il][jl >> 5], 1u << (jl & 31));
+          atomicOr(&S.cm[jl][il >> 5], 1u << (il & 31));
+        }
       }
     }
     __syncthreads();
