@@ -302,6 +302,43 @@ def test_tile_band_does_not_change_the_csr(precision):
                 assert np.array_equal(x.col_idx, y.col_idx) and np.array_equal(x.val, y.val)
 
 
+def _hard_series(N, T, seed):
+    """Factor-model series with voxels whose products span many decades:
+    spikes over a tiny background, values over 40 decades, large offsets,
+    a constant voxel and a duplicated one."""
+    b = bna.synth_bold(N, T, 12, seed)
+    rng = np.random.default_rng(seed)
+    for k in range(0, 40, 4):
+        x = (rng.standard_normal(T) * 1e-7).astype(np.float32)
+        x[rng.integers(T)] = 1.0
+        b[:, k] = x
+    for k in range(41, 60, 3):
+        b[:, k] = np.exp(np.linspace(-40.0, 10.0, T) + rng.standard_normal(T)).astype(np.float32)
+    for k in range(61, 80, 3):
+        b[:, k] = (1e6 + rng.standard_normal(T)).astype(np.float32)
+    b[:, 90] = 3.0
+    b[:, 91] = b[:, 92]
+    return b
+
+
+@pytest.mark.parametrize("T", [240, 1200])
+def test_every_pair_recomputed_is_bit_exact(builder, T):
+    """A recompute band wider than the range of r makes every pair a
+    candidate: every value of the CSR (r >= -2: all pairs) is then the
+    exact reference value (float products, double sum in time order,
+    CorMat.cpp:955-964, post_block), bit for bit, including pairs whose
+    products span many decades."""
+    N = 1100
+    b = _hard_series(N, T, 930 + T)
+    R, C, V = oracle.csr_corr(b, "r_ge", -2.0)
+    res = builder.corr_csr(dev(b), mode="r_ge", value=-2.0, precision="bf16x3", delta=3.0)
+    g = res.numpy()
+    assert res.stats["band_candidates"] >= N * (N - 1) // 2 - N
+    assert np.array_equal(g.row_ptr, R) and np.array_equal(g.col_idx, C)
+    bad = np.flatnonzero(g.val.view(np.uint32) != V.view(np.uint32))
+    assert len(bad) == 0, (len(bad), g.val[bad[:5]], V[bad[:5]])
+
+
 def test_host_buffer_path_equals_device_path(builder):
     b = bna.synth_bold(1000, 64, 10, 13)
     h = builder.corr_csr_host(b, mode="r_gt", value=0.45)
