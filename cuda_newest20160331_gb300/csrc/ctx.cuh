@@ -72,6 +72,16 @@ void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, dou
                    double* e2, int* iter, int* done);
 int ec_state_err(const void* host_copy);
 int ec_coop_grid(int n, int sms);
+int ec_chunk_count(int n);
+cudaError_t launch_ec_chunk_prep(int n, const int32_t* rp, const int32_t* ci, long long nnz_used,
+                                 unsigned long long* info, int* csplit, int grid, int* rowsplit,
+                                 cudaStream_t stream);
+cudaError_t prepare_ec_chunk();
+cudaError_t launch_ec_chunk(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                            const double* vald, long long nnz_used, const double* u,
+                            const float2* uf, double* un, float2* unf, double* parts, void* st,
+                            int grid, int max_iter, double eps, const int* rowsplit,
+                            const int* csplit, float2* part, cudaStream_t stream);
 cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const float* val,
                            const double* vald, long long nnz_used, double* u, float2* uf,
                            double* parts, void* st, int grid, int it_end, int max_iter,
@@ -140,7 +150,7 @@ enum Slot {
   S_BATCH_SUBJ, S_BATCH_TILES,
   S_MOD_LABEL, S_MOD_ROWS, S_MOD_LOC, S_MOD_CNT, S_MOD_LRP, S_MOD_LCI, S_MOD_VD, S_MOD_VF,
   S_MOD_RS, S_MOD_Y, S_MOD_PARTS, S_MOD_GROUPS, S_MOD_BLKGRP, S_MOD_ASSIGN, S_MOD_KMOD,
-  S_MOD_ADJ, S_COUNT
+  S_MOD_ADJ, S_EC_SPLIT, S_EC_PART, S_EC_ROWS, S_EC_FLAG, S_COUNT
 };
 
 // Small device block the host reads once per pass.
@@ -156,6 +166,7 @@ struct DevStatus {
 struct EcGraph {
   cudaGraphExec_t exec = nullptr;
   int iters = 0;  // iterations per replay
+  bool chunked = false;  // the column-chunked kernel
   const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int n = -1, grid = 0, max_iter = 0;
   long long nnz_used = -1;

@@ -342,6 +342,263 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
   }
 }
 
+// ---- column-chunked form -------------------------------------------------------
+//
+// For graphs whose iterate does not stay in L1 (random graphs of tens of
+// thousands of vertices), the (hi, lo) iterate gathers of ec_iter_kernel miss
+// L1 and pull a 32-byte L2 sector per 8-byte entry.  Here one 1024-thread block
+// per SM stages the iterate in shared memory a chunk of kEcChunkCols columns
+// at a time and gathers from there; each row's entries are split at the chunk
+// boundaries once per CSR (columns ascending within a row), and a row's
+// partial sum is carried from chunk to chunk in float-float.  Rows go to blocks
+// in contiguous ranges balanced by entries (plus a per-row weight); the FP64
+// epilogue, the block partials and the last-block reduction follow
+// ec_iter_kernel's, in a fixed order.
+constexpr int kEcChunkThreads = 1024;
+constexpr int kEcChunkCols = 24576;  // 192 KB of (hi, lo) pairs
+constexpr int kEcChunkRowsSmem = 3072;  // 24 KB of row sums beside them
+constexpr int kEcRowWeight = 32;     // entries a row costs in the block split
+
+// One warp, one row: eight entries per lane in flight per round of 256.
+template <int VK>
+__device__ __forceinline__ void ec_row_accum_smem(const int32_t* __restrict__ ci,
+                                                  const float* __restrict__ val,
+                                                  const double* __restrict__ vald,
+                                                  const float2* xs, int c0, long long b,
+                                                  long long e, int lane, float& sh, float& sl) {
+  for (long long k0 = b; k0 < e; k0 += 256) {
+    int c[8];
+    float vh[8], vl[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const long long k = k0 + lane + 32 * m;
+      const bool ok = k < e;
+      c[m] = ok ? __ldg(ci + k) - c0 : -1;
+      vh[m] = 1.0f;
+      vl[m] = 0.0f;
+      if (VK == 1) vh[m] = ok ? __ldg(val + k) : 0.0f;
+      if (VK == 2) {
+        const float2 d = split_df(ok ? __ldg(vald + k) : 0.0);
+        vh[m] = d.x;
+        vl[m] = d.y;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const float2 x = c[m] < 0 ? make_float2(0.0f, 0.0f) : xs[c[m]];
+      df_accum<VK>(sh, sl, vh[m], vl[m], x);
+    }
+  }
+}
+
+template <int VK>
+__global__ __launch_bounds__(kEcChunkThreads, 1) void ec_chunk_kernel(
+    int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+    const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
+    const double* __restrict__ u, const float2* __restrict__ uf, double* __restrict__ un,
+    float2* __restrict__ unf, double* parts, EcState* st, int max_iter, double eps,
+    const int* __restrict__ rowsplit, const int* __restrict__ csplit, int nch,
+    float2* __restrict__ part) {
+  extern __shared__ float2 xs[];
+  if (st->done || st->iter >= max_iter) return;
+  __shared__ double lam_s[2];
+  if (threadIdx.x == 0) {
+    const double l2 = st->lam2;
+    lam_s[1] = rsqrt(l2);
+    lam_s[0] = l2 == 0.0 ? 0.0 : l2 * lam_s[1];
+  }
+  constexpr int kW = kEcChunkThreads / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r0 = rowsplit[blockIdx.x], r1 = rowsplit[blockIdx.x + 1];
+  // the block's row sums between chunks: shared memory when they fit
+  float2* ps = xs + kEcChunkCols;
+  const bool in_smem = r1 - r0 <= kEcChunkRowsSmem;
+  for (int c = 0; c < nch; ++c) {
+    const int c0 = c * kEcChunkCols;
+    const int cn = min(kEcChunkCols, n - c0);
+    __syncthreads();  // the previous chunk's readers are done
+    // two pairs per 16-byte load (c0 is even: chunks are a multiple of 2 wide)
+    const float4* src4 = reinterpret_cast<const float4*>(uf + c0);
+    float4* dst4 = reinterpret_cast<float4*>(xs);
+    for (int k = threadIdx.x; k < cn / 2; k += kEcChunkThreads) dst4[k] = src4[k];
+    if ((cn & 1) && threadIdx.x == 0) xs[cn - 1] = uf[c0 + cn - 1];
+    __syncthreads();
+    for (int row = r0 + warp; row < r1; row += kW) {
+      long long b = c == 0 ? __ldg(rp + row) : __ldg(csplit + (size_t)(c - 1) * n + row);
+      long long e = c == nch - 1 ? __ldg(rp + row + 1) : __ldg(csplit + (size_t)c * n + row);
+      if (e > nnz_used) e = nnz_used;
+      if (b >= e && c > 0) continue;  // nothing of this row in this chunk
+      float sh = 0.0f, sl = 0.0f;
+      if (b < e) ec_row_accum_smem<VK>(ci, val, vald, xs, c0, b, e, lane, sh, sl);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+        float s2, e2;
+        two_sum(sh, oh, s2, e2);
+        sh = s2;
+        sl = __fadd_rn(sl, __fadd_rn(ol, e2));
+      }
+      if (lane == 0) {
+        float2* pr = in_smem ? &ps[row - r0] : &part[row];
+        if (c > 0) {  // add to the row's sum of the earlier chunks
+          const float2 p = *pr;
+          float s2, e2;
+          two_sum(p.x, sh, s2, e2);
+          sh = s2;
+          sl = __fadd_rn(__fadd_rn(p.y, sl), e2);
+        }
+        *pr = make_float2(sh, sl);
+      }
+    }
+  }
+  __syncthreads();  // every row's sum is in ps[] / part[]
+  const double lam = lam_s[0], inv = lam_s[1];
+  double a0 = 0, a1 = 0, a2 = 0;
+  for (int row = r0 + (int)threadIdx.x; row < r1; row += kEcChunkThreads) {
+    long long b = __ldg(rp + row), e = __ldg(rp + row + 1);
+    if (e > nnz_used) e = nnz_used;
+    const float2 sm = in_smem ? ps[row - r0] : part[row];
+    // a row without entries gives 0 even when 1 / lambda is infinite
+    const double y = e <= b ? 0.0 : ((double)sm.x + (double)sm.y) * inv;
+    const double old = u[row];
+    un[row] = y;
+    unf[row] = split_df(y);
+    a0 += y * y;
+    const double d = y - old, p = y + old;
+    a1 += d * d;
+    a2 += p * p;
+  }
+  // block partials: warp butterflies, then the warps' sums by warp 0
+  __shared__ double ws[kW][3];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  }
+  if (lane == 0) {
+    ws[warp][0] = a0;
+    ws[warp][1] = a1;
+    ws[warp][2] = a2;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    double t0 = ws[lane][0], t1 = ws[lane][1], t2 = ws[lane][2];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+      t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+      t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+    }
+    if (lane == 0) {
+      parts[blockIdx.x * 3 + 0] = t0;
+      parts[blockIdx.x * 3 + 1] = t1;
+      parts[blockIdx.x * 3 + 2] = t2;
+    }
+  }
+  // the last block to finish reduces the blocks' partials (warp 0: strided
+  // sums per lane, then a butterfly; a fixed order)
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(&st->counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (warp == 0) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+      t0 += __ldcg(parts + b * 3 + 0);
+      t1 += __ldcg(parts + b * 3 + 1);
+      t2 += __ldcg(parts + b * 3 + 2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+      t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+      t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+    }
+    if (lane == 0) {
+      st->lambda_used = lam;
+      st->lam2 = t0;
+      st->e1 = sqrt(t1);
+      st->e2 = sqrt(t2);
+      st->iter += 1;
+      if (st->e1 <= eps || st->e2 <= eps) st->done = 1;
+      st->counter = 0;
+    }
+  }
+}
+
+// Columns ascending within every row (the chunked form needs it):
+// info[0] = 1 if some row is not; and the gathers' locality: info[1] = the
+// entries whose iterate pair lies in another 32-byte sector than the row's
+// previous entry's (about every entry for a graph without column locality).
+// Warp per row.
+__global__ void ec_sorted_kernel(int n, const int32_t* __restrict__ rp,
+                                 const int32_t* __restrict__ ci, long long nnz_used,
+                                 unsigned long long* info) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  unsigned long long fresh = 0;
+  bool bad = false;
+  for (long long row = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); row < n;
+       row += nw) {
+    long long b = rp[row], e = rp[row + 1];
+    if (e > nnz_used) e = nnz_used;
+    for (long long k = b + lane; k < e; k += 32) {
+      const int cur = ci[k];
+      const int prev = k > b ? ci[k - 1] : -8;
+      bad |= k > b && cur <= prev;
+      fresh += (cur >> 2) != (prev >> 2);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) fresh += __shfl_xor_sync(0xffffffffu, fresh, o);
+  bad = __any_sync(0xffffffffu, bad);
+  if (lane == 0) {
+    if (bad) atomicOr(info, 1ull);
+    if (fresh) atomicAdd(info + 1, fresh);
+  }
+}
+
+// Chunk boundaries of every row: csplit[(c - 1) * n + row] = the first entry
+// of the row with a column >= c * kEcChunkCols (binary search), c = 1..nch-1;
+// and the block ranges: rowsplit[b] = the first row r with rp[r] + w r >=
+// b (nnz_used + w n) / G.
+__global__ void ec_split_kernel(int n, const int32_t* __restrict__ rp,
+                                const int32_t* __restrict__ ci, long long nnz_used, int nch,
+                                int* csplit, int G, int* rowsplit) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) {
+    const int row = (int)t;
+    long long b = rp[row], e = rp[row + 1];
+    if (e > nnz_used) e = nnz_used;
+    if (b > e) b = e;
+    for (int c = 1; c < nch; ++c) {
+      const int col = c * kEcChunkCols;
+      long long lo = b, hi = e;
+      while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (ci[mid] < col) lo = mid + 1; else hi = mid;
+      }
+      csplit[(size_t)(c - 1) * n + row] = (int)lo;
+    }
+  }
+  if (t <= G) {
+    const double total = (double)nnz_used + (double)kEcRowWeight * n;
+    const double want = total * (double)t / (double)G;
+    int lo = 0, hi = n;
+    while (lo < hi) {  // first r with min(rp[r], nnz_used) + w r >= want
+      const int mid = (lo + hi) >> 1;
+      const double f = (double)min((long long)rp[mid], nnz_used) + (double)kEcRowWeight * mid;
+      if (f < want) lo = mid + 1; else hi = mid;
+    }
+    rowsplit[t] = t == G ? n : lo;
+  }
+}
+
 // ---- persistent form ----------------------------------------------------------
 
 // Grid barrier for a cooperative launch (all blocks co-resident).  Bounded:
@@ -534,6 +791,60 @@ cudaError_t launch_ec_coop(int n, const int32_t* rp, const int32_t* ci, const fl
 }
 
 size_t ec_state_bytes() { return sizeof(EcState); }
+
+int ec_chunk_count(int n) { return (n + kEcChunkCols - 1) / kEcChunkCols; }
+
+// The chunked form's preparation: rows sorted and gather locality (info, read
+// by the caller), chunk splits and block ranges.  csplit: (nch - 1) x n ints; rowsplit:
+// grid + 1 ints.
+cudaError_t launch_ec_chunk_prep(int n, const int32_t* rp, const int32_t* ci, long long nnz_used,
+                                 unsigned long long* info, int* csplit, int grid, int* rowsplit,
+                                 cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(info, 0, 2 * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  const int blocks = (n + 7) / 8 < 4096 ? (n + 7) / 8 : 4096;
+  ec_sorted_kernel<<<blocks > 0 ? blocks : 1, 256, 0, stream>>>(n, rp, ci, nnz_used, info);
+  const long long cnt = (long long)n > grid + 1 ? n : grid + 1;
+  ec_split_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, stream>>>(
+      n, rp, ci, nnz_used, ec_chunk_count(n), csplit, grid, rowsplit);
+  return cudaGetLastError();
+}
+
+// Shared-memory limit of the chunked kernels (set outside any capture).
+cudaError_t prepare_ec_chunk() {
+  const int smem = (kEcChunkCols + kEcChunkRowsSmem) * (int)sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(ec_chunk_kernel<0>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(ec_chunk_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(ec_chunk_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+  return e;
+}
+
+cudaError_t launch_ec_chunk(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                            const double* vald, long long nnz_used, const double* u,
+                            const float2* uf, double* un, float2* unf, double* parts, void* st,
+                            int grid, int max_iter, double eps, const int* rowsplit,
+                            const int* csplit, float2* part, cudaStream_t stream) {
+  const int nch = ec_chunk_count(n);
+  const size_t smem = (size_t)(kEcChunkCols + kEcChunkRowsSmem) * sizeof(float2);
+  if (val)
+    ec_chunk_kernel<1><<<grid, kEcChunkThreads, smem, stream>>>(
+        n, rp, ci, val, vald, nnz_used, u, uf, un, unf, parts, (EcState*)st, max_iter, eps,
+        rowsplit, csplit, nch, part);
+  else if (vald)
+    ec_chunk_kernel<2><<<grid, kEcChunkThreads, smem, stream>>>(
+        n, rp, ci, val, vald, nnz_used, u, uf, un, unf, parts, (EcState*)st, max_iter, eps,
+        rowsplit, csplit, nch, part);
+  else
+    ec_chunk_kernel<0><<<grid, kEcChunkThreads, smem, stream>>>(
+        n, rp, ci, val, vald, nnz_used, u, uf, un, unf, parts, (EcState*)st, max_iter, eps,
+        rowsplit, csplit, nch, part);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ec_init(int n, double* u, float2* uf, double* parts, void* st, int grid,
                            int max_iter, cudaStream_t stream) {

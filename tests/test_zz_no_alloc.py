@@ -99,8 +99,9 @@ def test_noalloc_per_iteration_path_matches_oracle_and_bna_ec(weighted):
         assert s == (L.BNA_OK if conv_o else L.BNA_NOT_CONVERGED)
         assert it == it_o == it_b
         assert np.max(np.abs(ec - ec_o)) <= 1e-5 * scale
-        assert np.array_equal(ec, ec_b)
-        assert abs(lam - lam_o) <= 1e-5 * abs(lam_o) and lam == lam_b
+        # bna_ec may sum the rows in another order (its column-chunked form)
+        assert np.max(np.abs(ec - ec_b)) <= 1e-12 * scale
+        assert abs(lam - lam_o) <= 1e-5 * abs(lam_o) and abs(lam - lam_b) <= 1e-12 * abs(lam_b)
 
 
 @pytest.mark.parametrize("n,deg,max_iter", [(60000, 6, 7), (60000, 6, 45), (3000, 4, 5)])
