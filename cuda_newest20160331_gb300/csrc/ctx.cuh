@@ -167,7 +167,8 @@ struct EcGraph {
   cudaGraphExec_t exec = nullptr;
   int iters = 0;  // iterations per replay
   bool chunked = false;  // the column-chunked kernel
-  const void* key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // the CSR, the iterate, the state block, and the chunked kernel's buffers
+  const void* key[9] = {};
   int n = -1, grid = 0, max_iter = 0;
   long long nnz_used = -1;
   double eps = 0;

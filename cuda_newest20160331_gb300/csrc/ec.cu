@@ -399,7 +399,7 @@ __global__ __launch_bounds__(kEcChunkThreads, 1) void ec_chunk_kernel(
     float2* __restrict__ unf, double* parts, EcState* st, int max_iter, double eps,
     const int* __restrict__ rowsplit, const int* __restrict__ csplit, int nch,
     float2* __restrict__ part) {
-  extern __shared__ float2 xs[];
+  extern __shared__ __align__(16) float2 xs[];
   if (st->done || st->iter >= max_iter) return;
   __shared__ double lam_s[2];
   if (threadIdx.x == 0) {
@@ -417,11 +417,16 @@ __global__ __launch_bounds__(kEcChunkThreads, 1) void ec_chunk_kernel(
     const int c0 = c * kEcChunkCols;
     const int cn = min(kEcChunkCols, n - c0);
     __syncthreads();  // the previous chunk's readers are done
-    // two pairs per 16-byte load (c0 is even: chunks are a multiple of 2 wide)
-    const float4* src4 = reinterpret_cast<const float4*>(uf + c0);
-    float4* dst4 = reinterpret_cast<float4*>(xs);
-    for (int k = threadIdx.x; k < cn / 2; k += kEcChunkThreads) dst4[k] = src4[k];
-    if ((cn & 1) && threadIdx.x == 0) xs[cn - 1] = uf[c0 + cn - 1];
+    // two pairs per 16-byte load when the chunk starts on a 16-byte boundary
+    // (the second iterate buffer starts at uf + n: 8-byte aligned for odd n)
+    if ((reinterpret_cast<uintptr_t>(uf + c0) & 15u) == 0) {
+      const float4* src4 = reinterpret_cast<const float4*>(uf + c0);
+      float4* dst4 = reinterpret_cast<float4*>(xs);
+      for (int k = threadIdx.x; k < cn / 2; k += kEcChunkThreads) dst4[k] = src4[k];
+      if ((cn & 1) && threadIdx.x == 0) xs[cn - 1] = uf[c0 + cn - 1];
+    } else {
+      for (int k = threadIdx.x; k < cn; k += kEcChunkThreads) xs[k] = uf[c0 + k];
+    }
     __syncthreads();
     for (int row = r0 + warp; row < r1; row += kW) {
       long long b = c == 0 ? __ldg(rp + row) : __ldg(csplit + (size_t)(c - 1) * n + row);
@@ -531,8 +536,9 @@ __global__ __launch_bounds__(kEcChunkThreads, 1) void ec_chunk_kernel(
   }
 }
 
-// Columns ascending within every row (the chunked form needs it):
-// info[0] = 1 if some row is not; and the gathers' locality: info[1] = the
+// Columns ascending within every row and inside [0, n) (the chunked form
+// needs both: its gathers index the staged chunk): info[0] = 1 if some row
+// breaks either; and the gathers' locality: info[1] = the
 // entries whose iterate pair lies in another 32-byte sector than the row's
 // previous entry's (about every entry for a graph without column locality).
 // Warp per row.
@@ -550,7 +556,7 @@ __global__ void ec_sorted_kernel(int n, const int32_t* __restrict__ rp,
     for (long long k = b + lane; k < e; k += 32) {
       const int cur = ci[k];
       const int prev = k > b ? ci[k - 1] : -8;
-      bad |= k > b && cur <= prev;
+      bad |= (k > b && cur <= prev) || cur < 0 || cur >= n;
       fresh += (cur >> 2) != (prev >> 2);
     }
   }

@@ -155,10 +155,10 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
     if (chunked) CK(prepare_ec_chunk());
   }
   EcGraph& g = ctx->ecg;
-  const void* key[6] = {rp, ci, val, vald, u, state};
+  const void* key[9] = {rp, ci, val, vald, u, state, csplit, rowsplit, part};
   bool same = g.exec && g.n == n && g.grid == grid && g.max_iter == max_iter && g.eps == eps &&
               g.nnz_used == nnz_used && g.iters == giters && g.chunked == chunked;
-  for (int k = 0; k < 6 && same; ++k) same = (g.key[k] == key[k]);
+  for (int k = 0; k < 9 && same; ++k) same = (g.key[k] == key[k]);
   if (!same) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = EcGraph();
@@ -181,7 +181,7 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
     ce = cudaGraphInstantiate(&g.exec, graph, 0);
     cudaGraphDestroy(graph);
     CK(ce);
-    for (int k = 0; k < 6; ++k) g.key[k] = key[k];
+    for (int k = 0; k < 9; ++k) g.key[k] = key[k];
     g.n = n;
     g.grid = grid;
     g.max_iter = max_iter;
