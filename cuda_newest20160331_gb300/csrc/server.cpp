@@ -46,7 +46,9 @@
 
 namespace bna {
 cudaMemPool_t lib_pool(int device);
-cudaError_t copy_from_host(const void* src, void* dst, size_t bytes, int sms, cudaStream_t stream);
+cudaError_t copy_from_host(const void* src, void* dst, size_t bytes, int sms, cudaStream_t stream,
+                           unsigned long long* blocks, int* grid_out);
+int upload_max_blocks();
 }
 int32_t bna_ctx_trim_idle(bna_ctx* ctx);
 
@@ -76,6 +78,8 @@ struct Slot {
   int64_t progress = 0;
   cudaEvent_t fence[2] = {};      // launch gate: queue-depth events
   cudaEvent_t tev[2] = {};        // trace: around the series upload
+  unsigned long long* upblk = nullptr;  // trace: the upload's block times and SMs (device)
+  int upgrid = 0;
   int nfence = 0;
   bna_ctx* ctx = nullptr;
   cudaStream_t stream[kLevels] = {};  // stream[0]: highest priority
@@ -239,6 +243,38 @@ void slot_gate(void* user, void* stream, int32_t phase, int64_t done) {
   }
 }
 
+// Trace: how the SM-driven upload's blocks ran (whether they started
+// together, how long each took, on how many SMs).
+void trace_upload_blocks(bna_server* srv, Slot* s, int64_t id) {
+  const int g = s->upgrid;
+  if (!s->upblk || g <= 0) return;
+  std::vector<unsigned long long> b(3 * (size_t)g);
+  if (cudaMemcpy(b.data(), s->upblk, b.size() * sizeof(unsigned long long),
+                 cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  unsigned long long s0 = ~0ull, s1 = 0, e1 = 0;
+  std::vector<double> dur;
+  std::vector<unsigned long long> sm;
+  for (int k = 0; k < g; ++k) {
+    s0 = std::min(s0, b[3 * k]);
+    s1 = std::max(s1, b[3 * k]);
+    e1 = std::max(e1, b[3 * k + 1]);
+    dur.push_back((double)(b[3 * k + 1] - b[3 * k]));
+    sm.push_back(b[3 * k + 2]);
+  }
+  std::sort(dur.begin(), dur.end());
+  std::sort(sm.begin(), sm.end());
+  trace(srv, s, id, "upload_grid", g);
+  trace(srv, s, id, "upload_start_spread_us", (int64_t)((s1 - s0) / 1000));
+  trace(srv, s, id, "upload_span_us", (int64_t)((e1 - s0) / 1000));
+  trace(srv, s, id, "upload_block_p50_us", (int64_t)(dur[dur.size() / 2] / 1000));
+  trace(srv, s, id, "upload_block_max_us", (int64_t)(dur.back() / 1000));
+  trace(srv, s, id, "upload_sms",
+        (int64_t)(std::unique(sm.begin(), sm.end()) - sm.begin()));
+}
+
 // One request on one slot.
 void run_job(bna_server* srv, Slot* s, Job* j) {
   const bna_request& r = j->req;
@@ -253,8 +289,10 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
   // (copy-engine uploads slowed to a few GB/s while other requests shared
   // the device); a pageable buffer takes the copy engine
   const double tu0 = srv->tracing ? srv->now() : 0.0;
+  s->upgrid = 0;
   if (rc == BNA_OK && (srv->upload_ce ||
-                       bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st) != cudaSuccess) &&
+                       bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st, s->upblk,
+                                           &s->upgrid) != cudaSuccess) &&
       cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = BNA_CUDA_ERROR;
   if (srv->tracing) {
@@ -312,6 +350,7 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
     if (cudaEventElapsedTime(&ms, s->tev[0], s->tev[1]) == cudaSuccess)
       trace(srv, s, j->id, "upload_device_us", (int64_t)(ms * 1000));
     cudaGetLastError();
+    trace_upload_blocks(srv, s, j->id);
   }
   trace(srv, s, j->id, "done");
   out.status = rc;
@@ -422,6 +461,12 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
     if (*tp) {
       srv->tracing = true;
       srv->trace_path = tp;
+      // the steady clock's reading at t = 0 (CLOCK_MONOTONIC on Linux), to
+      // line the trace up with other processes' records
+      trace(srv, nullptr, 0, "clock_origin_ns",
+            (int64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+                srv->t0.time_since_epoch())
+                .count());
     }
   }
   // numerically lower = higher priority; greatest <= least
@@ -438,6 +483,10 @@ int32_t bna_server_create(int32_t device, int32_t slots, int64_t hbm_budget_byte
         rc = BNA_CUDA_ERROR;
     for (auto& e : s->tev)
       if (rc == BNA_OK && cudaEventCreate(&e) != cudaSuccess) rc = BNA_CUDA_ERROR;
+    if (rc == BNA_OK && srv->tracing &&
+        cudaMalloc(&s->upblk, 3 * sizeof(unsigned long long) * bna::upload_max_blocks()) !=
+            cudaSuccess)
+      rc = BNA_CUDA_ERROR;
     if (rc == BNA_OK) rc = bna_ctx_set_gate(s->ctx, slot_gate, s);
     for (int l = 0; l < srv->levels && rc == BNA_OK; ++l)
       if (cudaStreamCreateWithPriority(&s->stream[l], cudaStreamNonBlocking, greatest + l) !=
@@ -537,6 +586,7 @@ int32_t bna_server_destroy(bna_server* srv) {
       if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : s->tev)
       if (e) cudaEventDestroy(e);
+    if (s->upblk) cudaFree(s->upblk);
     bna_ctx_destroy(s->ctx);
     delete s;
   }
