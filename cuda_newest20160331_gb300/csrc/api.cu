@@ -232,12 +232,15 @@ int32_t corr_pass(bna_ctx* ctx, const CorrArgs& a, int precision, int pass, cuda
       const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[sampled ? S_TILES_SMP : S_TILES]);
       const int nt = sampled ? ctx->ntiles_smp : ctx->ntiles;
       const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : nt;
+      unsigned int* sched;
+      ENSURE(S_TCSCHED, 2 * sizeof(unsigned int), sched);
+      CK(cudaMemsetAsync(sched, 0, 2 * sizeof(unsigned int), st));
       for (int t0 = 0; t0 < nt; t0 += per, ++ctx->klaunch) {
         if (t0 > 0) gate(ctx, st, BNA_PHASE_CORR, t0);
         CK(launch_corr_tc(a, pass, precision == BNA_PREC_BF16X3 ? 0 : 1, tiles + t0,
                           std::min(per, nt - t0),
                           reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
-                          ctx->sms, st));
+                          ctx->sms, sched, st));
       }
       return BNA_OK;
     }
@@ -985,8 +988,11 @@ int32_t bna_corr_tile_values(bna_ctx* ctx, const float* bold_dev, int32_t N, int
       ENSURE(S_DUMPTILE, sizeof(int2), d);
       const int2 t = make_int2(I, J / 2);
       CK(cudaMemcpyAsync(d, &t, sizeof t, cudaMemcpyHostToDevice, st));
+      unsigned int* sched;
+      ENSURE(S_TCSCHED, 2 * sizeof(unsigned int), sched);
+      CK(cudaMemsetAsync(sched, 0, 2 * sizeof(unsigned int), st));
       CK(launch_corr_tc(a, 2, precision == BNA_PREC_BF16X3 ? 0 : 1, d, 1, bb, out_dev, J % 2, 1,
-                        st));
+                        sched, st));
       CK(cudaStreamSynchronize(st));
       break;
     }

@@ -63,11 +63,14 @@ static int32_t avg_accumulate(bna_ctx* ctx, int32_t nsub, const float* const* bo
     AvgPass ap{packed, unc, fisher ? 1 : 0, fisher ? 0.9f : (float)(1.0 - dk)};
     const int2* tiles = reinterpret_cast<const int2*>(ctx->ptr[S_TILES]);
     const int per = ctx->tiles_per_launch > 0 ? ctx->tiles_per_launch : ctx->ntiles;
+    unsigned int* sched;
+    ENSURE(S_TCSCHED, 2 * sizeof(unsigned int), sched);
+    CK(cudaMemsetAsync(sched, 0, 2 * sizeof(unsigned int), st));
     for (int t0 = 0; t0 < ctx->ntiles; t0 += per, ++ctx->klaunch)
       CK(launch_corr_tc(as, 4, prec == BNA_PREC_BF16X3 ? 0 : 1, tiles + t0,
                         std::min(per, ctx->ntiles - t0),
                         reinterpret_cast<const uint8_t*>(ctx->ptr[S_BLOCKBAD]), nullptr, 0,
-                        ctx->sms, st, &ap));
+                        ctx->sms, sched, st, &ap));
     avg_subj_fill(subj_host.data(), k, as.z, as.bad, as.ldz, T[k]);
   }
   CK(cudaMemcpyAsync(subj_dev, subj_host.data(), subj_host.size(), cudaMemcpyHostToDevice, st));

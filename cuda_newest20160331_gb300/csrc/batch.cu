@@ -284,6 +284,10 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
   } guard;
   guard.s = st;
   cudaGraphExec_t& count_exec = guard.e;
+  // the launches' tile counters (each launch leaves them zero)
+  unsigned int* sched;
+  ENSURE(S_TCSCHED, 2 * sizeof(unsigned int), sched);
+  CK(cudaMemsetAsync(sched, 0, 2 * sizeof(unsigned int), st));
   {
     cudaStream_t cap;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -291,7 +295,7 @@ int32_t bna_corr_csr_batch(bna_ctx* ctx, int32_t nsub, const float* const* bold_
     for (int t0 = 0; ce == cudaSuccess && t0 < ctx->batch_ntiles; t0 += per, ++launches)
       ce = launch_corr_tc_multi(batch, table_dev, tiles4 + t0,
                                 std::min(per, ctx->batch_ntiles - t0), form, dev_sel, absm,
-                                ctx->sms, cap);
+                                ctx->sms, sched, cap);
     cudaGraph_t graph = nullptr;
     const cudaError_t ee = cudaStreamEndCapture(cap, &graph);
     if (ce == cudaSuccess) ce = ee;

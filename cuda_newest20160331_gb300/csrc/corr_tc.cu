@@ -63,8 +63,17 @@ constexpr int TC_EPI_THREADS = 256;
 constexpr uint32_t TC_TMEM_COLS = 512;
 constexpr uint64_t kWaitNs = 4000000000ull;
 
+// Tiles are claimed one at a time from a counter in global memory (a CTA
+// that starts late, its SM held by another stream's kernel, finds the tiles
+// already taken instead of holding the launch open); the TMA warp claims and
+// passes each tile's index to the MMA and epilogue warps through this queue.
+constexpr int kTileQ = 8;
+constexpr int kTileQReaders = 1 + TC_EPI_THREADS / 32;  // the MMA thread, each epilogue warp
+
 struct TcSmem {
   uint64_t full[TC_MAX_STAGES], empty[TC_MAX_STAGES], tfull[2], tempty[2], done, hbar[2];
+  uint64_t qfull[kTileQ], qempty[kTileQ];
+  volatile int tq[kTileQ];  // claimed tile indices, -1 after the last
   uint32_t tmem_base;
   volatile uint32_t abort;
   uint32_t colmask[2][128][4];
@@ -82,6 +91,7 @@ struct TcSubj {  // 64-byte aligned through its CUtensorMap members
 };
 
 constexpr size_t TC_SMEM_BYTES = 1024 + (size_t)TC_RING_BYTES + sizeof(TcSmem);
+static_assert(TC_SMEM_BYTES <= 232448, "shared memory per CTA");
 
 struct TcArgs {
   CorrArgs a;
@@ -97,6 +107,9 @@ struct TcArgs {
   const TcSubj* subj;
   const int2* tiles;        // (I, Jp): rows of block I x columns of blocks 2Jp, 2Jp+1
   int ntiles;
+  // [0]: next tile to claim, [1]: CTAs finished; zero at launch, reset to
+  // zero by the launch's last CTA
+  unsigned int* sched;
   int nksteps;              // MMA K steps = ceil(T / elements per step)
   const uint8_t* blockbad;  // [nb]: block holds a voxel with NaN z
   float* dump;              // dump pass: 128 x 128 values of half `dump_half`
@@ -171,6 +184,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       ptx::mbar_init(ptx::smem_u32(&S.hbar[s]), 128);
     }
     ptx::mbar_init(ptx::smem_u32(&S.done), 1);
+    for (int s = 0; s < kTileQ; ++s) {
+      ptx::mbar_init(ptx::smem_u32(&S.qfull[s]), 1);
+      ptx::mbar_init(ptx::smem_u32(&S.qempty[s]), kTileQReaders);
+    }
     S.abort = 0;
     ptx::fence_mbar_init();
   }
@@ -196,7 +213,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       uint32_t f = 0;
       int last_round[TC_STAGES];
       for (int s = 0; s < TC_STAGES; ++s) last_round[s] = -1;
-      for (int t = blockIdx.x; t < p.ntiles && !S.abort; t += gridDim.x) {
+      int m = 0;
+      // the m-th claimed tile's index into the queue (bounded wait for its slot)
+      auto publish = [&](int t) {
+        const int qs = m % kTileQ;
+        const uint32_t qr = (uint32_t)(m / kTileQ);
+        if (!ptx::mbar_wait(ptx::smem_u32(&S.qempty[qs]), (qr & 1u) ^ 1u, kWaitNs)) return false;
+        S.tq[qs] = t;
+        ptx::mbar_arrive(ptx::smem_u32(&S.qfull[qs]));
+        ++m;
+        return true;
+      };
+      // the next tile is claimed while this one's copies are issued
+      int t = (int)atomicAdd(p.sched, 1u);
+      for (int t_next; t < p.ntiles && !S.abort; t = t_next) {
+        if (!publish(t)) {
+          atomicOr(a.err, ERR_TIMEOUT);
+          S.abort = 1;
+          break;
+        }
+        t_next = (int)atomicAdd(p.sched, 1u);
         int2 tile;
         const CUtensorMap* mh = &tm_hi;
         const CUtensorMap* ml = &tm_lo;
@@ -237,6 +273,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           last_round[s] = (int)round;
         }
       }
+      publish(-1);  // the end (on a timeout the readers' own bounded waits end)
       // drain: every issued copy must have landed before the CTA exits
       for (int s = 0; s < TC_STAGES; ++s)
         if (last_round[s] >= 0)
@@ -249,9 +286,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       constexpr uint32_t idesc = FORM == FORM_BF16X3 ? ptx::make_idesc(1, 1, TC_BM, TC_BN)
                                                      : ptx::make_idesc(2, 2, TC_BM, TC_BN);
       uint32_t f = 0;
-      int m = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < p.ntiles && ok && !S.abort; t += gridDim.x, ++m) {
+      for (int m = 0; !S.abort; ++m) {
+        const int qs = m % kTileQ;
+        if (!ptx::mbar_wait(ptx::smem_u32(&S.qfull[qs]), (uint32_t)(m / kTileQ) & 1u, kWaitNs)) {
+          ok = false;
+          break;
+        }
+        const int t = S.tq[qs];
+        ptx::mbar_arrive(ptx::smem_u32(&S.qempty[qs]));
+        if (t < 0) break;
         const int acc = m & 1;
         const uint32_t ar = (uint32_t)(m >> 1);
         if (!ptx::mbar_wait(ptx::smem_u32(&S.tempty[acc]), (ar & 1u) ^ 1u, kWaitNs)) {
@@ -376,8 +420,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       __syncwarp();
     };
-    int m = 0;
-    // tile coordinates and NaN-block flags run one tile ahead
     auto tile_at = [&](int t, int2& tl, int& ts) {
       if (MULTI) {
         const int4 t4 = p.tiles4[t];
@@ -395,26 +437,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int jj = 2 * tl.y + h;
       fj = jj < nbs ? bbad[jj] : 0;
     };
-    int2 nxt = make_int2(0, 0);
-    int nxt_s = 0;
-    uint8_t nbi = 0, nbj = 0;
-    if ((int)blockIdx.x < p.ntiles) {
-      tile_at(blockIdx.x, nxt, nxt_s);
-      flags_of(nxt, nxt_s, nbi, nbj);
-      enter(nxt_s);
-    } else {
-      enter(MULTI ? 0 : 0);
-    }
-    for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x, ++m) {
+    for (int m = 0;; ++m) {
       if (S.abort) break;
-      const int2 tile = nxt;
-      const int tile_s = nxt_s;
-      const bool bad_i = nbi != 0, bad_j = nbj != 0;
-      if (t + (int)gridDim.x < p.ntiles) {
-        tile_at(t + gridDim.x, nxt, nxt_s);
-        flags_of(nxt, nxt_s, nbi, nbj);
+      const int qs = m % kTileQ;
+      if (!ptx::mbar_wait(ptx::smem_u32(&S.qfull[qs]), (uint32_t)(m / kTileQ) & 1u, kWaitNs)) {
+        atomicOr(p.a.err, ERR_TIMEOUT);  // (this warp's `a` is set by its first tile)
+        S.abort = 1;
+        break;
       }
-      if (MULTI && tile_s != cur_s) {
+      const int t = S.tq[qs];
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(ptx::smem_u32(&S.qempty[qs]));
+      if (t < 0) break;
+      int2 tile;
+      int tile_s;
+      uint8_t nbi, nbj;
+      tile_at(t, tile, tile_s);
+      flags_of(tile, tile_s, nbi, nbj);
+      const bool bad_i = nbi != 0, bad_j = nbj != 0;
+      if (tile_s != cur_s) {  // the first tile, or another subject's
         leave();
         enter(tile_s);
       }
@@ -686,6 +727,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (PASS == 3)
     for (int b = threadIdx.x; b <= kHistBins; b += blockDim.x)
       if (S.hist[b]) atomicAdd(&a.hist[b], S.hist[b]);
+  // every CTA has stopped claiming by now: the last one resets the counters
+  if (threadIdx.x == 0 && atomicAdd(p.sched + 1, 1u) == gridDim.x - 1) {
+    p.sched[0] = 0;
+    p.sched[1] = 0;
+  }
 }
 
 // After the last launch of a count pass: mark the unused slots of every
@@ -865,10 +911,11 @@ cudaError_t prepare_corr_tc_multi(int form, bool dens, bool absm) {
 
 cudaError_t launch_corr_tc_multi(const CorrArgs& batch, const void* subj_dev, const int4* tiles4,
                                  int ntiles, int form, bool dens, bool absm, int grid,
-                                 cudaStream_t st) {
-  if (dens && absm) return cudaErrorInvalidValue;
+                                 unsigned int* sched, cudaStream_t st) {
+  if ((dens && absm) || !sched) return cudaErrorInvalidValue;
   TcArgs p{};
   p.a = batch;
+  p.sched = sched;
   p.tiles4 = tiles4;
   p.subj = static_cast<const TcSubj*>(subj_dev);
   p.ntiles = ntiles;
@@ -891,7 +938,8 @@ cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t s
 // 3 density histogram; form FORM_BF16X3 or FORM_TF32
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
-                           cudaStream_t st, const AvgPass* avg) {
+                           unsigned int* sched, cudaStream_t st, const AvgPass* avg) {
+  if (!sched) return cudaErrorInvalidValue;
   CUtensorMap mh, ml;
   if (form == FORM_BF16X3) {
     if (!a.zhi || !a.zlo || a.ldb % 64 != 0) return cudaErrorInvalidValue;
@@ -903,8 +951,9 @@ cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* ti
     if (!make_map(&mh, a.z, a.ldz, a.n_pad, true)) return cudaErrorInvalidValue;
     ml = mh;
   }
-  TcArgs p;
+  TcArgs p{};
   p.a = a;
+  p.sched = sched;
   p.tiles = tiles;
   p.ntiles = ntiles;
   const int per_step = form == FORM_BF16X3 ? Form<FORM_BF16X3>::kElemsPerStep

@@ -91,16 +91,17 @@ long long tc_tile_count(int nb);
 cudaError_t launch_tile_lists(int nb, int band, int2* tiles, long long n_smp, int s, int2* smp,
                               cudaStream_t st);
 cudaError_t launch_block_bad(const uint8_t* bad, int nb, uint8_t* blockbad, cudaStream_t st);
+// sched: the launch's tile counters (two, zero; the launch leaves them zero)
 cudaError_t launch_corr_tc(const CorrArgs& a, int pass, int form, const int2* tiles, int ntiles,
                            const uint8_t* blockbad, float* dump, int dump_half, int grid,
-                           cudaStream_t st, const AvgPass* avg = nullptr);
+                           unsigned int* sched, cudaStream_t st, const AvgPass* avg = nullptr);
 cudaError_t launch_seal_candidates(const CorrArgs& a, int nwarps, cudaStream_t st);
 size_t tc_subj_bytes();
 bool tc_subj_fill(void* host, int s, const CorrArgs& a, const uint8_t* blockbad, int form);
 cudaError_t prepare_corr_tc_multi(int form, bool dens, bool absm);
 cudaError_t launch_corr_tc_multi(const CorrArgs& batch, const void* subj_dev, const int4* tiles4,
                                  int ntiles, int form, bool dens, bool absm, int grid,
-                                 cudaStream_t st);
+                                 unsigned int* sched, cudaStream_t st);
 cudaError_t launch_rowlen_scan(const long long* rowlen, int n, long long* pre, long long* bsum,
                                long long* total, int32_t* row_ptr, uint32_t* err,
                                cudaStream_t stream);
@@ -150,7 +151,7 @@ enum Slot {
   S_BATCH_SUBJ, S_BATCH_TILES,
   S_MOD_LABEL, S_MOD_ROWS, S_MOD_LOC, S_MOD_CNT, S_MOD_LRP, S_MOD_LCI, S_MOD_VD, S_MOD_VF,
   S_MOD_RS, S_MOD_Y, S_MOD_PARTS, S_MOD_GROUPS, S_MOD_BLKGRP, S_MOD_ASSIGN, S_MOD_KMOD,
-  S_MOD_ADJ, S_EC_SPLIT, S_EC_PART, S_EC_ROWS, S_EC_FLAG, S_COUNT
+  S_MOD_ADJ, S_EC_SPLIT, S_EC_PART, S_EC_ROWS, S_EC_FLAG, S_TCSCHED, S_COUNT
 };
 
 // Small device block the host reads once per pass.

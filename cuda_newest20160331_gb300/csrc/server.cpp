@@ -107,6 +107,8 @@ int level_of(double work, int levels) {
 int tiles_per_launch(int T) { return std::max(512, (int)(1536LL * 1200 / std::max(T, 1))); }
 // Longest wait of one gate call for higher-priority requests to finish.
 constexpr int kGateWaitMs = 200;
+// Series uploads go in chunks of this size, with the launch gate before each.
+constexpr size_t kUploadChunk = 32u << 20;
 // A centrality past this many iterations (a graph that converges slowly or
 // never: the reference stops at 10,000) no longer holds up other requests;
 // such centralities run one at a time, in the order their requests started.
@@ -287,14 +289,23 @@ void run_job(bna_server* srv, Slot* s, Job* j) {
   if (srv->tracing) cudaEventRecord(s->tev[0], st);
   // the series by an SM-driven copy from the caller's page-locked buffer
   // (copy-engine uploads slowed to a few GB/s while other requests shared
-  // the device); a pageable buffer takes the copy engine
+  // the device); a pageable buffer takes the copy engine.  In chunks with the
+  // launch gate before each, the first included: a large request's upload
+  // waits while a smaller request runs (an upload whose host reads had turned
+  // slow, beside a small request, stretched that request's every kernel
+  // several-fold).
   const double tu0 = srv->tracing ? srv->now() : 0.0;
   s->upgrid = 0;
-  if (rc == BNA_OK && (srv->upload_ce ||
-                       bna::copy_from_host(r.bold_host, s->bold, bytes, srv->sms, st, s->upblk,
-                                           &s->upgrid) != cudaSuccess) &&
-      cudaMemcpyAsync(s->bold, r.bold_host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    rc = BNA_CUDA_ERROR;
+  for (size_t off = 0; rc == BNA_OK && off < bytes; off += kUploadChunk) {
+    slot_gate(s, st, BNA_PHASE_UPLOAD, (int64_t)off);
+    const size_t n = std::min(kUploadChunk, bytes - off);
+    const char* src = reinterpret_cast<const char*>(r.bold_host) + off;
+    char* dst = reinterpret_cast<char*>(s->bold) + off;
+    if ((srv->upload_ce ||
+         bna::copy_from_host(src, dst, n, srv->sms, st, s->upblk, &s->upgrid) != cudaSuccess) &&
+        cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      rc = BNA_CUDA_ERROR;
+  }
   if (srv->tracing) {
     trace(srv, s, j->id, "upload_call_us", (int64_t)((srv->now() - tu0) * 1e6));
     cudaEventRecord(s->tev[1], st);

@@ -167,8 +167,14 @@ int32_t bna_ctx_set_option(bna_ctx* ctx, int32_t option, int64_t value);
  * the fill runs in row-block chunks and a centrality launch or replay holds
  * about a millisecond of iterations.  The gate may block, e.g. to keep a large
  * request from queueing work while a smaller one runs (the server's use).
- * NULL removes it. */
-typedef enum bna_phase { BNA_PHASE_CORR = 0, BNA_PHASE_FILL = 1, BNA_PHASE_EC = 2 } bna_phase;
+ * NULL removes it.  BNA_PHASE_UPLOAD (done = bytes uploaded) is the server's
+ * own call before each chunk of a request's series upload. */
+typedef enum bna_phase {
+  BNA_PHASE_CORR = 0,
+  BNA_PHASE_FILL = 1,
+  BNA_PHASE_EC = 2,
+  BNA_PHASE_UPLOAD = 3
+} bna_phase;
 typedef void (*bna_gate_fn)(void* user, void* stream, int32_t phase, int64_t done);
 int32_t bna_ctx_set_gate(bna_ctx* ctx, bna_gate_fn gate, void* user);
 
