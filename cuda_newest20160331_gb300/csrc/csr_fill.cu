@@ -32,6 +32,32 @@ constexpr int kFillWarps = 8;
 constexpr long long kFillDenseE = 1024;  // entries above which a sub-tile takes the dense path
 constexpr int kFillDenseLoads = 8;       // edge-list loads in flight per thread (dense path)
 
+// Asynchronous global -> shared copies (no registers held while in flight).
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 __device__ __forceinline__ int popc_before4(const uint32_t* m, int pos) {
   const int w = pos >> 5;
   int c = __popc(m[w] & ((1u << (pos & 31)) - 1u));
@@ -48,84 +74,155 @@ __device__ __forceinline__ int popc_before4(const uint32_t* m, int pos) {
 // (transposed); the diagonal sub-tile both.  Each CSR row is thus written by
 // `parts` CTAs, each filling one contiguous stretch of it segment after
 // segment while it runs, so partial sectors are completed in L2 instead of
-// being read back and written piecemeal.  Per sub-tile, the rows' segment
-// starts are loaded before the entries (no dependence between the two) and a
-// lane keeps its first kFillKeep entries, candidates already resolved, in
-// registers for the placing pass.  Sub-tiles above kFillDenseE entries are
-// queued (once) for csr_fill_dense_kernel.
+// being read back and written piecemeal.  A lane keeps its first kFillKeep
+// entries, candidates resolved, in registers for the placing pass.
+// Sub-tiles above kFillDenseE entries are queued (once) for
+// csr_fill_dense_kernel.  The block's row starts are read once into shared
+// memory, and each warp's loads run ahead of its work by asynchronous copies
+// into shared memory: while it places a sub-tile's entries, the next
+// sub-tile's segment offsets and first kFillStage entries and the ranges of
+// the one after that are in flight (the entries' load latency was the
+// kernel's main stall).
 constexpr int kFillKeep = 8;
+constexpr int kFillStage = 128;  // entries staged per warp ahead of use
 
-__global__ __launch_bounds__(kFillWarps * 32) void csr_fill_rows_kernel(CorrArgs a, int I0,
-                                                                        int parts) {
+__global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrArgs a, int I0,
+                                                                           int parts) {
   __shared__ uint32_t rmask[kFillWarps][128][4];  // direct: row il's columns jl
   __shared__ uint32_t tmask[kFillWarps][128][4];  // transposed: row jl's columns il
   __shared__ int dbase[kFillWarps][128];
   __shared__ int tbase[kFillWarps][128];
+  __shared__ int rp_s[128];                        // row_ptr of the block's rows (0 past the end)
+  __shared__ int nsg[kFillWarps][128];             // staged: rows' block-J segment offsets
+  __shared__ longlong2 netab[kFillWarps][2][4];    // staged: quadrant ranges (two sub-tiles)
+  __shared__ uint2 ent[kFillWarps][kFillStage];    // staged: first entries (raw)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int Ir = blockIdx.x / parts, part = blockIdx.x - Ir * parts;
   const int I = I0 + Ir;
   const int per = (a.nb + parts - 1) / parts;
   const int j0 = part * per, j1 = min(a.nb, j0 + per);
+  if (threadIdx.x < 128) {
+    const int gi = I * 128 + (int)threadIdx.x;
+    rp_s[threadIdx.x] = gi < a.n ? a.row_ptr[gi] : 0;
+  }
+  __syncthreads();
   uint32_t(*rm)[4] = rmask[w];
   uint32_t(*tm)[4] = tmask[w];
-  for (int J = j0 + w; J < j1; J += kFillWarps) {
-    const int lo = min(I, J), hi = max(I, J);
-    const long long st = subtile_index(lo, hi, a.nb);
-    long long s0 = 0, c0 = 0;
-    if (lane < 4) {
-      const longlong2 e = a.etab[st * 4 + lane];
-      s0 = e.x;
-      c0 = e.y;
-    }
-    int rbeg[4];  // rows lane + 32k: start of their block-J segment
+  // a sub-tile's four quadrant ranges (lanes 0-3)
+  auto fetch_ranges = [&](int J, int slot) {
+    const long long st = subtile_index(min(I, J), max(I, J), a.nb);
+    if (lane < 4) cp_async16(&netab[w][slot][lane], a.etab + st * 4 + lane);
+  };
+  // its rows' segment offsets (rows past the last real one read the padding,
+  // never used) and, when the fill places it here, its first entries; its
+  // ranges are in netab[w][slot]
+  auto fetch_rest = [&](int J, int slot) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int gi = I * 128 + lane + 32 * k;
-      rbeg[k] = gi < a.n ? a.row_ptr[gi] + a.seg[(size_t)J * a.n_pad + gi] : 0;
-    }
-    long long start[4], cnt[4];
+    for (int k = 0; k < 4; ++k)
+      cp_async4(&nsg[w][lane + 32 * k], a.seg + (size_t)J * a.n_pad + I * 128 + lane + 32 * k);
+    long long s[4], c[4];
+    bool inside = true;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      start[q] = __shfl_sync(0xffffffffu, s0, q);
-      cnt[q] = __shfl_sync(0xffffffffu, c0, q);
+      const longlong2 r = netab[w][slot][q];
+      s[q] = r.x;
+      c[q] = r.y;
+      inside &= c[q] >= 0 && s[q] >= 0 && s[q] + c[q] <= a.ecap;
     }
+    const long long E = c[0] + c[1] + c[2] + c[3];
+    if (!inside || E > kFillDenseE) return;
+    const long long p1 = c[0], p2 = p1 + c[1], p3 = p2 + c[2];
+#pragma unroll
+    for (int k = 0; k < kFillStage / 32; ++k) {
+      const long long e = lane + 32 * k;
+      if (e < E) {
+        const long long at = e < p1 ? s[0] + e : e < p2 ? s[1] + (e - p1)
+                             : e < p3 ? s[2] + (e - p2) : s[3] + (e - p3);
+        cp_async8(&ent[w][e], a.elist + at);
+      }
+    }
+  };
+  int v = 0;  // this warp's sub-tile count (range slot v & 1)
+  if (j0 + w < j1) {
+    fetch_ranges(j0 + w, 0);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncwarp();
+    fetch_rest(j0 + w, 0);
+    if (j0 + w + kFillWarps < j1) fetch_ranges(j0 + w + kFillWarps, 1);
+    cp_async_commit();
+  }
+  for (int J = j0 + w; J < j1; J += kFillWarps, ++v) {
+    const int slot = v & 1;
+    const int lo = min(I, J), hi = max(I, J);
+    cp_async_wait_all();
+    __syncwarp();
+    long long s0 = 0, c0 = 0;
+    if (lane < 4) {
+      s0 = netab[w][slot][lane].x;
+      c0 = netab[w][slot][lane].y;
+    }
+    // rows lane + 32k: start of their block-J segment (the transposed
+    // entries' base; the previous sub-tile's placing is over)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tbase[w][lane + 32 * k] = rp_s[lane + 32 * k] + nsg[w][lane + 32 * k];
+    // entry e of quadrant q is elist[b[q] + e] for p[q] <= e < p[q + 1]
+    long long b[4], p1 = 0, p2 = 0, p3 = 0, E = 0;
     bool inside = true;  // ranges written while the pool overflowed are not read
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      inside &= cnt[q] >= 0 && start[q] >= 0 && start[q] + cnt[q] <= a.ecap;
-    const long long E = cnt[0] + cnt[1] + cnt[2] + cnt[3];
-    if (!inside || E == 0 || E > kFillDenseE) continue;  // flagged / placed by the dense pass
-    const bool diag = I == J, trans = J < I;
-    for (int idx = lane; idx < 512; idx += 32) {
-      (&rm[0][0])[idx] = 0u;
-      (&tm[0][0])[idx] = 0u;
+    for (int q = 0; q < 4; ++q) {
+      const long long st = __shfl_sync(0xffffffffu, s0, q);
+      const long long ct = __shfl_sync(0xffffffffu, c0, q);
+      inside &= ct >= 0 && st >= 0 && st + ct <= a.ecap;
+      b[q] = st - E;
+      E += ct;
+      if (q == 0) p1 = E;
+      if (q == 1) p2 = E;
+      if (q == 2) p3 = E;
     }
-    __syncwarp();
-    const long long p1 = cnt[0], p2 = p1 + cnt[1], p3 = p2 + cnt[2];
-    // entry e with its candidate bit resolved: bit 15 set = not an edge,
-    // .y = the value to store
-    auto entry = [&](long long e) {
-      const int q = e < p1 ? 0 : e < p2 ? 1 : e < p3 ? 2 : 3;
-      const long long off = e - (q == 0 ? 0 : q == 1 ? p1 : q == 2 ? p2 : p3);
-      const long long s = q == 0 ? start[0] : q == 1 ? start[1] : q == 2 ? start[2] : start[3];
-      uint2 en = a.elist[s + off];
+    const bool use = inside && E != 0 && E <= kFillDenseE;  // else flagged / the dense pass's
+    auto load = [&](long long e) {
+      return a.elist[e + (e < p1 ? b[0] : e < p2 ? b[1] : e < p3 ? b[2] : b[3])];
+    };
+    // candidate bit resolved: bit 15 set = not an edge, .y = the value to store
+    auto resolve = [&](uint2 en) {
       if ((en.x >> 14) & 1u) {
-        float v = 0.0f;
+        float val = 0.0f;
         bool edge = false;
-        hash_lookup(a, pair_key(lo * 128 + (en.x & 127), hi * 128 + ((en.x >> 7) & 127)), v, edge);
-        en.y = __float_as_uint(v);
+        hash_lookup(a, pair_key(lo * 128 + (en.x & 127), hi * 128 + ((en.x >> 7) & 127)), val,
+                    edge);
+        en.y = __float_as_uint(val);
         if (!edge) en.x |= 1u << 15;
       }
       return en;
     };
-    // 1. masks
+    const int kmax = use ? (int)min((E + 31) / 32, (long long)kFillKeep) : 0;
     uint2 keep[kFillKeep];
 #pragma unroll
     for (int k = 0; k < kFillKeep; ++k) {
       const long long e = lane + 32 * k;
       keep[k] = make_uint2(1u << 15, 0u);
-      if (e < E) keep[k] = entry(e);
+      if (k < kmax && e < E) keep[k] = k < kFillStage / 32 ? ent[w][e] : load(e);
     }
+    __syncwarp();  // the staged data read by every lane before the next copies land
+    if (J + kFillWarps < j1) {
+      fetch_rest(J + kFillWarps, slot ^ 1);
+      if (J + 2 * kFillWarps < j1) fetch_ranges(J + 2 * kFillWarps, slot);
+    }
+    cp_async_commit();
+    if (!use) continue;
+#pragma unroll
+    for (int k = 0; k < kFillKeep; ++k)
+      if (k < kmax) keep[k] = resolve(keep[k]);
+    const bool diag = I == J, trans = J < I;
+    // the masks this sub-tile uses: direct (rows of I), transposed (rows of
+    // J as columns of I), both on the diagonal
+    if (!trans)
+      for (int idx = lane; idx < 512; idx += 32) (&rm[0][0])[idx] = 0u;
+    if (trans || diag)
+      for (int idx = lane; idx < 512; idx += 32) (&tm[0][0])[idx] = 0u;
+    __syncwarp();
+    // 1. masks
     auto mark = [&](uint2 en) {
       if ((en.x >> 15) & 1u) return;
       const int il = en.x & 127, jl = (en.x >> 7) & 127;
@@ -133,34 +230,37 @@ __global__ __launch_bounds__(kFillWarps * 32) void csr_fill_rows_kernel(CorrArgs
       if (trans || diag) atomicOr(&tm[jl][il >> 5], 1u << (il & 31));
     };
 #pragma unroll
-    for (int k = 0; k < kFillKeep; ++k) mark(keep[k]);
-    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) mark(entry(e));
+    for (int k = 0; k < kFillKeep; ++k)
+      if (k < kmax) mark(keep[k]);
+    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) mark(resolve(load(e)));
     __syncwarp();
     // 2. segment bases of the block's rows for column block J (on the
     // diagonal the transposed entries, columns < the row, come first)
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int r = lane + 32 * k;
-      const int c = __popc(tm[r][0]) + __popc(tm[r][1]) + __popc(tm[r][2]) + __popc(tm[r][3]);
-      tbase[w][r] = rbeg[k];
-      dbase[w][r] = diag ? rbeg[k] + c : rbeg[k];
+      dbase[w][r] = diag ? tbase[w][r] + __popc(tm[r][0]) + __popc(tm[r][1]) + __popc(tm[r][2]) +
+                               __popc(tm[r][3])
+                         : tbase[w][r];
     }
     __syncwarp();
     // 3. place this block's entries: direct (row il) and transposed (row jl)
     auto place = [&](uint2 en) {
       if ((en.x >> 15) & 1u) return;
       const int il = en.x & 127, jl = (en.x >> 7) & 127;
-      const float v = __uint_as_float(en.y);
+      const float val = __uint_as_float(en.y);
       if (!trans)
-        put_edge(a, (long long)dbase[w][il] + popc_before4(rm[il], jl), hi * 128 + jl, v);
+        put_edge(a, (long long)dbase[w][il] + popc_before4(rm[il], jl), hi * 128 + jl, val);
       if (trans || diag)
-        put_edge(a, (long long)tbase[w][jl] + popc_before4(tm[jl], il), lo * 128 + il, v);
+        put_edge(a, (long long)tbase[w][jl] + popc_before4(tm[jl], il), lo * 128 + il, val);
     };
 #pragma unroll
-    for (int k = 0; k < kFillKeep; ++k) place(keep[k]);
-    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) place(entry(e));
+    for (int k = 0; k < kFillKeep; ++k)
+      if (k < kmax) place(keep[k]);
+    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) place(resolve(load(e)));
     __syncwarp();
   }
+  cp_async_wait_all();  // nothing in flight into shared memory at exit
 }
 
 // The dense sub-tiles' list (and the check of every sub-tile's ranges),
