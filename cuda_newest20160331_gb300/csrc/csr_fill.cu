@@ -58,6 +58,16 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// put_edge for positions in 32 bits (a CSR's row offsets are int32)
+__device__ __forceinline__ void put_edge32(const CorrArgs& a, int pos, int col, float v) {
+  if ((unsigned long long)(unsigned)pos >= (unsigned long long)a.nnz) {
+    atomicOr(a.err, ERR_RANGE);
+    return;
+  }
+  a.col_idx[pos] = col;
+  if (a.weighted) a.val[pos] = v;
+}
+
 __device__ __forceinline__ int popc_before4(const uint32_t* m, int pos) {
   const int w = pos >> 5;
   int c = __popc(m[w] & ((1u << (pos & 31)) - 1u));
@@ -88,8 +98,8 @@ constexpr int kFillStage = 128;  // entries staged per warp ahead of use
 
 __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrArgs a, int I0,
                                                                            int parts) {
-  __shared__ uint32_t rmask[kFillWarps][128][4];  // direct: row il's columns jl
-  __shared__ uint32_t tmask[kFillWarps][128][4];  // transposed: row jl's columns il
+  __shared__ __align__(16) uint32_t rmask[kFillWarps][128][4];  // direct: row il's columns jl
+  __shared__ __align__(16) uint32_t tmask[kFillWarps][128][4];  // transposed: row jl's columns il
   __shared__ int dbase[kFillWarps][128];
   __shared__ int tbase[kFillWarps][128];
   __shared__ int rp_s[128];                        // row_ptr of the block's rows (0 past the end)
@@ -217,10 +227,13 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
     const bool diag = I == J, trans = J < I;
     // the masks this sub-tile uses: direct (rows of I), transposed (rows of
     // J as columns of I), both on the diagonal
+    const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
     if (!trans)
-      for (int idx = lane; idx < 512; idx += 32) (&rm[0][0])[idx] = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) reinterpret_cast<uint4*>(rm)[lane + 32 * k] = zero4;
     if (trans || diag)
-      for (int idx = lane; idx < 512; idx += 32) (&tm[0][0])[idx] = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) reinterpret_cast<uint4*>(tm)[lane + 32 * k] = zero4;
     __syncwarp();
     // 1. masks
     auto mark = [&](uint2 en) {
@@ -249,10 +262,8 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
       if ((en.x >> 15) & 1u) return;
       const int il = en.x & 127, jl = (en.x >> 7) & 127;
       const float val = __uint_as_float(en.y);
-      if (!trans)
-        put_edge(a, (long long)dbase[w][il] + popc_before4(rm[il], jl), hi * 128 + jl, val);
-      if (trans || diag)
-        put_edge(a, (long long)tbase[w][jl] + popc_before4(tm[jl], il), lo * 128 + il, val);
+      if (!trans) put_edge32(a, dbase[w][il] + popc_before4(rm[il], jl), hi * 128 + jl, val);
+      if (trans || diag) put_edge32(a, tbase[w][jl] + popc_before4(tm[jl], il), lo * 128 + il, val);
     };
 #pragma unroll
     for (int k = 0; k < kFillKeep; ++k)
