@@ -110,8 +110,11 @@ constexpr int kGateWaitMs = 200;
 // Series uploads go in chunks of this size, with the launch gate before each.
 constexpr size_t kUploadChunk = 32u << 20;
 // A centrality past this many iterations (a graph that converges slowly or
-// never: the reference stops at 10,000) no longer holds up other requests;
-// such centralities run one at a time, in the order their requests started.
+// never: the reference stops at 10,000) no longer holds up other requests,
+// other such centralities included: they share the device (how many
+// iterations one still needs is not known, and run one at a time a request
+// whose centrality converged soon after this mark waited 0.35 s behind a
+// never-converging one).
 constexpr int64_t kLongEc = 1000;
 
 }  // namespace
@@ -200,6 +203,7 @@ void release_slot_memory(Slot* s) {
 
 bool long_ec(const Slot* s) { return s->phase == BNA_PHASE_EC && s->progress >= kLongEc; }
 
+
 // Launch gate of a slot's context (bna_ctx_set_gate).
 void slot_gate(void* user, void* stream, int32_t phase, int64_t done) {
   Slot* s = static_cast<Slot*>(user);
@@ -219,15 +223,10 @@ void slot_gate(void* user, void* stream, int32_t phase, int64_t done) {
     ++s->nfence;
   }
   lk.lock();
-  const bool mine_long = long_ec(s);
   auto higher = [&]() {
     for (const Slot* o : srv->slots) {
-      if (o == s || !o->busy) continue;
-      if (long_ec(o)) {
-        if (mine_long && o->seq < s->seq) return true;
-      } else if (o->work < s->work || (o->work == s->work && o->seq < s->seq)) {
-        return true;
-      }
+      if (o == s || !o->busy || long_ec(o)) continue;
+      if (o->work < s->work || (o->work == s->work && o->seq < s->seq)) return true;
     }
     return false;
   };
