@@ -68,6 +68,10 @@ cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const fl
                            const double* vald, long long nnz_used, const double* u,
                            const float2* uf, double* un, float2* unf, double* parts, void* st,
                            int grid, int max_iter, double eps, cudaStream_t stream);
+cudaError_t launch_ec_iter_sparse(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                           const double* vald, long long nnz_used, const double* u,
+                           const float2* uf, double* un, float2* unf, double* parts, void* st,
+                           int grid, int max_iter, double eps, cudaStream_t stream);
 void ec_state_read(const void* host_copy, double* lam2, double* lambda_used, double* e1,
                    double* e2, int* iter, int* done);
 int ec_state_err(const void* host_copy);

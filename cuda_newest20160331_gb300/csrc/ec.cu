@@ -267,6 +267,84 @@ __device__ __forceinline__ void ec_block_rows(int n, const int32_t* __restrict__
   }
 }
 
+// The same iteration's work for a sparse graph (average degree <= 2, the
+// graphs whose centrality converges slowly or never): one thread per row
+// (the epilogue's row), its few entries summed in order in float-float, so a
+// warp does not walk ~20 nearly empty rows one after another; a row of more
+// than kEcSparseRow entries is summed by the whole warp as above.
+constexpr int kEcSparseRow = 32;
+
+template <int VK>
+__device__ __forceinline__ void ec_block_rows_sparse(int n, const int32_t* __restrict__ rp,
+                                                     const int32_t* __restrict__ ci,
+                                                     const float* __restrict__ val,
+                                                     const double* __restrict__ vald,
+                                                     long long nnz_used, const double* uc,
+                                                     const float2* ufc, double* un, float2* unf,
+                                                     double inv, double& a0, double& a1,
+                                                     double& a2) {
+  constexpr int kW = kEcThreads / 32;
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * kW;
+  const int k = threadIdx.x / kW, w = threadIdx.x % kW;
+  for (long long base = (long long)blockIdx.x * kW; base < n; base += (long long)kEcRounds * nw) {
+    const long long row = base + (long long)k * nw + w;
+    long long b = 0, e = 0;
+    if (row < n) {
+      b = __ldg(rp + row);
+      e = __ldg(rp + row + 1);
+      if (e > nnz_used) e = nnz_used;
+      if (b > e) b = e;
+    }
+    float sh = 0.0f, sl = 0.0f;
+    const bool wide = e - b > kEcSparseRow;
+    if (!wide) {
+#pragma unroll 4
+      for (long long q = b; q < e; ++q) {
+        float vh = 1.0f, vl = 0.0f;
+        if (VK == 1) vh = __ldg(val + q);
+        if (VK == 2) {
+          const float2 d = split_df(__ldg(vald + q));
+          vh = d.x;
+          vl = d.y;
+        }
+        df_accum<VK>(sh, sl, vh, vl, ufc[__ldg(ci + q)]);
+      }
+    }
+    // wide rows: the warp sums each of them together (every lane takes part)
+    for (unsigned m = __ballot_sync(0xffffffffu, wide); m; m &= m - 1) {
+      const int src = __ffs(m) - 1;
+      const long long wb = __shfl_sync(0xffffffffu, b, src), we = __shfl_sync(0xffffffffu, e, src);
+      float wh = 0.0f, wl = 0.0f;
+      ec_row_accum<VK>(ci, val, vald, ufc, wb, we, lane, wh, wl, false);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, wh, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, wl, o);
+        float s2, e2;
+        two_sum(wh, oh, s2, e2);
+        wh = s2;
+        wl = __fadd_rn(wl, __fadd_rn(ol, e2));
+      }
+      if (lane == src) {
+        sh = wh;
+        sl = wl;
+      }
+    }
+    if (row < n) {
+      // as ec_block_rows: a row without entries gives 0 (weighted-net.cu:160-167)
+      const double y = e <= b ? 0.0 : ((double)sh + (double)sl) * inv;
+      const double old = uc[row];
+      un[row] = y;
+      unf[row] = split_df(y);
+      a0 += y * y;
+      const double d = y - old, p = y + old;
+      a1 += d * d;
+      a2 += p * p;
+    }
+  }
+}
+
 // Block sums of the three partials (warp butterflies over the first aw warps,
 // then a butterfly over the warps' sums in warp 0) into parts[blockIdx.x * 3 ..].
 __device__ __forceinline__ void ec_block_partials(double a0, double a1, double a2, int aw,
@@ -306,7 +384,8 @@ __device__ __forceinline__ void ec_block_partials(double a0, double a1, double a
 }
 
 // VK: 0 binary (val NULL), 1 float values, 2 double values (split into a float pair).
-template <int VK>
+// SPARSE: rows by ec_block_rows_sparse.
+template <int VK, bool SPARSE = false>
 __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
     int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
     const float* __restrict__ val, const double* __restrict__ vald, long long nnz_used,
@@ -325,7 +404,10 @@ __global__ __launch_bounds__(kEcThreads, 4) void ec_iter_kernel(
   const double lam = lam_s[0];
   const double inv = lam_s[1];
   double a0 = 0, a1 = 0, a2 = 0;
-  ec_block_rows<VK>(n, rp, ci, val, vald, nnz_used, u, uf, un, unf, inv, false, a0, a1, a2);
+  if (SPARSE)
+    ec_block_rows_sparse<VK>(n, rp, ci, val, vald, nnz_used, u, uf, un, unf, inv, a0, a1, a2);
+  else
+    ec_block_rows<VK>(n, rp, ci, val, vald, nnz_used, u, uf, un, unf, inv, false, a0, a1, a2);
   ec_block_partials(a0, a1, a2, kEcThreads / 32, parts);
   if (last_block_arrives(st)) {
     __shared__ double tot[3];
@@ -871,6 +953,24 @@ cudaError_t launch_ec_iter(int n, const int32_t* rp, const int32_t* ci, const fl
   else
     ec_iter_kernel<0><<<grid, kEcThreads, 0, stream>>>(n, rp, ci, val, vald, nnz_used, u, uf, un,
                                                        unf, parts, (EcState*)st, max_iter, eps);
+  return cudaGetLastError();
+}
+
+// launch_ec_iter for a graph of average degree <= 2 (rows by thread).
+cudaError_t launch_ec_iter_sparse(int n, const int32_t* rp, const int32_t* ci, const float* val,
+                                  const double* vald, long long nnz_used, const double* u,
+                                  const float2* uf, double* un, float2* unf, double* parts,
+                                  void* st, int grid, int max_iter, double eps,
+                                  cudaStream_t stream) {
+  if (val)
+    ec_iter_kernel<1, true><<<grid, kEcThreads, 0, stream>>>(
+        n, rp, ci, val, vald, nnz_used, u, uf, un, unf, parts, (EcState*)st, max_iter, eps);
+  else if (vald)
+    ec_iter_kernel<2, true><<<grid, kEcThreads, 0, stream>>>(
+        n, rp, ci, val, vald, nnz_used, u, uf, un, unf, parts, (EcState*)st, max_iter, eps);
+  else
+    ec_iter_kernel<0, true><<<grid, kEcThreads, 0, stream>>>(
+        n, rp, ci, val, vald, nnz_used, u, uf, un, unf, parts, (EcState*)st, max_iter, eps);
   return cudaGetLastError();
 }
 

@@ -70,6 +70,14 @@ int32_t bna_csr_rethreshold(bna_ctx* ctx, const bna_csr* in_dev, int32_t mode, d
 // per-iteration kernel and 93 us chunked).
 constexpr int kEcChunkMax = 4;
 constexpr double kEcChunkFresh = 0.6;
+// ... and at least this many entries per row on average: every block stages
+// the whole iterate each iteration, which a sparse graph's few gathers do not
+// repay (graphs of a few hundred edges on 50,665 and 94,939 vertices took 33
+// and 55 us per iteration chunked, one on 168,220 vertices 33 us unchunked)
+constexpr long long kEcChunkMinDeg = 8;
+// Graphs of at most this many entries per row on average (those whose
+// centrality converges slowly or never) sum their rows a thread per row.
+constexpr long long kEcSparseDeg = 2;
 
 static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci, const float* val,
                       const double* vald, long long nnz, int max_iter, double eps, double* ec_dev,
@@ -135,7 +143,9 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
   // gathers have little locality (most entries in a sector of their own:
   // clustered graphs hit L1 with the per-iteration kernel and run faster there)
   const int nch = ec_chunk_count(n);
-  bool chunked = nch >= 1 && nch <= kEcChunkMax && nnz_used > 0;
+  bool chunked = nch >= 1 && nch <= kEcChunkMax && nnz_used > 0 &&
+                 nnz_used >= kEcChunkMinDeg * (long long)n;
+  const bool sparse = nnz_used <= kEcSparseDeg * (long long)n;
   int* csplit = nullptr;
   int* rowsplit = nullptr;
   float2* part = nullptr;
@@ -170,6 +180,9 @@ static int32_t ec_run(bna_ctx* ctx, int n, const int32_t* rp, const int32_t* ci,
       if (chunked)
         launch_ec_chunk(n, rp, ci, val, vald, nnz_used, u + cur, uf + cur, u + nxt, uf + nxt,
                         parts, state, cgrid_rows, max_iter, eps, rowsplit, csplit, part, cap);
+      else if (sparse)
+        launch_ec_iter_sparse(n, rp, ci, val, vald, nnz_used, u + cur, uf + cur, u + nxt,
+                              uf + nxt, parts, state, grid, max_iter, eps, cap);
       else
         launch_ec_iter(n, rp, ci, val, vald, nnz_used, u + cur, uf + cur, u + nxt, uf + nxt,
                        parts, state, grid, max_iter, eps, cap);

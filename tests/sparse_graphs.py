@@ -50,3 +50,23 @@ def random_graph(n, deg, seed):
     R = np.zeros(n + 1, np.int32)
     np.add.at(R, rows + 1, 1)
     return np.cumsum(R).astype(np.int32), cols, vals
+
+
+def sparse_hub_graph(n, pairs, hub, seed):
+    """Symmetric graph of `pairs` random pairs plus vertex 0 joined to vertices
+    1..hub (a row of `hub` entries), columns ascending, values in (0, 1)."""
+    rng = np.random.default_rng(seed)
+    i = np.concatenate([rng.integers(0, n, pairs), np.zeros(hub, np.int64)])
+    j = np.concatenate([rng.integers(0, n, pairs), np.arange(1, hub + 1)])
+    keep = i != j
+    i, j = i[keep], j[keep]
+    w = rng.uniform(0.05, 1.0, len(i)).astype(np.float32)
+    rows = np.concatenate([i, j])
+    cols = np.concatenate([j, i])
+    vals = np.concatenate([w, w])
+    key = rows.astype(np.int64) * n + cols
+    key, first = np.unique(key, return_index=True)
+    rows, cols, vals = (key // n).astype(np.int32), (key % n).astype(np.int32), vals[first]
+    R = np.zeros(n + 1, np.int32)
+    np.add.at(R, rows + 1, 1)
+    return np.cumsum(R).astype(np.int32), cols, vals

@@ -12,6 +12,7 @@ import pytest
 import cuda_newest20160331_gb300 as bna
 import oracle
 from sparse_graphs import SPARSE_CASES, random_graph as _random_graph, sparse_graphs
+from sparse_graphs import sparse_hub_graph
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -470,6 +471,27 @@ def test_ec_large_graph_matches_oracle(builder, n, unsorted):
     ec, lam, it, _ = builder.ec(csr)
     assert it == it_o
     assert np.max(np.abs(ec.cpu().numpy() - ec_o)) <= 1e-9 * np.max(np.abs(ec_o))
+
+
+@pytest.mark.parametrize("hub", [0, 600])
+def test_ec_sparse_large_graph_matches_oracle(builder, hub):
+    """Graphs above the persistent kernel's size with at most two entries per
+    row on average (the graphs whose centrality converges slowly or never)
+    sum their rows a thread per row; a row of 600 entries is summed by its
+    warp.  300 iterations (neither side converges), weighted and binary:
+    iterations, status and values against the FP64 oracle."""
+    R, C, V = sparse_hub_graph(40000, 30000, hub, 17)
+    assert len(C) <= 2 * (len(R) - 1)
+    for vals in (V, None):
+        ec_o, lam_o, it_o, conv_o = oracle.ec(R, C, None if vals is None else vals.astype(np.float64),
+                                              max_iter=300)
+        csr = bna.CsrResult(len(R) - 1, len(C), dev(R), dev(C),
+                            None if vals is None else dev(vals), {})
+        ec, lam, it, conv = builder.ec(csr, max_iter=300)
+        ec = ec.cpu().numpy()
+        assert conv == conv_o and it == it_o, (it, it_o)
+        assert np.max(np.abs(ec - ec_o)) <= 1e-9 * np.max(np.abs(ec_o))
+        assert abs(lam - lam_o) <= 1e-9 * abs(lam_o)
 
 
 @pytest.mark.parametrize("n", [7, 20000])
