@@ -68,6 +68,15 @@ __device__ __forceinline__ void put_edge32(const CorrArgs& a, int pos, int col, 
   if (a.weighted) a.val[pos] = v;
 }
 
+// popc_before4 of a 16-byte-aligned row of four mask words, read in one load
+__device__ __forceinline__ int popc_before4v(const uint32_t* m, int pos) {
+  const uint4 v = *reinterpret_cast<const uint4*>(m);
+  const int w = pos >> 5;
+  const uint32_t low = (1u << (pos & 31)) - 1u;
+  return __popc(w == 0 ? v.x & low : v.x) + (w >= 1 ? __popc(w == 1 ? v.y & low : v.y) : 0) +
+         (w >= 2 ? __popc(w == 2 ? v.z & low : v.z) : 0) + (w == 3 ? __popc(v.w & low) : 0);
+}
+
 __device__ __forceinline__ int popc_before4(const uint32_t* m, int pos) {
   const int w = pos >> 5;
   int c = __popc(m[w] & ((1u << (pos & 31)) - 1u));
@@ -177,7 +186,8 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
 #pragma unroll
     for (int k = 0; k < 4; ++k) tbase[w][lane + 32 * k] = rp_s[lane + 32 * k] + nsg[w][lane + 32 * k];
     // entry e of quadrant q is elist[b[q] + e] for p[q] <= e < p[q + 1]
-    long long b[4], p1 = 0, p2 = 0, p3 = 0, E = 0;
+    long long b[4], E = 0;
+    int p1 = 0, p2 = 0, p3 = 0;  // a sub-tile placed here has at most kFillDenseE entries
     bool inside = true;  // ranges written while the pool overflowed are not read
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -186,12 +196,13 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
       inside &= ct >= 0 && st >= 0 && st + ct <= a.ecap;
       b[q] = st - E;
       E += ct;
-      if (q == 0) p1 = E;
-      if (q == 1) p2 = E;
-      if (q == 2) p3 = E;
+      if (q == 0) p1 = (int)E;
+      if (q == 1) p2 = (int)E;
+      if (q == 2) p3 = (int)E;
     }
     const bool use = inside && E != 0 && E <= kFillDenseE;  // else flagged / the dense pass's
-    auto load = [&](long long e) {
+    const int Ei = use ? (int)E : 0;
+    auto load = [&](int e) {
       return a.elist[e + (e < p1 ? b[0] : e < p2 ? b[1] : e < p3 ? b[2] : b[3])];
     };
     // candidate bit resolved: bit 15 set = not an edge, .y = the value to store
@@ -206,13 +217,13 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
       }
       return en;
     };
-    const int kmax = use ? (int)min((E + 31) / 32, (long long)kFillKeep) : 0;
+    const int kmax = min((Ei + 31) / 32, kFillKeep);
     uint2 keep[kFillKeep];
 #pragma unroll
     for (int k = 0; k < kFillKeep; ++k) {
-      const long long e = lane + 32 * k;
+      const int e = lane + 32 * k;
       keep[k] = make_uint2(1u << 15, 0u);
-      if (k < kmax && e < E) keep[k] = k < kFillStage / 32 ? ent[w][e] : load(e);
+      if (k < kmax && e < Ei) keep[k] = k < kFillStage / 32 ? ent[w][e] : load(e);
     }
     __syncwarp();  // the staged data read by every lane before the next copies land
     if (J + kFillWarps < j1) {
@@ -245,16 +256,19 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
 #pragma unroll
     for (int k = 0; k < kFillKeep; ++k)
       if (k < kmax) mark(keep[k]);
-    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) mark(resolve(load(e)));
+    for (int e = lane + 32 * kFillKeep; e < Ei; e += 32) mark(resolve(load(e)));
     __syncwarp();
     // 2. segment bases of the block's rows for column block J (on the
     // diagonal the transposed entries, columns < the row, come first)
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int r = lane + 32 * k;
-      dbase[w][r] = diag ? tbase[w][r] + __popc(tm[r][0]) + __popc(tm[r][1]) + __popc(tm[r][2]) +
-                               __popc(tm[r][3])
-                         : tbase[w][r];
+      if (diag) {
+        const uint4 c = *reinterpret_cast<const uint4*>(tm[r]);
+        dbase[w][r] = tbase[w][r] + __popc(c.x) + __popc(c.y) + __popc(c.z) + __popc(c.w);
+      } else {
+        dbase[w][r] = tbase[w][r];
+      }
     }
     __syncwarp();
     // 3. place this block's entries: direct (row il) and transposed (row jl)
@@ -262,13 +276,13 @@ __global__ __launch_bounds__(kFillWarps * 32, 4) void csr_fill_rows_kernel(CorrA
       if ((en.x >> 15) & 1u) return;
       const int il = en.x & 127, jl = (en.x >> 7) & 127;
       const float val = __uint_as_float(en.y);
-      if (!trans) put_edge32(a, dbase[w][il] + popc_before4(rm[il], jl), hi * 128 + jl, val);
-      if (trans || diag) put_edge32(a, tbase[w][jl] + popc_before4(tm[jl], il), lo * 128 + il, val);
+      if (!trans) put_edge32(a, dbase[w][il] + popc_before4v(rm[il], jl), hi * 128 + jl, val);
+      if (trans || diag) put_edge32(a, tbase[w][jl] + popc_before4v(tm[jl], il), lo * 128 + il, val);
     };
 #pragma unroll
     for (int k = 0; k < kFillKeep; ++k)
       if (k < kmax) place(keep[k]);
-    for (long long e = lane + 32 * kFillKeep; e < E; e += 32) place(resolve(load(e)));
+    for (int e = lane + 32 * kFillKeep; e < Ei; e += 32) place(resolve(load(e)));
     __syncwarp();
   }
   cp_async_wait_all();  // nothing in flight into shared memory at exit
