@@ -16,7 +16,7 @@ and TF32 forms on the same input and reports max |r - r_fp64| of each form.
 The line's "serve" object is a serving sample: R requests (default 120) with
 Poisson arrivals at 4/s through bna_server (continuous admission by HBM
 budget), latency p50/p99 and each request's slowdown against running alone.
---workload serving runs the full 1,000-request case and prints its own line.
+--workload serving runs the full case (R default 1,000) and prints its own line.
 
 --gpus N > 1 runs under torchrun: every rank builds its own replica of the
 workload (the path has no cross-GPU exchange: replicas only), barrier + max
@@ -56,7 +56,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--modularity", default="auto", choices=["auto", "on", "off"],
                    help="Newman modularity of the step's CSR (auto: N <= 100,000)")
-    p.add_argument("--serve-requests", type=int, default=120)
+    p.add_argument("--serve-requests", type=int, default=None,
+                   help="serving requests (default 120 in the line, 1,000 for --workload serving)")
     p.add_argument("--serve-slots", type=int, default=4)
     p.add_argument("--serve-budget-gb", type=float, default=160.0)
     p.add_argument("--serve-dump", default="", help="write per-request records (JSON) here")
@@ -560,7 +561,7 @@ def main():
                               "higher_is_better": True, "n_gpus": 1, "batch": bt}), flush=True)
         return
     if args.workload == "serving":
-        sv = serve_run(1000 if args.serve_requests == 120 else args.serve_requests,
+        sv = serve_run(1000 if args.serve_requests is None else args.serve_requests,
                        slots=args.serve_slots, dump=args.serve_dump,
                        budget=int(args.serve_budget_gb * 2**30))
         if rank == 0:
@@ -572,8 +573,9 @@ def main():
     # another (a builder context and its arena from the measurements below
     # would share the device with them)
     serve = None
-    if rank == 0 and args.serve_requests > 0:
-        serve = serve_run(args.serve_requests, slots=args.serve_slots, dump=args.serve_dump,
+    n_serve = 120 if args.serve_requests is None else args.serve_requests
+    if rank == 0 and n_serve > 0:
+        serve = serve_run(n_serve, slots=args.serve_slots, dump=args.serve_dump,
                        budget=int(args.serve_budget_gb * 2**30))
     w = workloads.get(args.workload)
     precision = args.precision
